@@ -1,0 +1,379 @@
+"""Benchmark: direct-sum gravity + verlet at N = 1,048,580 on GB300.
+
+One step = one pipeline step of physim with the simple_astro element and the
+verlet integrator over 1,048,576 cube bodies + 4 stars (e = 0.01, dt = 1e-5):
+N(N-1) pair interactions plus the f64 kick-drift.  Prints one JSON line.
+
+  value     Gpair-interactions/s of the device-resident path (state in HBM;
+            CUDA events on the simulation's stream around each step, L2
+            flushed between timed steps).
+  e2e       the same metric through the plugin C ABI with host Entity arrays:
+            simple_astro_transform + physim_gpu_verlet_integrate per step,
+            host<->device copies inside the timed region (wall clock).
+  roofline  the pair kernel against the FP32 peak: 20 flop per pair
+            (Nyland, Harris & Prins, GPU Gems 3 ch. 31) / event time, peak =
+            SMs x 128 FP32 lanes x 2 x max SM clock.
+  cpu_baseline  the C restatement of the reference (single thread, as physim's
+            transform runs) on a bounded sample of bodies.
+
+--impl reference times the reference algorithm's CPU implementation (the C
+restatement, the Rust reference cannot be built here) on all host cores.
+Under torchrun every rank runs an independent replica (the path has no
+exchange step); value is the sum of the ranks' pairs over the slowest rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_CUBE = 1_048_576
+E = 0.01
+DT = 1e-5
+FLOP_PER_PAIR = 20
+FP32_LANES_PER_SM = 128
+METRIC = "Gpair-interactions/s at N=1M (direct-sum simple_astro + verlet)"
+WORKLOAD = "direct-sum N=1,048,580 (1,048,576 cube U[-0.5,0.5]^3 seed 1 + 4 stars m=1e5), e=0.01, verlet dt=1e-5"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--cpu-seconds", type=float, default=12.0,
+                   help="target seconds of CPU work for the CPU-baseline sample")
+    p.add_argument("--e2e-steps", type=int, default=None)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--skip-e2e", action="store_true", help="profiling runs: device path only")
+    p.add_argument("--bodies", type=int, default=N_CUBE,
+                   help="cube bodies (profiling of smaller cases; the reported workload is "
+                        "the default 1,048,576)")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas only)
+# ---------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            backend = "nccl" if _cuda_ok() else "gloo"
+            dist.init_process_group(backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        return self._reduce(v, "max")
+
+    def sum(self, v: float) -> float:
+        return self._reduce(v, "sum")
+
+    def _reduce(self, v, op):
+        if not self.pg:
+            return v
+        import torch
+        dev = torch.device("cuda", self.local) if _cuda_ok() else torch.device("cpu")
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX if op == "max" else self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def _cuda_ok() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except FileNotFoundError:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        rows = []
+        for ln in out.strip().splitlines():
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append({"sm": float(parts[1]), "max": float(parts[2]),
+                             "power": float(parts[3]) if parts[3] not in ("[N/A]", "") else 0.0,
+                             "hw": parts[5], "hwt": parts[6], "swt": parts[7], "cap": parts[8]})
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        sm_max = max(r["max"] for r in rows)
+        loaded = [r for r in rows if r["power"] > 200.0] or rows
+        reasons = set()
+        for r in rows:
+            for key, name in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"),
+                              ("swt", "sw_thermal_slowdown"), ("cap", "sw_power_cap")):
+                if r[key].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r["sm"] for r in loaded), "sm_max_mhz": sm_max,
+                "samples": len(rows), "reasons": sorted(reasons)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            pass
+    return {}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the C restatement on a bounded sample
+# ---------------------------------------------------------------------------
+def cpu_sample_rate(state, threads: int, target_s: float) -> dict:
+    import oracle
+    n = len(state)
+    rng = np.random.default_rng(123)
+    k = 8
+    t_per = None
+    while True:
+        idx = rng.choice(n, k, replace=False)
+        t0 = time.perf_counter()
+        oracle.simple_astro_sample(state, E, idx, threads=threads)
+        dt = time.perf_counter() - t0
+        if dt > 0.5 or k >= n:
+            t_per = dt / k
+            break
+        k = min(n, k * 4)
+    k = int(min(n, max(k, target_s / max(t_per, 1e-9))))
+    idx = rng.choice(n, k, replace=False)
+    t0 = time.perf_counter()
+    oracle.simple_astro_sample(state, E, idx, threads=threads)
+    dt = time.perf_counter() - t0
+    pairs = k * (n - 1)
+    return {"value": pairs / dt / 1e9, "unit": "Gpair-interactions/s", "cores": threads,
+            "seconds": dt,
+            "sample": f"{k} bodies x {n - 1} partners of the {n}-body workload (f64 C "
+                      f"restatement of simple_astro, transformers.rs:219-244)"}
+
+
+def run_reference(args, dist: Dist):
+    if dist.rank != 0:
+        return
+    import oracle
+    from physim_gb300 import ics
+    state = ics.workload_large(N_CUBE)
+    threads = oracle.load().oracle_max_threads()
+    per_step = max(args.cpu_seconds / 3.0, 1.0)
+    for _ in range(args.warmup):
+        cpu_sample_rate(state, threads, per_step / 4)
+    vals = [cpu_sample_rate(state, threads, per_step) for _ in range(args.steps)]
+    value = statistics.median(v["value"] for v in vals)
+    n = len(state)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gpair-interactions/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": n * (n - 1) / (value * 1e9) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD,
+                   "implementation": "C restatement of physim's simple_astro (oracle/, OpenMP "
+                                     "over bodies); the Rust reference needs cargo, absent here",
+                   "per_step_sample": vals[0]["sample"]},
+        "cpu_baseline": {"value": value, "unit": "Gpair-interactions/s", "cores": threads,
+                         "kind": "port", "sample": vals[0]["sample"]},
+        "e2e": {"value": value, "unit": "Gpair-interactions/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args, dist: Dist):
+    import torch
+
+    import physim_gb300 as pg
+    from physim_gb300 import ics
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    device = dist.local
+    torch.cuda.set_device(device)
+    state = ics.workload_large(args.bodies)
+    n = len(state)
+    pairs_step = n * (n - 1) - 0  # no fixed bodies in this workload
+    props = torch.cuda.get_device_properties(device)
+    sms = props.multi_processor_count
+    peaks = measured_peaks()
+    stream = torch.cuda.Stream(device=device)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+
+    sim = pg.Simulation(state, pg.SimConfig(gravity="simple_astro", e=E, dt=DT, device=device,
+                                            stream=stream.cuda_stream))
+    sim.set_profiling(True)
+    with torch.cuda.stream(stream):
+        sim.step(args.warmup)
+    sim.synchronize()
+
+    clocks = Clocks(device)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    grav_ms = []
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall = time.perf_counter()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()  # L2 flush between timed steps (outside the events)
+            starts[k].record(stream)
+            sim.step(1)
+            ends[k].record(stream)
+        g, _ = sim.last_step_ms()
+        grav_ms.append(g)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall
+    dist.barrier()
+    clk = clocks.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = dist.max(sum(step_ms))
+    all_pairs = dist.sum(float(pairs_step * args.steps))
+    value = all_pairs / (total_ms / 1e3) / 1e9
+    ms_per_step = total_ms / args.steps
+    launches = sim.launches_per_step * args.steps
+    sim.close()
+
+    # kernel roofline (pair kernel only)
+    kern_ms = statistics.mean(grav_ms)
+    achieved_tflops = FLOP_PER_PAIR * pairs_step / (kern_ms / 1e3) / 1e12
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    peak_tflops = sms * FP32_LANES_PER_SM * 2 * sm_max * 1e6 / 1e12
+    traffic = None
+    tfile = ROOT / "profiles" / "direct_forces_traffic.json"
+    if tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get("bytes_per_launch")
+        except ValueError:
+            traffic = None
+
+    # e2e through the plugin C ABI with host arrays
+    e2e = None
+    if not args.skip_e2e:
+        e2e_steps = args.e2e_steps or max(2, min(args.steps, 3))
+        el = pg.TransformElementHandler("simple_astro", {"e": E, "device": device})
+        verlet = pg.GpuVerlet(device)
+        cur = state.copy()
+        acc = pg.accelerations(n)
+        el.transform(cur, acc)  # warm: allocations and module load
+        times = []
+        for _ in range(e2e_steps):
+            t0 = time.perf_counter()
+            acc = np.zeros(n, dtype=pg.ACCELERATION)
+            el.transform(cur, acc)
+            cur = verlet.integrate(cur, acc, DT)
+            times.append(time.perf_counter() - t0)
+        el.destroy()
+        verlet.close()
+        t_e2e = dist.max(sum(times))
+        e2e = {"value": dist.sum(float(pairs_step * e2e_steps)) / t_e2e / 1e9,
+               "unit": "Gpair-interactions/s",
+               "h2d_bytes_per_step": n * (80 + 24) + n * (80 + 24),
+               "d2h_bytes_per_step": n * 24 + n * 80,
+               "steps": e2e_steps,
+               "path": "simple_astro_transform + physim_gpu_verlet_integrate on host Entity arrays"}
+
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_sample_rate(state, 1, args.cpu_seconds)
+        cpu.pop("seconds", None)
+        cpu["kind"] = "port"
+
+    if dist.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gpair-interactions/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32 pairs, f64 integration", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "bodies": n, "pairs_per_step": pairs_step,
+                       "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU",
+                       "l2": "flushed between timed steps (256 MiB write, outside the events)",
+                       "compensated_sums": True, "wall_s": wall},
+            "roofline": {"bound": "fp32", "kernel": "direct_forces_kernel",
+                         "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",
+                         "frac": achieved_tflops / peak_tflops, "traffic": traffic,
+                         "peak_basis": f"{sms} SMs x {FP32_LANES_PER_SM} FP32 lanes x 2 x "
+                                       f"{sm_max:.0f} MHz (max SM clock of measured peaks)",
+                         "flop_per_pair": FLOP_PER_PAIR, "kernel_ms": kern_ms},
+            "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu,
+        }
+        if clk:
+            line["clocks"] = clk
+            if clk.get("sm_mhz"):
+                line["roofline"]["frac_at_observed_clock"] = achieved_tflops / (
+                    sms * FP32_LANES_PER_SM * 2 * clk["sm_mhz"] * 1e6 / 1e12)
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

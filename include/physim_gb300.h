@@ -1,0 +1,272 @@
+/*
+ * physim_gb300.h -- C ABI of libphysim_gb300.so, a GB300 (sm_103a) build of
+ * physim's gravity + integration hot path.
+ *
+ * Two front doors:
+ *
+ *  1. A drop-in physim *transform plugin*.  The library exports exactly the
+ *     symbols that physim's plugin loader binds for a C plugin
+ *     (physim-core/src/plugin/discover.rs:327-373, plugin/transform.rs:32-104,
+ *     c_plugin/plugin.c:133-284), for the three gravity elements of the astro
+ *     crate: `astro` (quadtree Barnes-Hut), `astro2` (octree Barnes-Hut) and
+ *     `simple_astro` (direct sum), astro/src/transformers.rs:16-271.  Element
+ *     names, properties (`theta`, `e`) and the Entity layout are unchanged, so
+ *     pipeline TOML files and CLI strings load it unchanged.
+ *
+ *  2. A device-resident C API (physim_gpu_*): the verlet integrator
+ *     (integrators/src/verlet.rs) over host arrays, and simulations whose
+ *     state stays in HBM between steps.
+ *
+ * Types below have the layout of c_plugin/physim.h:6-94 (same type names;
+ * enum constants carry a PHYSIM_ prefix).  All functions are thread-compatible:
+ * one call at a time per object, as physim's pipeline does.
+ */
+#ifndef PHYSIM_GB300_H
+#define PHYSIM_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------------------- */
+/* Types shared with physim (c_plugin/physim.h)                             */
+/* ----------------------------------------------------------------------- */
+
+/* physim-core/src/plugin/meta.rs ElementKind (c_plugin/physim.h:6-13) */
+typedef enum ElementKind {
+    PHYSIM_KIND_INITIALISER = 0,
+    PHYSIM_KIND_TRANSFORM = 1,
+    PHYSIM_KIND_RENDER = 2,
+    PHYSIM_KIND_SYNTH = 3,
+    PHYSIM_KIND_TRANSMUTE = 4,
+    PHYSIM_KIND_INTEGRATOR = 5
+} ElementKind;
+
+/* physim-core/src/messages.rs:29-36 -- messages posted from C must say C. */
+typedef enum MessageOrigin { PHYSIM_ORIGIN_RUST = 0, PHYSIM_ORIGIN_C = 1 } MessageOrigin;
+
+/* physim-core/src/messages.rs:11-19 */
+typedef enum MessagePriority {
+    PHYSIM_PRIORITY_BACKGROUND = 0,
+    PHYSIM_PRIORITY_LOW = 1,
+    PHYSIM_PRIORITY_NORMAL = 2,
+    PHYSIM_PRIORITY_HIGH = 3,
+    PHYSIM_PRIORITY_REALTIME = 4,
+    PHYSIM_PRIORITY_CRITICAL = 5
+} MessagePriority;
+
+/* physim-core/src/messages.rs:38-46 */
+typedef struct CMessage {
+    MessagePriority priority;
+    const char *topic;
+    const char *message;
+    uintptr_t sender_id;
+    MessageOrigin origin;
+} CMessage;
+
+/* physim-core/src/lib.rs:16-29: 80 bytes, id at 64, fixed at 72. */
+typedef struct Entity {
+    double x;
+    double y;
+    double z;
+    double vx;
+    double vy;
+    double vz;
+    double radius;
+    double mass;
+    uintptr_t id;
+    bool fixed;
+} Entity;
+
+/* physim-core/src/lib.rs:31-37 */
+typedef struct Acceleration {
+    double x;
+    double y;
+    double z;
+} Acceleration;
+
+/* physim-core/src/plugin/mod.rs RustStringAllocFn (host_alloc_string) */
+typedef char *(*RustStringAllocFn)(const char *);
+
+/* physim-core/src/plugin/transform.rs:32-50 (48 bytes of function pointers) */
+typedef struct TransformElementAPI {
+    void *(*init)(const uint8_t *, uintptr_t);
+    void (*transform)(const void *, const Entity *, uintptr_t, Acceleration *, uintptr_t);
+    void (*destroy)(void *);
+    char *(*get_property_descriptions)(void *, RustStringAllocFn);
+    void (*recv_message)(void *obj, const CMessage *msg);
+    void (*post_configuration_messages)(void *obj);
+} TransformElementAPI;
+
+/* physim-core/src/plugin/meta.rs:94-106 */
+typedef struct ElementMetaFFI {
+    ElementKind kind;
+    char *name;
+    char *plugin;
+    char *version;
+    char *license;
+    char *author;
+    char *blurb;
+    char *repo;
+} ElementMetaFFI;
+
+/* ----------------------------------------------------------------------- */
+/* 1. Plugin discovery (physim-core/src/plugin/discover.rs:327-373,         */
+/*    physim-core/src/plugin/mod.rs:118-160, c_plugin/plugin.c:133-147)     */
+/* ----------------------------------------------------------------------- */
+
+/* Returns "C": physim then skips its rustc-version check (discover.rs:345). */
+const char *get_plugin_abi_info(void);
+/* Returns "astro,astro2,simple_astro" (discover.rs:362-371). */
+const char *register_plugin(void);
+/* Stores physim's message-bus pointer (plugin/mod.rs:234-244).  The library
+ * resolves physim's `post_bus_callback` (messages.rs:201-226) at run time. */
+void set_callback_target(void *target);
+
+/* ----------------------------------------------------------------------- */
+/* 1a. Transform elements.  Each set replaces the symbols that             */
+/*     physim-attribute/src/lib.rs:39-202 generates for the element:        */
+/*       astro2       -> AstroOctreeElement  astro/src/transformers.rs:114-203
+ *       astro        -> AstroElement        astro/src/transformers.rs:16-112
+ *       simple_astro -> SimpleAstroElement  astro/src/transformers.rs:205-271
+ *
+ *  init(json, len): a JSON object (not NUL-terminated).  Keys read:
+ *    theta  (astro, astro2; default 1.0), e (all; absolute value; default 1.0)
+ *  and, for this build only (ignored by the reference, so TOML stays valid):
+ *    leaf_size  (astro, astro2; bodies per tree leaf, 1..64; default 1 = the
+ *                reference's tree)
+ *    traversal  ("exact": each body uses its own reference interaction list,
+ *                the default; "warp": a cell is accepted only when every body
+ *                of a 32-body warp accepts it)
+ *    device     (CUDA device ordinal, default 0)
+ *  Returns NULL for text that is not a JSON object (transform.rs:72-76).  It
+ *  does not touch the GPU; the CUDA context is created by the first transform.
+ *
+ *  transform(obj, state, n, acc, n_acc): acc[i] += a_i for every non-fixed
+ *  body i, as the reference does.  On a CUDA error or n_acc < n the library
+ *  prints the reason to stderr and aborts, which is what the reference's
+ *  catch_unwind wrapper does on a panic (physim-attribute/src/lib.rs:94-97).
+ * ----------------------------------------------------------------------- */
+const TransformElementAPI *astro2_get_api(void);
+ElementMetaFFI astro2_register(RustStringAllocFn alloc);
+void *astro2_init(const uint8_t *config, uintptr_t len);
+void astro2_transform(const void *obj, const Entity *state, uintptr_t state_len,
+                      Acceleration *acceleration, uintptr_t acceleration_len);
+void astro2_destroy(void *obj);
+char *astro2_get_property_descriptions(void *obj, RustStringAllocFn alloc);
+void astro2_recv_message(void *obj, const CMessage *msg);
+void astro2_post_configuration_messages(void *obj);
+
+const TransformElementAPI *astro_get_api(void);
+ElementMetaFFI astro_register(RustStringAllocFn alloc);
+void *astro_init(const uint8_t *config, uintptr_t len);
+void astro_transform(const void *obj, const Entity *state, uintptr_t state_len,
+                     Acceleration *acceleration, uintptr_t acceleration_len);
+void astro_destroy(void *obj);
+char *astro_get_property_descriptions(void *obj, RustStringAllocFn alloc);
+void astro_recv_message(void *obj, const CMessage *msg);
+void astro_post_configuration_messages(void *obj);
+
+const TransformElementAPI *simple_astro_get_api(void);
+ElementMetaFFI simple_astro_register(RustStringAllocFn alloc);
+void *simple_astro_init(const uint8_t *config, uintptr_t len);
+void simple_astro_transform(const void *obj, const Entity *state, uintptr_t state_len,
+                            Acceleration *acceleration, uintptr_t acceleration_len);
+void simple_astro_destroy(void *obj);
+char *simple_astro_get_property_descriptions(void *obj, RustStringAllocFn alloc);
+void simple_astro_recv_message(void *obj, const CMessage *msg);
+void simple_astro_post_configuration_messages(void *obj);
+
+/* ----------------------------------------------------------------------- */
+/* 2. Device-resident C API                                                 */
+/* ----------------------------------------------------------------------- */
+
+/* Status codes returned by every physim_gpu_* function. */
+enum {
+    PHYSIM_OK = 0,
+    PHYSIM_ERR_ARGUMENT = 1, /* invalid argument (message in physim_gpu_last_error) */
+    PHYSIM_ERR_CUDA = 2,     /* a CUDA runtime call failed */
+    PHYSIM_ERR_MEMORY = 3,   /* host or device allocation failed / over budget */
+    PHYSIM_ERR_TREE = 4,     /* tree build or traversal overflowed its bounds */
+    PHYSIM_ERR_TIMEOUT = 5   /* a bounded device-side wait gave up */
+};
+
+/* Message for the last failing call on this thread ("" if none). */
+const char *physim_gpu_last_error(void);
+
+/* Gravity elements, by the reference's element names. */
+typedef enum PhysimGravity {
+    PHYSIM_GRAVITY_SIMPLE_ASTRO = 0, /* direct sum, transformers.rs:205-271 */
+    PHYSIM_GRAVITY_ASTRO2 = 1,       /* octree Barnes-Hut, transformers.rs:114-203 */
+    PHYSIM_GRAVITY_ASTRO = 2         /* quadtree Barnes-Hut, transformers.rs:16-112 */
+} PhysimGravity;
+
+typedef enum PhysimTraversal {
+    PHYSIM_TRAVERSAL_EXACT = 0, /* per-body reference interaction lists */
+    PHYSIM_TRAVERSAL_WARP = 1   /* a cell is accepted only if the whole warp accepts it */
+} PhysimTraversal;
+
+/* Settings of one device-resident simulation. */
+typedef struct PhysimSimConfig {
+    uint32_t gravity;     /* PhysimGravity */
+    uint32_t leaf_size;   /* Barnes-Hut bodies per leaf, 1..64 (1 = reference tree) */
+    uint32_t traversal;   /* PhysimTraversal */
+    uint32_t compensated; /* 1: FP32 pairs, compensated per-body sums; 0: plain FP32 sums */
+    double theta;         /* opening parameter: extent/r < theta accepts a cell */
+    double e;             /* easing factor added to r^2 (astro/src/lib.rs:95-98) */
+    double dt;            /* verlet time step */
+    void *stream;         /* cudaStream_t to run on; NULL: the simulation makes its own */
+    int32_t device;       /* CUDA device ordinal */
+    uint32_t reserved[3]; /* must be zero */
+} PhysimSimConfig;
+
+/* Fills *cfg with the reference's defaults: simple_astro, theta 1.0, e 1.0,
+ * dt 1e-6 (pipeline.rs:334), leaf 1, exact traversal, compensated sums. */
+void physim_gpu_sim_config_default(PhysimSimConfig *cfg);
+
+typedef struct PhysimSim PhysimSim;
+
+/* Allocates device state for n bodies.  Nothing is uploaded yet. */
+int physim_gpu_sim_create(const PhysimSimConfig *cfg, size_t n, PhysimSim **out);
+/* Copies the host state in and clears the verlet history, so the next step
+ * is the reference's Taylor first step (verlet.rs:24-50). */
+int physim_gpu_sim_upload(PhysimSim *sim, const Entity *state, size_t n);
+/* Enqueues `steps` pipeline steps (gravity, then verlet), asynchronously on
+ * the simulation's stream. */
+int physim_gpu_sim_step(PhysimSim *sim, uint32_t steps);
+/* Waits for the stream, then copies the current state out. */
+int physim_gpu_sim_download(PhysimSim *sim, Entity *state, size_t n);
+/* Waits, then writes the accelerations of the current state (not +=). */
+int physim_gpu_sim_accelerations(PhysimSim *sim, Acceleration *acc, size_t n);
+/* Waits for all work enqueued on the simulation's stream. */
+int physim_gpu_sim_synchronize(PhysimSim *sim);
+/* The cudaStream_t the simulation runs on. */
+void *physim_gpu_sim_stream(PhysimSim *sim);
+/* Number of kernel launches one step enqueues (for launch accounting). */
+int physim_gpu_sim_launches_per_step(PhysimSim *sim);
+/* Records CUDA events around the gravity kernels and the integrator of each
+ * step (enable != 0); physim_gpu_sim_last_step_ms waits for the last step and
+ * returns the two device times in milliseconds. */
+int physim_gpu_sim_set_profiling(PhysimSim *sim, int enable);
+int physim_gpu_sim_last_step_ms(PhysimSim *sim, double *gravity_ms, double *integrate_ms);
+void physim_gpu_sim_destroy(PhysimSim *sim);
+
+/* Verlet integrator over host arrays (integrators/src/verlet.rs:19-121).
+ * A Rust IntegratorElement shim evaluates acc_fn itself and hands the
+ * accelerations over; the step runs on the GPU in f64 in the reference's
+ * operation order, so new_state is bit-identical to the reference's. */
+typedef struct PhysimVerlet PhysimVerlet;
+int physim_gpu_verlet_create(int32_t device, PhysimVerlet **out);
+int physim_gpu_verlet_integrate(PhysimVerlet *v, const Entity *entities, Entity *new_state,
+                                size_t n, const Acceleration *acc, double dt);
+void physim_gpu_verlet_destroy(PhysimVerlet *v);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PHYSIM_GB300_H */

@@ -1,0 +1,528 @@
+/*
+ * physim_oracle.c -- CPU restatement of physim's gravity + integration hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the shipped library links, loads or
+ * calls this file.  It is the checker that the CUDA path is compared against
+ * (tests/, __graft_entry__.smoke(), and bench.py's CPU-baseline leg).
+ *
+ * Every function restates the reference algorithm in plain C with f64
+ * arithmetic, in the reference's operation order, so that the results are the
+ * ones physim computes on the same input arrays:
+ *
+ *   law             astro/src/lib.rs:84-113   (Star::newtons_law_of_universal_gravitation)
+ *   centre_of_mass  astro/src/lib.rs:40-50
+ *   fake            astro/src/lib.rs:64-76    (panics on a NaN x -> reported as status 2)
+ *   tree push       astro/src/octree.rs:59-128, astro/src/quadtree.rs:59-128
+ *   traversal       astro/src/octree.rs:130-158, astro/src/quadtree.rs:130-159
+ *   octant ids      astro/src/octree.rs:160-215, astro/src/quadtree.rs:161-194
+ *   astro2          astro/src/transformers.rs:122-160
+ *   astro           astro/src/transformers.rs:31-69
+ *   simple_astro    astro/src/transformers.rs:219-244
+ *   verlet          integrators/src/verlet.rs:24-107
+ *   pipeline step   physim-core/src/pipeline.rs:137-141,166-173
+ *
+ * Parity status: the reference is Rust and cannot be built here, and its own
+ * tests hold no force, acceleration or trajectory values.  The tree structure
+ * is pinned by the reference's leaf-count tests (ported in tests/); the force
+ * arithmetic is pinned only by analytic known-answer cases derived from the
+ * formula in astro/src/lib.rs:84-113.  Force/trajectory parity with the Rust
+ * binary itself is therefore "parity unpinned".
+ *
+ * Notes on restating Rust f64 arithmetic in C:
+ *   - x.powi(2) is x*x (LLVM lowers powi with exponent 2 to one multiply).
+ *   - x.powf(0.5) is evaluated as sqrt(x); LLVM rewrites pow(x, 0.5) to sqrt
+ *     for the finite non-negative arguments that occur here.
+ *   - Rust does not contract a*b+c into an FMA, so this file must be compiled
+ *     with -ffp-contract=off (the build recipe does so).
+ *   - f64::max ignores a NaN operand, as C's fmax does.
+ */
+#include <math.h>
+#include <stdbool.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* physim-core/src/lib.rs:16-29, c_plugin/physim.h:37-48 (80 bytes). */
+typedef struct Entity {
+    double x, y, z, vx, vy, vz, radius, mass;
+    uintptr_t id;
+    bool fixed;
+} Entity;
+
+/* physim-core/src/lib.rs:31-37 (24 bytes). */
+typedef struct Acceleration {
+    double x, y, z;
+} Acceleration;
+
+#define ORACLE_G 1.0 /* astro/src/lib.rs:27 */
+
+int oracle_sizeof_entity(void) { return (int)sizeof(Entity); }
+int oracle_sizeof_acceleration(void) { return (int)sizeof(Acceleration); }
+
+/* astro/src/lib.rs:84-113.  a = self, b = other, e = easing factor. */
+void oracle_law(const Entity *a, const Entity *b, double e, double out[3])
+{
+    double ac0 = a->x, ac1 = a->y, ac2 = a->z;
+    double bc0 = b->x, bc1 = b->y, bc2 = b->z;
+    double d0 = ac0 - bc0, d1 = ac1 - bc1, d2 = ac2 - bc2;
+    double r_norm = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    double r_easing = d0 * d0 + d1 * d1 + d2 * d2 + e;
+    double r0 = (bc0 - ac0) / r_norm;
+    double r1 = (bc1 - ac1) / r_norm;
+    double r2 = (bc2 - ac2) / r_norm;
+    double am = a->mass, bm = b->mass;
+    out[0] = r0 * ORACLE_G * am * bm / r_easing;
+    out[1] = r1 * ORACLE_G * am * bm / r_easing;
+    out[2] = r2 * ORACLE_G * am * bm / r_easing;
+}
+
+/* astro/src/lib.rs:40-50 */
+static void centre_of_mass(const Entity *self, const Entity *other, double out[3])
+{
+    double total_mass = self->mass + other->mass;
+    double inv_total_mass = 1.0 / total_mass;
+    out[0] = (self->mass * self->x + other->mass * other->x) * inv_total_mass;
+    out[1] = (self->mass * self->y + other->mass * other->y) * inv_total_mass;
+    out[2] = (self->mass * self->z + other->mass * other->z) * inv_total_mass;
+}
+
+/* astro/src/lib.rs:64-76.  Returns 0, or 2 where the reference panics. */
+static int fake(const double c[3], double mass, Entity *out)
+{
+    if (isnan(c[0])) return 2;
+    memset(out, 0, sizeof *out);
+    out->x = c[0];
+    out->y = c[1];
+    out->z = c[2];
+    out->radius = 0.0;
+    out->mass = mass;
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Pointer octree / quadtree in an index arena (astro/src/octree.rs,        */
+/* astro/src/quadtree.rs).  `nchild` is 8 for the octree, 4 for the quadtree. */
+/* ------------------------------------------------------------------------ */
+typedef struct Node {
+    double centre[3];
+    double extent;
+    int has_entity;
+    Entity entity;
+    int32_t child[8];
+} Node;
+
+typedef struct Tree {
+    int nchild;
+    Node *nodes;
+    size_t len, cap;
+} Tree;
+
+static int32_t tree_new_node(Tree *t, const double c[3], double extent)
+{
+    if (t->len == t->cap) {
+        size_t cap = t->cap ? t->cap * 2 : 64;
+        Node *p = (Node *)realloc(t->nodes, cap * sizeof(Node));
+        if (!p) return -1;
+        t->nodes = p;
+        t->cap = cap;
+    }
+    Node *n = &t->nodes[t->len];
+    memset(n, 0, sizeof *n);
+    n->centre[0] = c[0];
+    n->centre[1] = c[1];
+    n->centre[2] = c[2];
+    n->extent = extent;
+    for (int i = 0; i < 8; ++i) n->child[i] = -1;
+    return (int32_t)t->len++;
+}
+
+Tree *oracle_tree_new(int nchild, const double centre[3], double extent)
+{
+    if (nchild != 8 && nchild != 4) return NULL;
+    Tree *t = (Tree *)calloc(1, sizeof(Tree));
+    if (!t) return NULL;
+    t->nchild = nchild;
+    if (tree_new_node(t, centre, extent) != 0) {
+        free(t);
+        return NULL;
+    }
+    return t;
+}
+
+void oracle_tree_free(Tree *t)
+{
+    if (!t) return;
+    free(t->nodes);
+    free(t);
+}
+
+size_t oracle_tree_node_count(const Tree *t) { return t->len; }
+
+static int node_is_leaf(const Tree *t, const Node *n)
+{
+    for (int i = 0; i < t->nchild; ++i)
+        if (n->child[i] >= 0) return 0;
+    return 1;
+}
+
+/* octree.rs:160-165 / quadtree.rs:161-165 */
+static int octant_id(const Tree *t, const Node *n, const double p[3])
+{
+    int xb = p[0] > n->centre[0];
+    int yb = p[1] > n->centre[1];
+    if (t->nchild == 4) return xb | (yb << 1);
+    int zb = p[2] > n->centre[2];
+    return xb | (yb << 1) | (zb << 2);
+}
+
+/* octree.rs:167-215 / quadtree.rs:167-194 */
+static void octant_centre(const Tree *t, const Node *n, const double p[3], double out[3])
+{
+    int id = octant_id(t, n, p);
+    double h = n->extent / 2.0;
+    out[0] = (id & 1) ? n->centre[0] + h : n->centre[0] - h;
+    out[1] = (id & 2) ? n->centre[1] + h : n->centre[1] - h;
+    if (t->nchild == 4)
+        out[2] = n->centre[2];
+    else
+        out[2] = (id & 4) ? n->centre[2] + h : n->centre[2] - h;
+}
+
+/* octree.rs:59-128 (same body in quadtree.rs).  Returns 0 on success,
+ * 1 where the reference panics with "Recursion too deep", 2 where it panics
+ * in fake() on a NaN centre of mass, -1 on allocation failure. */
+int oracle_tree_push(Tree *t, const Entity *item_in)
+{
+    Entity item = *item_in;
+    int32_t ni = 0;
+    for (int count = 0;; ++count) {
+        if (count > 64) return 1;
+        Node *node = &t->nodes[ni];
+        if (!node->has_entity) {
+            node->entity = item;
+            node->has_entity = 1;
+            return 0;
+        }
+        Entity current = node->entity;
+        int leaf = node_is_leaf(t, node);
+        if (leaf && fabs(current.x - item.x) < 1e-9 && fabs(current.y - item.y) < 1e-9 &&
+            fabs(current.z - item.z) < 1e-9) {
+            double c[3] = {item.x, item.y, item.z};
+            Entity f;
+            if (fake(c, current.mass + item.mass, &f)) return 2;
+            node->entity = f;
+            return 0;
+        }
+        double com[3];
+        centre_of_mass(&current, &item, com);
+        Entity f;
+        if (fake(com, current.mass + item.mass, &f)) return 2;
+        node->entity = f;
+        if (leaf) {
+            double pc[3] = {current.x, current.y, current.z};
+            int idx = octant_id(t, node, pc);
+            double cc[3];
+            octant_centre(t, node, pc, cc);
+            double ext = node->extent / 2.0;
+            int32_t c = tree_new_node(t, cc, ext);
+            if (c < 0) return -1;
+            node = &t->nodes[ni]; /* realloc may move the arena */
+            t->nodes[c].entity = current;
+            t->nodes[c].has_entity = 1;
+            node->child[idx] = c;
+        }
+        double ip[3] = {item.x, item.y, item.z};
+        int idx = octant_id(t, node, ip);
+        if (node->child[idx] >= 0) {
+            ni = node->child[idx];
+            continue;
+        }
+        double cc[3];
+        octant_centre(t, node, ip, cc);
+        double ext = node->extent / 2.0;
+        int32_t c = tree_new_node(t, cc, ext);
+        if (c < 0) return -1;
+        node = &t->nodes[ni];
+        t->nodes[c].entity = item;
+        t->nodes[c].has_entity = 1;
+        node->child[idx] = c;
+        return 0;
+    }
+}
+
+/* octree.rs:130-158.  Writes at most `cap` entities to `out` (may be NULL)
+ * and returns the full length of the list. */
+size_t oracle_tree_leaves(const Tree *t, const double loc[3], double theta, Entity *out, size_t cap)
+{
+    size_t n_out = 0;
+    size_t sp = 0, scap = 256;
+    int32_t *stack = (int32_t *)malloc(scap * sizeof(int32_t));
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const Node *node = &t->nodes[stack[--sp]];
+        if (node->has_entity) {
+            double d0 = loc[0] - node->centre[0];
+            double d1 = loc[1] - node->centre[1];
+            double d2 = loc[2] - node->centre[2];
+            double r = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+            if (node->extent / r < theta) {
+                if (out && n_out < cap) out[n_out] = node->entity;
+                ++n_out;
+                continue;
+            }
+        }
+        if (!node->has_entity) continue;
+        if (node_is_leaf(t, node)) {
+            if (out && n_out < cap) out[n_out] = node->entity;
+            ++n_out;
+        } else {
+            for (int i = 0; i < t->nchild; ++i) {
+                if (node->child[i] < 0) continue;
+                if (sp == scap) {
+                    scap *= 2;
+                    stack = (int32_t *)realloc(stack, scap * sizeof(int32_t));
+                }
+                stack[sp++] = node->child[i];
+            }
+        }
+    }
+    free(stack);
+    return n_out;
+}
+
+/* The per-body force loop shared by astro / astro2 (transformers.rs:138-159)
+ * and simple_astro (transformers.rs:224-243). */
+static void accumulate_list(const Entity *a, const Entity *list, size_t len, double e, Acceleration *acc)
+{
+    double f[3] = {0.0, 0.0, 0.0};
+    for (size_t k = 0; k < len; ++k) {
+        const Entity *b = &list[k];
+        if (a->x == b->x && a->y == b->y && a->z == b->z) continue;
+        double fij[3];
+        oracle_law(a, b, e, fij);
+        f[0] += fij[0];
+        f[1] += fij[1];
+        f[2] += fij[2];
+    }
+    acc->x += f[0] / a->mass;
+    acc->y += f[1] / a->mass;
+    acc->z += f[2] / a->mass;
+}
+
+/* transformers.rs:219-244 (simple_astro).  `+=` into acc. */
+void oracle_simple_astro(const Entity *state, size_t n, double e, Acceleration *acc)
+{
+    for (size_t i = 0; i < n; ++i) {
+        if (state[i].fixed) continue;
+        accumulate_list(&state[i], state, n, e, &acc[i]);
+    }
+}
+
+/* simple_astro restricted to the bodies listed in idx (a sample), with the
+ * per-body loop spread over OpenMP threads (`threads` <= 0: all).  Each body's
+ * sum is the same serial sum as oracle_simple_astro, so results are identical.
+ * acc_out[k] receives (not accumulates) body idx[k]'s acceleration. */
+void oracle_simple_astro_sample(const Entity *state, size_t n, double e, const int64_t *idx,
+                                size_t n_idx, Acceleration *acc_out, int threads)
+{
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
+#endif
+    for (long k = 0; k < (long)n_idx; ++k) {
+        Acceleration a = {0.0, 0.0, 0.0};
+        const Entity *s = &state[idx[k]];
+        if (!s->fixed) accumulate_list(s, state, n, e, &a);
+        acc_out[k] = a;
+    }
+    (void)threads;
+}
+
+static double state_extent(const Entity *state, size_t n)
+{
+    /* transformers.rs:126-131: max over |x|,|y|,|z|, 1.0 for an empty state. */
+    if (n == 0) return 1.0;
+    double m = fabs(state[0].x);
+    for (size_t i = 0; i < n; ++i) {
+        if (i > 0) m = fmax(m, fabs(state[i].x));
+        m = fmax(m, fabs(state[i].y));
+        m = fmax(m, fabs(state[i].z));
+    }
+    return m;
+}
+
+double oracle_state_extent(const Entity *state, size_t n) { return state_extent(state, n); }
+
+/* astro2 (nchild 8, transformers.rs:122-160) and astro (nchild 4,
+ * transformers.rs:31-69), restricted to the bodies in idx (NULL: all bodies,
+ * accumulated with `+=` into acc[i]; else acc[k] += for body idx[k]).
+ * Returns 0 or the tree's panic status. */
+int oracle_barnes_hut(int nchild, const Entity *state, size_t n, double theta, double e,
+                      const int64_t *idx, size_t n_idx, Acceleration *acc, int threads)
+{
+    double extent = state_extent(state, n);
+    double c0[3] = {0.0, 0.0, 0.0};
+    Tree *t = oracle_tree_new(nchild, c0, 1.0 * extent);
+    if (!t) return -1;
+    for (size_t i = 0; i < n; ++i) {
+        int st = oracle_tree_push(t, &state[i]);
+        if (st) {
+            oracle_tree_free(t);
+            return st;
+        }
+    }
+    size_t count = idx ? n_idx : n;
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel num_threads(threads)
+#endif
+    {
+        size_t cap = 1024;
+        Entity *list = (Entity *)malloc(cap * sizeof(Entity));
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 16)
+#endif
+        for (long k = 0; k < (long)count; ++k) {
+            size_t i = idx ? (size_t)idx[k] : (size_t)k;
+            const Entity *a = &state[i];
+            if (a->fixed) continue;
+            double loc[3] = {a->x, a->y, a->z};
+            size_t len = oracle_tree_leaves(t, loc, theta, list, cap);
+            if (len > cap) {
+                while (cap < len) cap *= 2;
+                list = (Entity *)realloc(list, cap * sizeof(Entity));
+                len = oracle_tree_leaves(t, loc, theta, list, cap);
+            }
+            accumulate_list(a, list, len, e, &acc[idx ? (size_t)k : i]);
+        }
+        free(list);
+    }
+    (void)threads;
+    oracle_tree_free(t);
+    return 0;
+}
+
+int oracle_astro2(const Entity *state, size_t n, double theta, double e, Acceleration *acc)
+{
+    return oracle_barnes_hut(8, state, n, theta, e, NULL, 0, acc, 1);
+}
+
+int oracle_astro(const Entity *state, size_t n, double theta, double e, Acceleration *acc)
+{
+    return oracle_barnes_hut(4, state, n, theta, e, NULL, 0, acc, 1);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Verlet (integrators/src/verlet.rs:19-107).                                */
+/* ------------------------------------------------------------------------ */
+typedef struct Verlet {
+    Entity *previous_state;
+    size_t len;
+} Verlet;
+
+Verlet *oracle_verlet_new(void) { return (Verlet *)calloc(1, sizeof(Verlet)); }
+
+void oracle_verlet_free(Verlet *v)
+{
+    if (!v) return;
+    free(v->previous_state);
+    free(v);
+}
+
+static void verlet_store_previous(Verlet *v, const Entity *entities, size_t n)
+{
+    if (v->len != n) {
+        free(v->previous_state);
+        v->previous_state = (Entity *)malloc((n ? n : 1) * sizeof(Entity));
+        v->len = n;
+    }
+    memcpy(v->previous_state, entities, n * sizeof(Entity));
+}
+
+/* verlet.rs:85-107 with the accelerations already evaluated by acc_fn.
+ * Returns 1 when the Taylor first step (initial_integration) was taken. */
+int oracle_verlet_step(Verlet *v, const Entity *entities, Entity *new_state, size_t n,
+                       const Acceleration *a, double dt)
+{
+    double dt2 = dt * dt;
+    if (v->len != n) {
+        /* verlet.rs:24-50 (previous_state is stored first) */
+        verlet_store_previous(v, entities, n);
+        for (size_t i = 0; i < n; ++i) {
+            const Entity *en = &entities[i];
+            double x = en->x + en->vx * dt + 0.5 * a[i].x * dt2;
+            double y = en->y + en->vy * dt + 0.5 * a[i].y * dt2;
+            double z = en->z + en->vz * dt + 0.5 * a[i].z * dt2;
+            double vx = en->vx + a[i].x * dt;
+            double vy = en->vy + a[i].y * dt;
+            double vz = en->vz + a[i].z * dt;
+            Entity ne = *en;
+            ne.x = x; ne.y = y; ne.z = z;
+            ne.vx = vx; ne.vy = vy; ne.vz = vz;
+            new_state[i] = ne;
+        }
+        return 1;
+    }
+    /* verlet.rs:52-82 */
+    for (size_t i = 0; i < n; ++i) {
+        const Entity *en = &entities[i];
+        const Entity *prev = &v->previous_state[i];
+        double x = 2.0 * en->x - prev->x + a[i].x * dt2;
+        double y = 2.0 * en->y - prev->y + a[i].y * dt2;
+        double z = 2.0 * en->z - prev->z + a[i].z * dt2;
+        double vx = (x - en->x) / dt;
+        double vy = (y - en->y) / dt;
+        double vz = (z - en->z) / dt;
+        Entity ne = *en;
+        ne.x = x; ne.y = y; ne.z = z;
+        ne.vx = vx; ne.vy = vy; ne.vz = vz;
+        new_state[i] = ne;
+    }
+    verlet_store_previous(v, entities, n);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Pipeline loop (pipeline.rs:137-141,166-173) with one gravity transform    */
+/* and the verlet integrator.  element: 0 simple_astro, 1 astro2, 2 astro.   */
+/* state is advanced in place by `steps` steps.  Returns 0 or a panic status. */
+/* ------------------------------------------------------------------------ */
+int oracle_run_pipeline(Entity *state, size_t n, int element, double theta, double e, double dt,
+                        int steps, int threads)
+{
+    Verlet *v = oracle_verlet_new();
+    Entity *new_state = (Entity *)malloc((n ? n : 1) * sizeof(Entity));
+    Acceleration *acc = (Acceleration *)malloc((n ? n : 1) * sizeof(Acceleration));
+    int64_t *all = (int64_t *)malloc((n ? n : 1) * sizeof(int64_t));
+    for (size_t i = 0; i < n; ++i) all[i] = (int64_t)i;
+    int st = 0;
+    for (int s = 0; s < steps && st == 0; ++s) {
+        memset(acc, 0, n * sizeof(Acceleration));
+        if (element == 0) {
+            oracle_simple_astro_sample(state, n, e, all, n, acc, threads);
+        } else {
+            st = oracle_barnes_hut(element == 1 ? 8 : 4, state, n, theta, e, NULL, 0, acc, threads);
+        }
+        if (st) break;
+        oracle_verlet_step(v, state, new_state, n, acc, dt);
+        memcpy(state, new_state, n * sizeof(Entity));
+    }
+    free(all);
+    free(acc);
+    free(new_state);
+    oracle_verlet_free(v);
+    return st;
+}
+
+/* Number of OpenMP threads this build would use (1 without OpenMP). */
+int oracle_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

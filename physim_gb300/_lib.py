@@ -1,0 +1,129 @@
+"""ctypes binding of libphysim_gb300.so (declarations in include/physim_gb300.h).
+
+Importing this module loads the CUDA library; there is no CPU fallback.  If
+the shared library has not been built the import fails with an error that
+says how to build it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libphysim_gb300.so"
+
+PHYSIM_OK = 0
+PHYSIM_ERR_ARGUMENT = 1
+PHYSIM_ERR_CUDA = 2
+PHYSIM_ERR_MEMORY = 3
+PHYSIM_ERR_TREE = 4
+PHYSIM_ERR_TIMEOUT = 5
+
+GRAVITY_SIMPLE_ASTRO = 0
+GRAVITY_ASTRO2 = 1
+GRAVITY_ASTRO = 2
+TRAVERSAL_EXACT = 0
+TRAVERSAL_WARP = 1
+
+
+class CMessage(C.Structure):
+    _fields_ = [("priority", C.c_int), ("topic", C.c_char_p), ("message", C.c_char_p),
+                ("sender_id", C.c_size_t), ("origin", C.c_int)]
+
+
+class ElementMetaFFI(C.Structure):
+    _fields_ = [("kind", C.c_int), ("name", C.c_void_p), ("plugin", C.c_void_p),
+                ("version", C.c_void_p), ("license", C.c_void_p), ("author", C.c_void_p),
+                ("blurb", C.c_void_p), ("repo", C.c_void_p)]
+
+
+RustStringAllocFn = C.CFUNCTYPE(C.c_void_p, C.c_char_p)
+InitFn = C.CFUNCTYPE(C.c_void_p, C.c_void_p, C.c_size_t)
+TransformFn = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t)
+DestroyFn = C.CFUNCTYPE(None, C.c_void_p)
+DescFn = C.CFUNCTYPE(C.c_void_p, C.c_void_p, C.c_void_p)
+RecvFn = C.CFUNCTYPE(None, C.c_void_p, C.POINTER(CMessage))
+PostFn = C.CFUNCTYPE(None, C.c_void_p)
+
+
+class TransformElementAPI(C.Structure):
+    _fields_ = [("init", InitFn), ("transform", TransformFn), ("destroy", DestroyFn),
+                ("get_property_descriptions", DescFn), ("recv_message", RecvFn),
+                ("post_configuration_messages", PostFn)]
+
+
+class PhysimSimConfig(C.Structure):
+    _fields_ = [("gravity", C.c_uint32), ("leaf_size", C.c_uint32), ("traversal", C.c_uint32),
+                ("compensated", C.c_uint32), ("theta", C.c_double), ("e", C.c_double),
+                ("dt", C.c_double), ("stream", C.c_void_p), ("device", C.c_int32),
+                ("reserved", C.c_uint32 * 3)]
+
+
+ELEMENTS = ("astro", "astro2", "simple_astro")
+ELEMENT_SUFFIXES = ("get_api", "register", "init", "transform", "destroy",
+                    "get_property_descriptions", "recv_message", "post_configuration_messages")
+
+
+def _load() -> C.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(
+            f"{LIB_PATH} is missing: build it with `python -c \"import __graft_entry__ as g; "
+            "g.build()\"` (requires nvcc); physim_gb300 has no CPU fallback")
+    lib = C.CDLL(str(LIB_PATH), mode=os.RTLD_NOW | os.RTLD_LOCAL)
+    vp, sz, i32, u32, dbl = C.c_void_p, C.c_size_t, C.c_int32, C.c_uint32, C.c_double
+    sig = {
+        "get_plugin_abi_info": (C.c_char_p, []),
+        "register_plugin": (C.c_char_p, []),
+        "set_callback_target": (None, [vp]),
+        "physim_gpu_last_error": (C.c_char_p, []),
+        "physim_gpu_sim_config_default": (None, [C.POINTER(PhysimSimConfig)]),
+        "physim_gpu_sim_create": (C.c_int, [C.POINTER(PhysimSimConfig), sz, C.POINTER(vp)]),
+        "physim_gpu_sim_upload": (C.c_int, [vp, vp, sz]),
+        "physim_gpu_sim_step": (C.c_int, [vp, u32]),
+        "physim_gpu_sim_download": (C.c_int, [vp, vp, sz]),
+        "physim_gpu_sim_accelerations": (C.c_int, [vp, vp, sz]),
+        "physim_gpu_sim_synchronize": (C.c_int, [vp]),
+        "physim_gpu_sim_stream": (vp, [vp]),
+        "physim_gpu_sim_launches_per_step": (C.c_int, [vp]),
+        "physim_gpu_sim_set_profiling": (C.c_int, [vp, C.c_int]),
+        "physim_gpu_sim_last_step_ms": (C.c_int, [vp, C.POINTER(dbl), C.POINTER(dbl)]),
+        "physim_gpu_sim_destroy": (None, [vp]),
+        "physim_gpu_verlet_create": (C.c_int, [i32, C.POINTER(vp)]),
+        "physim_gpu_verlet_integrate": (C.c_int, [vp, vp, vp, sz, vp, dbl]),
+        "physim_gpu_verlet_destroy": (None, [vp]),
+    }
+    for el in ELEMENTS:
+        sig[f"{el}_get_api"] = (C.POINTER(TransformElementAPI), [])
+        sig[f"{el}_register"] = (ElementMetaFFI, [RustStringAllocFn])
+        sig[f"{el}_init"] = (vp, [vp, sz])
+        sig[f"{el}_transform"] = (None, [vp, vp, sz, vp, sz])
+        sig[f"{el}_destroy"] = (None, [vp])
+        sig[f"{el}_get_property_descriptions"] = (vp, [vp, vp])
+        sig[f"{el}_recv_message"] = (None, [vp, C.POINTER(CMessage)])
+        sig[f"{el}_post_configuration_messages"] = (None, [vp])
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+class PhysimError(RuntimeError):
+    """A physim_gpu_* call returned a non-zero status."""
+
+    def __init__(self, code: int, what: str):
+        super().__init__(f"{what} failed with status {code}: {last_error()}")
+        self.code = code
+
+
+def last_error() -> str:
+    msg = lib.physim_gpu_last_error()
+    return msg.decode(errors="replace") if msg else ""
+
+
+def check(code: int, what: str) -> None:
+    if code != PHYSIM_OK:
+        raise PhysimError(code, what)

@@ -1,0 +1,94 @@
+// element.cu -- the compute behind a transform element's transform call:
+// host Entity array in, `acc[i] += a_i` out (astro/src/transformers.rs:122-160
+// for astro2, :31-69 for astro, :219-244 for simple_astro).
+//
+// Per call: the Entity array (80 B/body) and the caller's accelerations
+// (24 B/body) are copied to the device, unpacked to f32 (x,y,z,m) + f64
+// state, the gravity kernels run, the accelerations are added on the device
+// in f64 and copied back.  Fixed bodies keep their incoming value untouched.
+#include "common.cuh"
+#include "engine.h"
+#include "plugin_state.h"
+
+namespace pg {
+
+static int ensure_doubles(double *&p, size_t &cap, size_t need)
+{
+    if (need <= cap) return PHYSIM_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    PG_CUDA(cudaMalloc((void **)&p, need * sizeof(double)));
+    cap = need;
+    return PHYSIM_OK;
+}
+
+static int accumulate_locked(ElementState *el, const Entity *state, size_t n, Acceleration *acc)
+{
+    if (n == 0) return PHYSIM_OK;
+    PG_CHECK(n < (size_t)INT32_MAX, PHYSIM_ERR_ARGUMENT, "too many bodies: %zu", n);
+    PG_CUDA(cudaSetDevice(el->device));
+    if (!el->ready) {
+        PG_CUDA(cudaStreamCreateWithFlags(&el->stream, cudaStreamNonBlocking));
+        el->ready = true;
+    }
+    cudaStream_t st = el->stream;
+    const bool tree = el->kind != 0;
+    PG_TRY(bodies_reserve(el->bodies, n, tree));
+    if (el->acc_cap < n) {
+        if (el->d_acc) cudaFree(el->d_acc);
+        el->d_acc = nullptr;
+        el->acc_cap = 0;
+        PG_CUDA(cudaMalloc((void **)&el->d_acc, n * sizeof(Acceleration)));
+        el->acc_cap = n;
+    }
+    PG_CUDA(cudaMemcpyAsync(el->bodies.aos, state, n * sizeof(Entity), cudaMemcpyHostToDevice, st));
+    PG_CUDA(cudaMemcpyAsync(el->d_acc, acc, n * sizeof(Acceleration), cudaMemcpyHostToDevice, st));
+    PG_TRY(launch_unpack(el->bodies, el->bodies.aos, n, tree, st));
+    int splits = 1;
+    if (!tree) {
+        if (el->plan_n != (int)n) {
+            el->plan = plan_direct((int)n, el->device, true);
+            el->plan_n = (int)n;
+        }
+        splits = el->plan.splits;
+        PG_TRY(ensure_doubles(el->partial, el->partial_cap, (size_t)splits * 3 * n));
+        PG_TRY(launch_direct(el->plan, el->bodies.body4, (float)el->e, el->partial, st));
+    } else {
+        PG_TRY(ensure_doubles(el->partial, el->partial_cap, 3 * n));
+        PG_TRY(bh_reserve(el->bh, n, el->device));
+        BhParams p;
+        p.nchild = el->kind == 1 ? 8 : 4;
+        p.theta = el->theta;
+        p.e = el->e;
+        p.leaf_size = el->leaf_size;
+        p.traversal = el->traversal;
+        PG_TRY(bh_accelerations(el->bh, el->bodies, p, el->partial, st));
+    }
+    PG_TRY(launch_accumulate_aos(el->bodies, el->partial, splits, el->d_acc, st));
+    PG_CUDA(cudaMemcpyAsync(acc, el->d_acc, n * sizeof(Acceleration), cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    return PHYSIM_OK;
+}
+
+int element_accumulate(ElementState *el, const Entity *state, size_t n, Acceleration *acc)
+{
+    std::lock_guard<std::mutex> g(el->lock);
+    return accumulate_locked(el, state, n, acc);
+}
+
+void element_destroy(ElementState *el)
+{
+    if (el->ready) {
+        cudaSetDevice(el->device);
+        cudaStreamSynchronize(el->stream);
+        bodies_free(el->bodies);
+        if (el->d_acc) cudaFree(el->d_acc);
+        if (el->partial) cudaFree(el->partial);
+        bh_free(el->bh);
+        cudaStreamDestroy(el->stream);
+    }
+    delete el;
+}
+
+}  // namespace pg

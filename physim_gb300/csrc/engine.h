@@ -1,0 +1,96 @@
+// engine.h -- internal interfaces shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "physim_gb300.h"
+
+namespace pg {
+
+// Bodies are padded to a multiple of this many entries (zero mass at the
+// origin), so every kernel can read whole tiles without bounds checks.
+constexpr int kBodyPad = 1024;
+
+inline size_t pad_bodies(size_t n) { return (n + kBodyPad - 1) / kBodyPad * kBodyPad; }
+
+// Guard added to r^2 (r^2 + e)^2 before the reciprocal square root.  It makes
+// the contribution of a body at exactly the same position zero (dx = 0 times
+// a finite factor), which is the reference's "skip equal centres" rule
+// (astro/src/transformers.rs:145,230), without a per-pair branch.  It is below
+// FLT_MIN * 10, so it changes no pair whose r^2 (r^2 + e)^2 exceeds 1e-30 by
+// more than 1e-7 relative.
+constexpr float kPairGuard = 1.0e-37f;
+
+// ------------------------------------------------------------------------
+// Direct sum (simple_astro)
+// ------------------------------------------------------------------------
+struct DirectPlan {
+    int block = 256;       // threads per block
+    int ipt = 4;           // bodies per thread
+    int splits = 1;        // j-range chunks (partial sums combined afterwards)
+    int n = 0;             // bodies
+    int n_itiles = 0;      // i tiles of block*ipt bodies
+    int n_jtiles = 0;      // j tiles of `block` bodies
+    int chunk_tiles = 0;   // j tiles per split
+    bool compensated = true;
+};
+
+// Heuristic plan that fills the GPU: picks the i-tile shape and the number of
+// j splits whose block count wastes least in the last wave.
+DirectPlan plan_direct(int n, int device, bool compensated);
+// Enumerates the candidate plans the autotuner times for n bodies.
+int direct_candidates(int n, int device, bool compensated, DirectPlan *out, int cap);
+
+// Launches the pair kernel.  body4: n_pad (x,y,z,m) f32 entries.  partial:
+// splits x 3 x n doubles, partial[(s*3+c)*n + i].
+int launch_direct(const DirectPlan &plan, const float4 *body4, float e, double *partial,
+                  cudaStream_t stream);
+
+// ------------------------------------------------------------------------
+// Body staging, integration and accumulation (integrate.cu)
+// ------------------------------------------------------------------------
+struct DeviceBodies {
+    size_t n = 0, cap = 0;  // live bodies, allocated capacity (padded)
+    float4 *body4 = nullptr;  // f32 (x,y,z,m), padded with zero-mass entries
+    uint8_t *fixed = nullptr;
+    double *x = nullptr, *y = nullptr, *z = nullptr;     // f64 positions
+    double *vx = nullptr, *vy = nullptr, *vz = nullptr;  // f64 velocities
+    double *px = nullptr, *py = nullptr, *pz = nullptr;  // verlet previous positions
+    double *m = nullptr;                                  // f64 masses
+    double *radius = nullptr;
+    uint64_t *id = nullptr;
+    Entity *aos = nullptr;  // staging for host<->device copies
+};
+
+int bodies_reserve(DeviceBodies &b, size_t n, bool with_state);
+void bodies_free(DeviceBodies &b);
+
+// Unpacks an Entity array already on the device into the SoA arrays.
+int launch_unpack(DeviceBodies &b, const Entity *d_aos, size_t n, bool full_state,
+                  cudaStream_t stream);
+// Packs the SoA state back into b.aos.
+int launch_pack(DeviceBodies &b, cudaStream_t stream);
+
+// acc[i] += a_i (f64) for each non-fixed body, a_i = sum over splits of the
+// partial sums; NaN for a massless body (the reference divides F by m_i).
+int launch_accumulate_aos(const DeviceBodies &b, const double *partial, int splits,
+                          Acceleration *d_acc, cudaStream_t stream);
+// acc_soa[c*n + i] = a_i (f64).
+int launch_combine_soa(const DeviceBodies &b, const double *partial, int splits,
+                       double *acc_soa, cudaStream_t stream);
+// Verlet step (verlet.rs:24-82) fused with the combine of the partial sums,
+// updating the f64 state and the f32 body copy in place.
+int launch_verlet(DeviceBodies &b, const double *partial, int splits, double dt, bool initial,
+                  cudaStream_t stream);
+
+// Verlet over explicit device arrays (the host-array integrator path).
+int launch_verlet_aos(const Entity *d_in, const Entity *d_prev, Entity *d_out,
+                      const Acceleration *d_acc, size_t n, double dt, bool initial,
+                      cudaStream_t stream);
+
+// Device count / SM count helpers (cached).
+int device_sm_count(int device);
+
+}  // namespace pg

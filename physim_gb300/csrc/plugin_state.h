@@ -1,0 +1,61 @@
+// plugin_state.h -- per-instance state of a transform element.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "engine.h"
+
+namespace pg {
+
+struct BhWorkspace;
+
+struct ElementState {
+    int kind = 0;  // 0 simple_astro, 1 astro2, 2 astro
+    double theta = 1.0;
+    double e = 1.0;
+    int leaf_size = 1;
+    int traversal = PHYSIM_TRAVERSAL_EXACT;
+    int device = 0;
+
+    // GPU resources, created by the first transform.
+    std::mutex lock;
+    bool ready = false;
+    cudaStream_t stream = nullptr;
+    DeviceBodies bodies;
+    Acceleration *d_acc = nullptr;
+    size_t acc_cap = 0;
+    double *partial = nullptr;
+    size_t partial_cap = 0;
+    DirectPlan plan;
+    int plan_n = -1;
+    BhWorkspace *bh = nullptr;
+};
+
+// acc[i] += a_i on host arrays (host->device copies, kernels, device->host).
+int element_accumulate(ElementState *el, const Entity *state, size_t n, Acceleration *acc);
+void element_destroy(ElementState *el);
+
+// ------------------------------------------------------------------------
+// Barnes-Hut (bh.cu)
+// ------------------------------------------------------------------------
+struct BhParams {
+    int nchild = 8;  // 8 octree (astro2), 4 quadtree (astro)
+    double theta = 1.0;
+    double e = 1.0;
+    int leaf_size = 1;
+    int traversal = PHYSIM_TRAVERSAL_EXACT;
+    bool compensated = true;
+};
+
+int bh_reserve(BhWorkspace *&ws, size_t n, int device);
+void bh_free(BhWorkspace *ws);
+// Accelerations of the bodies in b (f64 positions and f32 copies must be
+// current) into partial[c*n + i] (one split).
+int bh_accelerations(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, double *partial,
+                     cudaStream_t stream);
+// Kernel launches one bh_accelerations call makes.
+int bh_launches(const BhWorkspace *ws);
+
+}  // namespace pg

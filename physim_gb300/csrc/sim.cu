@@ -1,0 +1,348 @@
+// sim.cu -- device-resident simulations (physim_gpu_sim_*) and the verlet
+// integrator over host arrays (physim_gpu_verlet_*).
+//
+// A simulation restates one pipeline step of physim (pipeline.rs:137-173 with
+// a single gravity transform and the verlet integrator, verlet.rs:85-107) but
+// keeps the state in HBM: per step, the gravity kernels write per-body
+// partial sums and one fused kernel combines them and applies the verlet
+// update in f64, refreshing the f32 body copy the next step reads.
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "common.cuh"
+#include "engine.h"
+#include "plugin_state.h"
+
+struct PhysimSim {
+    PhysimSimConfig cfg;
+    size_t n = 0;
+    bool own_stream = false;
+    cudaStream_t stream = nullptr;
+    pg::DeviceBodies b;
+    double *partial = nullptr;
+    size_t partial_cap = 0;
+    double *acc_soa = nullptr;
+    pg::DirectPlan plan;
+    pg::BhWorkspace *bh = nullptr;
+    bool history = false;  // verlet previous_state is valid
+    bool uploaded = false;
+    // Optional per-step timing: events around the gravity kernels and the
+    // integrator of the most recent step.
+    bool profiling = false;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+};
+
+struct PhysimVerlet {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    Entity *d_in = nullptr, *d_prev = nullptr, *d_out = nullptr;
+    Acceleration *d_acc = nullptr;
+    size_t cap = 0;
+    size_t prev_len = 0;  // length of previous_state (verlet.rs:102)
+    bool has_prev = false;
+};
+
+namespace {
+
+using namespace pg;
+
+int sim_forces(PhysimSim *s, int *splits_out)
+{
+    const size_t n = s->n;
+    const PhysimSimConfig &c = s->cfg;
+    if (c.gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO) {
+        *splits_out = s->plan.splits;
+        return launch_direct(s->plan, s->b.body4, (float)c.e, s->partial, s->stream);
+    }
+    BhParams p;
+    p.nchild = c.gravity == PHYSIM_GRAVITY_ASTRO2 ? 8 : 4;
+    p.theta = c.theta;
+    p.e = c.e;
+    p.leaf_size = (int)c.leaf_size;
+    p.traversal = (int)c.traversal;
+    p.compensated = c.compensated != 0;
+    *splits_out = 1;
+    (void)n;
+    return bh_accelerations(s->bh, s->b, p, s->partial, s->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+void physim_gpu_sim_config_default(PhysimSimConfig *cfg)
+{
+    if (!cfg) return;
+    memset(cfg, 0, sizeof *cfg);
+    cfg->gravity = PHYSIM_GRAVITY_SIMPLE_ASTRO;
+    cfg->leaf_size = 1;
+    cfg->traversal = PHYSIM_TRAVERSAL_EXACT;
+    cfg->compensated = 1;
+    cfg->theta = 1.0;
+    cfg->e = 1.0;
+    cfg->dt = 1e-6;
+    cfg->stream = nullptr;
+    cfg->device = 0;
+}
+
+int physim_gpu_sim_create(const PhysimSimConfig *cfg, size_t n, PhysimSim **out)
+{
+    PG_CHECK(cfg && out, PHYSIM_ERR_ARGUMENT, "null argument");
+    *out = nullptr;
+    PG_CHECK(cfg->gravity <= PHYSIM_GRAVITY_ASTRO, PHYSIM_ERR_ARGUMENT, "unknown gravity %u",
+             cfg->gravity);
+    PG_CHECK(cfg->leaf_size >= 1 && cfg->leaf_size <= 64, PHYSIM_ERR_ARGUMENT,
+             "leaf_size %u outside 1..64", cfg->leaf_size);
+    PG_CHECK(cfg->traversal <= PHYSIM_TRAVERSAL_WARP, PHYSIM_ERR_ARGUMENT, "unknown traversal");
+    PG_CHECK(n < (size_t)INT32_MAX, PHYSIM_ERR_ARGUMENT, "too many bodies: %zu", n);
+    PG_CHECK(cfg->reserved[0] == 0 && cfg->reserved[1] == 0 && cfg->reserved[2] == 0,
+             PHYSIM_ERR_ARGUMENT, "reserved fields must be zero");
+    PG_CUDA(cudaSetDevice(cfg->device));
+    PhysimSim *s = new (std::nothrow) PhysimSim();
+    PG_CHECK(s, PHYSIM_ERR_MEMORY, "out of host memory");
+    s->cfg = *cfg;
+    s->cfg.e = fabs(cfg->e);
+    s->n = n;
+    int rc = PHYSIM_OK;
+    if (cfg->stream) {
+        s->stream = (cudaStream_t)cfg->stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            set_error("cudaStreamCreate failed");
+            delete s;
+            return PHYSIM_ERR_CUDA;
+        }
+        s->own_stream = true;
+    }
+    rc = bodies_reserve(s->b, n, true);
+    size_t partial_elems = 3 * (n ? n : 1);
+    if (rc == PHYSIM_OK && cfg->gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO) {
+        s->plan = plan_direct((int)n, cfg->device, cfg->compensated != 0);
+        partial_elems *= (size_t)s->plan.splits;
+    }
+    if (rc == PHYSIM_OK && cfg->gravity != PHYSIM_GRAVITY_SIMPLE_ASTRO)
+        rc = bh_reserve(s->bh, n, cfg->device);
+    if (rc == PHYSIM_OK && cudaMalloc((void **)&s->partial, partial_elems * sizeof(double)) !=
+                               cudaSuccess) {
+        set_error("cudaMalloc of partial sums failed");
+        rc = PHYSIM_ERR_MEMORY;
+    }
+    s->partial_cap = partial_elems;
+    if (rc != PHYSIM_OK) {
+        physim_gpu_sim_destroy(s);
+        return rc;
+    }
+    *out = s;
+    return PHYSIM_OK;
+}
+
+int physim_gpu_sim_upload(PhysimSim *s, const Entity *state, size_t n)
+{
+    PG_CHECK(s && (state || n == 0), PHYSIM_ERR_ARGUMENT, "null argument");
+    PG_CHECK(n == s->n, PHYSIM_ERR_ARGUMENT, "upload of %zu bodies into a simulation of %zu", n,
+             s->n);
+    PG_CUDA(cudaSetDevice(s->cfg.device));
+    if (n) {
+        PG_CUDA(cudaMemcpyAsync(s->b.aos, state, n * sizeof(Entity), cudaMemcpyHostToDevice,
+                                s->stream));
+        PG_TRY(launch_unpack(s->b, s->b.aos, n, true, s->stream));
+    }
+    s->history = false;
+    s->uploaded = true;
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    return PHYSIM_OK;
+}
+
+int physim_gpu_sim_step(PhysimSim *s, uint32_t steps)
+{
+    PG_CHECK(s, PHYSIM_ERR_ARGUMENT, "null simulation");
+    PG_CHECK(s->uploaded, PHYSIM_ERR_ARGUMENT, "step before upload");
+    PG_CUDA(cudaSetDevice(s->cfg.device));
+    for (uint32_t k = 0; k < steps; ++k) {
+        if (s->n == 0) break;
+        int splits = 1;
+        if (s->profiling) PG_CUDA(cudaEventRecord(s->ev[0], s->stream));
+        PG_TRY(sim_forces(s, &splits));
+        if (s->profiling) PG_CUDA(cudaEventRecord(s->ev[1], s->stream));
+        PG_TRY(launch_verlet(s->b, s->partial, splits, s->cfg.dt, !s->history, s->stream));
+        if (s->profiling) PG_CUDA(cudaEventRecord(s->ev[2], s->stream));
+        s->history = true;
+    }
+    return PHYSIM_OK;
+}
+
+int physim_gpu_sim_set_profiling(PhysimSim *s, int enable)
+{
+    PG_CHECK(s, PHYSIM_ERR_ARGUMENT, "null simulation");
+    PG_CUDA(cudaSetDevice(s->cfg.device));
+    if (enable && !s->ev[0])
+        for (cudaEvent_t &e : s->ev) PG_CUDA(cudaEventCreate(&e));
+    s->profiling = enable != 0;
+    return PHYSIM_OK;
+}
+
+int physim_gpu_sim_last_step_ms(PhysimSim *s, double *gravity_ms, double *integrate_ms)
+{
+    PG_CHECK(s && gravity_ms && integrate_ms, PHYSIM_ERR_ARGUMENT, "null argument");
+    PG_CHECK(s->profiling, PHYSIM_ERR_ARGUMENT, "profiling is off");
+    PG_CUDA(cudaSetDevice(s->cfg.device));
+    PG_CUDA(cudaEventSynchronize(s->ev[2]));
+    float a = 0.f, b = 0.f;
+    PG_CUDA(cudaEventElapsedTime(&a, s->ev[0], s->ev[1]));
+    PG_CUDA(cudaEventElapsedTime(&b, s->ev[1], s->ev[2]));
+    *gravity_ms = a;
+    *integrate_ms = b;
+    return PHYSIM_OK;
+}
+
+int physim_gpu_sim_download(PhysimSim *s, Entity *state, size_t n)
+{
+    PG_CHECK(s && (state || n == 0), PHYSIM_ERR_ARGUMENT, "null argument");
+    PG_CHECK(n == s->n, PHYSIM_ERR_ARGUMENT, "download of %zu bodies from a simulation of %zu",
+             n, s->n);
+    PG_CUDA(cudaSetDevice(s->cfg.device));
+    if (n) {
+        PG_TRY(launch_pack(s->b, s->stream));
+        PG_CUDA(cudaMemcpyAsync(state, s->b.aos, n * sizeof(Entity), cudaMemcpyDeviceToHost,
+                                s->stream));
+    }
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    return PHYSIM_OK;
+}
+
+int physim_gpu_sim_accelerations(PhysimSim *s, Acceleration *acc, size_t n)
+{
+    PG_CHECK(s && (acc || n == 0), PHYSIM_ERR_ARGUMENT, "null argument");
+    PG_CHECK(n == s->n, PHYSIM_ERR_ARGUMENT, "size mismatch %zu vs %zu", n, s->n);
+    PG_CHECK(s->uploaded, PHYSIM_ERR_ARGUMENT, "accelerations before upload");
+    if (n == 0) return PHYSIM_OK;
+    PG_CUDA(cudaSetDevice(s->cfg.device));
+    if (!s->acc_soa) PG_CUDA(cudaMalloc((void **)&s->acc_soa, 3 * n * sizeof(double)));
+    int splits = 1;
+    PG_TRY(sim_forces(s, &splits));
+    PG_TRY(launch_combine_soa(s->b, s->partial, splits, s->acc_soa, s->stream));
+    std::vector<double> h(3 * n);
+    PG_CUDA(cudaMemcpyAsync(h.data(), s->acc_soa, 3 * n * sizeof(double), cudaMemcpyDeviceToHost,
+                            s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    for (size_t i = 0; i < n; ++i) {
+        acc[i].x = h[i];
+        acc[i].y = h[n + i];
+        acc[i].z = h[2 * n + i];
+    }
+    return PHYSIM_OK;
+}
+
+int physim_gpu_sim_synchronize(PhysimSim *s)
+{
+    PG_CHECK(s, PHYSIM_ERR_ARGUMENT, "null simulation");
+    PG_CUDA(cudaSetDevice(s->cfg.device));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    return PHYSIM_OK;
+}
+
+void *physim_gpu_sim_stream(PhysimSim *s) { return s ? (void *)s->stream : nullptr; }
+
+int physim_gpu_sim_launches_per_step(PhysimSim *s)
+{
+    if (!s) return 0;
+    if (s->cfg.gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO) return 2;
+    return bh_launches(s->bh) + 1;
+}
+
+void physim_gpu_sim_destroy(PhysimSim *s)
+{
+    if (!s) return;
+    cudaSetDevice(s->cfg.device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    bodies_free(s->b);
+    if (s->partial) cudaFree(s->partial);
+    if (s->acc_soa) cudaFree(s->acc_soa);
+    bh_free(s->bh);
+    for (cudaEvent_t e : s->ev)
+        if (e) cudaEventDestroy(e);
+    if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+// ------------------------------------------------------------------------
+// Verlet over host arrays
+// ------------------------------------------------------------------------
+int physim_gpu_verlet_create(int32_t device, PhysimVerlet **out)
+{
+    PG_CHECK(out, PHYSIM_ERR_ARGUMENT, "null argument");
+    *out = nullptr;
+    PhysimVerlet *v = new (std::nothrow) PhysimVerlet();
+    PG_CHECK(v, PHYSIM_ERR_MEMORY, "out of host memory");
+    v->device = device;
+    *out = v;
+    return PHYSIM_OK;
+}
+
+int physim_gpu_verlet_integrate(PhysimVerlet *v, const Entity *entities, Entity *new_state,
+                                size_t n, const Acceleration *acc, double dt)
+{
+    PG_CHECK(v, PHYSIM_ERR_ARGUMENT, "null integrator");
+    PG_CHECK(n == 0 || (entities && new_state && acc), PHYSIM_ERR_ARGUMENT, "null argument");
+    PG_CUDA(cudaSetDevice(v->device));
+    if (!v->stream) PG_CUDA(cudaStreamCreateWithFlags(&v->stream, cudaStreamNonBlocking));
+    if (n > v->cap) {
+        Entity **bufs[] = {&v->d_in, &v->d_prev, &v->d_out};
+        // Keep previous_state across a growth only if its length still matches.
+        Entity *old_prev = v->d_prev;
+        size_t old_cap = v->cap;
+        if (v->d_in) cudaFree(v->d_in);
+        if (v->d_out) cudaFree(v->d_out);
+        if (v->d_acc) cudaFree(v->d_acc);
+        v->d_in = v->d_out = nullptr;
+        v->d_acc = nullptr;
+        v->d_prev = nullptr;
+        for (Entity **b : bufs) PG_CUDA(cudaMalloc((void **)b, n * sizeof(Entity)));
+        PG_CUDA(cudaMalloc((void **)&v->d_acc, n * sizeof(Acceleration)));
+        if (old_prev) {
+            if (v->has_prev && v->prev_len <= old_cap && v->prev_len > 0)
+                PG_CUDA(cudaMemcpyAsync(v->d_prev, old_prev, v->prev_len * sizeof(Entity),
+                                        cudaMemcpyDeviceToDevice, v->stream));
+            PG_CUDA(cudaStreamSynchronize(v->stream));
+            cudaFree(old_prev);
+        }
+        v->cap = n;
+    }
+    // verlet.rs:102: a different length means the Taylor first step.
+    const bool initial = !v->has_prev || v->prev_len != n;
+    if (n) {
+        PG_CUDA(cudaMemcpyAsync(v->d_in, entities, n * sizeof(Entity), cudaMemcpyHostToDevice,
+                                v->stream));
+        PG_CUDA(cudaMemcpyAsync(v->d_acc, acc, n * sizeof(Acceleration), cudaMemcpyHostToDevice,
+                                v->stream));
+        PG_TRY(launch_verlet_aos(v->d_in, v->d_prev, v->d_out, v->d_acc, n, dt, initial,
+                                 v->stream));
+        PG_CUDA(cudaMemcpyAsync(new_state, v->d_out, n * sizeof(Entity), cudaMemcpyDeviceToHost,
+                                v->stream));
+    }
+    PG_CUDA(cudaStreamSynchronize(v->stream));
+    // previous_state = entities (verlet.rs:31,81)
+    Entity *t = v->d_prev;
+    v->d_prev = v->d_in;
+    v->d_in = t;
+    v->prev_len = n;
+    v->has_prev = true;
+    return PHYSIM_OK;
+}
+
+void physim_gpu_verlet_destroy(PhysimVerlet *v)
+{
+    if (!v) return;
+    cudaSetDevice(v->device);
+    if (v->stream) cudaStreamSynchronize(v->stream);
+    if (v->d_in) cudaFree(v->d_in);
+    if (v->d_prev) cudaFree(v->d_prev);
+    if (v->d_out) cudaFree(v->d_out);
+    if (v->d_acc) cudaFree(v->d_acc);
+    if (v->stream) cudaStreamDestroy(v->stream);
+    delete v;
+}
+
+}  // extern "C"

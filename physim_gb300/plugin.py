@@ -1,0 +1,154 @@
+"""Host-side mirror of physim's transform-element handler.
+
+`TransformElementHandler` loads an element through the same C ABI that
+physim's Rust host uses (physim-core/src/plugin/transform.rs:52-134): it
+resolves `{name}_get_api`, calls `init` with the JSON property object, and
+calls `transform(obj, state, n, acc, n)` with host Entity / Acceleration
+arrays.  `Pipeline` restates the pipeline step that feeds them
+(physim-core/src/pipeline.rs:137-141,166-173): zeroed accelerations, every
+transform in order, then the integrator.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+from typing import Iterable
+
+import numpy as np
+
+from . import _lib
+from ._lib import lib, check
+from .entity import ACCELERATION, ENTITY, as_accelerations, as_entities
+
+_libc = C.CDLL(None)
+_libc.free.argtypes = [C.c_void_p]
+_libc.free.restype = None
+# physim hands plugins `host_alloc_string` (physim-core/src/plugin/meta.rs:137-155);
+# libc's strdup has the same contract and its result is freed with free().
+_strdup_addr = C.cast(_libc.strdup, C.c_void_p).value
+HOST_ALLOC = _lib.RustStringAllocFn(_strdup_addr)
+
+
+class NullElement(RuntimeError):
+    """init returned NULL (TransformElementLoadError::NullElement, transform.rs:72-76)."""
+
+
+def _take_string(ptr: int | None) -> str | None:
+    if not ptr:
+        return None
+    s = C.string_at(ptr).decode()
+    _libc.free(ptr)
+    return s
+
+
+def register(name: str) -> dict:
+    """Calls `{name}_register` with the host allocator and returns the metadata."""
+    meta = getattr(lib, f"{name}_register")(HOST_ALLOC)
+    out = {"kind": meta.kind}
+    for f in ("name", "plugin", "version", "license", "author", "blurb", "repo"):
+        out[f] = _take_string(getattr(meta, f))
+    return out
+
+
+class TransformElementHandler:
+    """One element instance created through `{name}_get_api()->init`."""
+
+    def __init__(self, name: str, properties: dict | None = None, *, raw_json: bytes | None = None):
+        self.name = name
+        self.api = getattr(lib, f"{name}_get_api")().contents
+        text = raw_json if raw_json is not None else json.dumps(properties or {}).encode()
+        buf = C.create_string_buffer(text, len(text))
+        self.instance = self.api.init(C.cast(buf, C.c_void_p), len(text))
+        if not self.instance:
+            raise NullElement(f"{name}: init rejected {text!r}")
+
+    def transform(self, state: np.ndarray, acc: np.ndarray) -> None:
+        """acc += this element's accelerations of `state` (in place)."""
+        state = as_entities(state)
+        if acc.dtype != ACCELERATION or acc.dtype.itemsize != 24:
+            raise TypeError("acc must be an ACCELERATION array (updated in place)")
+        if not (acc.flags.c_contiguous and acc.flags.writeable):
+            raise ValueError("acc must be C-contiguous and writeable")
+        self.api.transform(self.instance, state.ctypes.data, len(state), acc.ctypes.data, len(acc))
+
+    def get_property_descriptions(self) -> dict:
+        ptr = self.api.get_property_descriptions(self.instance, C.cast(HOST_ALLOC, C.c_void_p))
+        s = _take_string(ptr)
+        if s is None:
+            raise RuntimeError("Unable to load descriptions of properties")
+        return json.loads(s)
+
+    def post_configuration_messages(self) -> None:
+        self.api.post_configuration_messages(self.instance)
+
+    def recv_message(self, topic: str, message: str, priority: int = 2, sender: int = 0) -> None:
+        m = _lib.CMessage(priority, topic.encode(), message.encode(), sender, 0)
+        self.api.recv_message(self.instance, C.byref(m))
+
+    def destroy(self) -> None:
+        if self.instance:
+            self.api.destroy(self.instance)
+            self.instance = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.destroy()
+
+
+class GpuVerlet:
+    """The verlet integrator (integrators/src/verlet.rs) over host arrays, on the GPU."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(lib.physim_gpu_verlet_create(device, C.byref(h)), "physim_gpu_verlet_create")
+        self.handle = h
+
+    def integrate(self, entities: np.ndarray, acc: np.ndarray, dt: float) -> np.ndarray:
+        entities, acc = as_entities(entities), as_accelerations(acc)
+        new_state = np.empty_like(entities)
+        check(lib.physim_gpu_verlet_integrate(self.handle, entities.ctypes.data,
+                                              new_state.ctypes.data, len(entities),
+                                              acc.ctypes.data, dt),
+              "physim_gpu_verlet_integrate")
+        return new_state
+
+    def close(self) -> None:
+        if self.handle:
+            lib.physim_gpu_verlet_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Pipeline:
+    """pipeline.rs:137-173 restated: per step, zeroed accelerations, every
+    transform in order (`transform_fn`), then the integrator."""
+
+    def __init__(self, transforms: Iterable[TransformElementHandler], integrator: GpuVerlet,
+                 dt: float):
+        self.transforms = list(transforms)
+        self.integrator = integrator
+        self.dt = dt
+
+    def step(self, state: np.ndarray) -> np.ndarray:
+        acc = np.zeros(len(state), dtype=ACCELERATION)
+        for t in self.transforms:
+            t.transform(state, acc)
+        return self.integrator.integrate(state, acc, self.dt)
+
+    def run(self, state: np.ndarray, iterations: int) -> np.ndarray:
+        for _ in range(iterations):
+            state = self.step(state)
+        return state

@@ -1,0 +1,115 @@
+"""Device-resident simulations (physim_gpu_sim_* in include/physim_gb300.h)."""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._lib import (GRAVITY_ASTRO, GRAVITY_ASTRO2, GRAVITY_SIMPLE_ASTRO, TRAVERSAL_EXACT,
+                   TRAVERSAL_WARP, PhysimSimConfig, check, lib)
+from .entity import ACCELERATION, ENTITY, as_entities
+
+GRAVITY = {"simple_astro": GRAVITY_SIMPLE_ASTRO, "astro2": GRAVITY_ASTRO2, "astro": GRAVITY_ASTRO}
+TRAVERSAL = {"exact": TRAVERSAL_EXACT, "warp": TRAVERSAL_WARP}
+
+
+@dataclass
+class SimConfig:
+    gravity: str = "simple_astro"
+    theta: float = 1.0
+    e: float = 1.0
+    dt: float = 1e-6
+    leaf_size: int = 1
+    traversal: str = "exact"
+    compensated: bool = True
+    device: int = 0
+    stream: int | None = None  # a cudaStream_t (e.g. torch.cuda.Stream().cuda_stream)
+
+    def to_c(self) -> PhysimSimConfig:
+        c = PhysimSimConfig()
+        lib.physim_gpu_sim_config_default(C.byref(c))
+        c.gravity = GRAVITY[self.gravity]
+        c.theta = self.theta
+        c.e = self.e
+        c.dt = self.dt
+        c.leaf_size = self.leaf_size
+        c.traversal = TRAVERSAL[self.traversal]
+        c.compensated = 1 if self.compensated else 0
+        c.device = self.device
+        c.stream = self.stream or None
+        return c
+
+
+class Simulation:
+    """A simulation whose state stays on the GPU between steps."""
+
+    def __init__(self, state: np.ndarray, config: SimConfig):
+        state = as_entities(state)
+        self.n = len(state)
+        self.config = config
+        h = C.c_void_p()
+        cfg = config.to_c()
+        check(lib.physim_gpu_sim_create(C.byref(cfg), self.n, C.byref(h)),
+              "physim_gpu_sim_create")
+        self.handle = h
+        self.upload(state)
+
+    def upload(self, state: np.ndarray) -> None:
+        state = as_entities(state)
+        check(lib.physim_gpu_sim_upload(self.handle, state.ctypes.data, len(state)),
+              "physim_gpu_sim_upload")
+
+    def step(self, steps: int = 1) -> None:
+        check(lib.physim_gpu_sim_step(self.handle, steps), "physim_gpu_sim_step")
+
+    def synchronize(self) -> None:
+        check(lib.physim_gpu_sim_synchronize(self.handle), "physim_gpu_sim_synchronize")
+
+    def download(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=ENTITY)
+        check(lib.physim_gpu_sim_download(self.handle, out.ctypes.data, self.n),
+              "physim_gpu_sim_download")
+        return out
+
+    def accelerations(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=ACCELERATION)
+        check(lib.physim_gpu_sim_accelerations(self.handle, out.ctypes.data, self.n),
+              "physim_gpu_sim_accelerations")
+        return out
+
+    def set_profiling(self, enable: bool = True) -> None:
+        check(lib.physim_gpu_sim_set_profiling(self.handle, 1 if enable else 0),
+              "physim_gpu_sim_set_profiling")
+
+    def last_step_ms(self) -> tuple[float, float]:
+        """(gravity kernels, integrator) device milliseconds of the last step."""
+        g, i = C.c_double(), C.c_double()
+        check(lib.physim_gpu_sim_last_step_ms(self.handle, C.byref(g), C.byref(i)),
+              "physim_gpu_sim_last_step_ms")
+        return g.value, i.value
+
+    @property
+    def stream(self) -> int:
+        return lib.physim_gpu_sim_stream(self.handle) or 0
+
+    @property
+    def launches_per_step(self) -> int:
+        return lib.physim_gpu_sim_launches_per_step(self.handle)
+
+    def close(self) -> None:
+        if self.handle:
+            lib.physim_gpu_sim_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
