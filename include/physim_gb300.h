@@ -255,6 +255,30 @@ int physim_gpu_sim_set_profiling(PhysimSim *sim, int enable);
 int physim_gpu_sim_last_step_ms(PhysimSim *sim, double *gravity_ms, double *integrate_ms);
 void physim_gpu_sim_destroy(PhysimSim *sim);
 
+/* The Barnes-Hut tree of a simulation's current state, copied to host arrays
+ * supplied by the caller (any pointer may be NULL).  Nodes are stored level by
+ * level; the children of a node are contiguous and in octant order. */
+typedef struct PhysimTreeSnapshot {
+    size_t cap_nodes;      /* in: capacity of the node_* arrays */
+    uint64_t *keys;        /* [n] Morton key of each sorted position */
+    uint32_t *order;       /* [n] body index at each sorted position */
+    int32_t *node_begin;   /* [cap] first sorted body of the node */
+    int32_t *node_count;   /* [cap] bodies in the node */
+    int32_t *node_child;   /* [cap] index of the first child, -1 for a leaf */
+    uint8_t *node_nchild;  /* [cap] number of children */
+    uint8_t *node_level;   /* [cap] depth below the root */
+    double *node_centre;   /* [4*m] planes cx, cy, cz, half-width; m = min(n_nodes, cap) */
+    float *node_com;       /* [4*cap] centre of mass x, y, z and mass, per node */
+    size_t n_bodies;       /* out */
+    size_t n_nodes;        /* out: nodes in the tree */
+    double extent;         /* out: root half-width X (transformers.rs:126-132) */
+    uint32_t flags;        /* out: bit 0 node arrays full (tree truncated), bit 1 stack overflow */
+} PhysimTreeSnapshot;
+
+/* Builds the tree of the current state of an astro/astro2 simulation and
+ * copies it out. */
+int physim_gpu_sim_tree_snapshot(PhysimSim *sim, PhysimTreeSnapshot *out);
+
 /* Verlet integrator over host arrays (integrators/src/verlet.rs:19-121).
  * A Rust IntegratorElement shim evaluates acc_fn itself and hands the
  * accelerations over; the step runs on the GPU in f64 in the reference's

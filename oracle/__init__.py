@@ -73,6 +73,9 @@ def load() -> C.CDLL:
         "oracle_verlet_step": (i32, [vp, vp, vp, sz, vp, dbl]),
         "oracle_run_pipeline": (i32, [vp, sz, i32, dbl, dbl, dbl, i32, i32]),
         "oracle_max_threads": (i32, []),
+        "bh_model_extent": (dbl, [vp, sz]),
+        "bh_model_keys": (None, [vp, sz, i32, vp]),
+        "bh_model_build": (C.c_long, [vp, sz, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, sz]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -222,3 +225,30 @@ class Tree:
             self.lib.oracle_tree_free(self.h)
         except Exception:
             pass
+
+
+def bh_model(state: np.ndarray, nchild: int = 8, leaf: int = 16) -> dict:
+    """The CPU model of the GPU tree build (bh_model.c): keys, sort order and
+    the level-by-level tree, for bit-exact comparison with the GPU."""
+    lib = load()
+    state = _ent(state)
+    n = len(state)
+    cap = 4 * max(n, 64) + 64 * 31
+    keys = np.zeros(n, np.uint64)
+    order = np.zeros(n, np.uint32)
+    nb = np.zeros(cap, np.int32)
+    nc = np.zeros(cap, np.int32)
+    ch = np.zeros(cap, np.int32)
+    nn = np.zeros(cap, np.uint8)
+    lvl = np.zeros(cap, np.uint8)
+    cen = np.zeros(4 * cap, np.float64)
+    total = lib.bh_model_build(state.ctypes.data, n, nchild, leaf, keys.ctypes.data,
+                               order.ctypes.data, nb.ctypes.data, nc.ctypes.data, ch.ctypes.data,
+                               nn.ctypes.data, lvl.ctypes.data, cen.ctypes.data, cap)
+    if total < 0:
+        raise RuntimeError("model tree capacity exceeded")
+    m = int(total)
+    cen = cen.reshape(4, cap)[:, :m]
+    return {"keys": keys, "order": order, "begin": nb[:m], "count": nc[:m], "child": ch[:m],
+            "nchild": nn[:m], "level": lvl[:m], "centre": cen,
+            "extent": lib.bh_model_extent(state.ctypes.data, n)}

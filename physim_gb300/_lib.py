@@ -59,6 +59,15 @@ class PhysimSimConfig(C.Structure):
                 ("reserved", C.c_uint32 * 3)]
 
 
+class PhysimTreeSnapshot(C.Structure):
+    _fields_ = [("cap_nodes", C.c_size_t), ("keys", C.c_void_p), ("order", C.c_void_p),
+                ("node_begin", C.c_void_p), ("node_count", C.c_void_p),
+                ("node_child", C.c_void_p), ("node_nchild", C.c_void_p),
+                ("node_level", C.c_void_p), ("node_centre", C.c_void_p),
+                ("node_com", C.c_void_p), ("n_bodies", C.c_size_t), ("n_nodes", C.c_size_t),
+                ("extent", C.c_double), ("flags", C.c_uint32)]
+
+
 ELEMENTS = ("astro", "astro2", "simple_astro")
 ELEMENT_SUFFIXES = ("get_api", "register", "init", "transform", "destroy",
                     "get_property_descriptions", "recv_message", "post_configuration_messages")
@@ -88,6 +97,7 @@ def _load() -> C.CDLL:
         "physim_gpu_sim_set_profiling": (C.c_int, [vp, C.c_int]),
         "physim_gpu_sim_last_step_ms": (C.c_int, [vp, C.POINTER(dbl), C.POINTER(dbl)]),
         "physim_gpu_sim_destroy": (None, [vp]),
+        "physim_gpu_sim_tree_snapshot": (C.c_int, [vp, C.POINTER(PhysimTreeSnapshot)]),
         "physim_gpu_verlet_create": (C.c_int, [i32, C.POINTER(vp)]),
         "physim_gpu_verlet_integrate": (C.c_int, [vp, vp, vp, sz, vp, dbl]),
         "physim_gpu_verlet_destroy": (None, [vp]),

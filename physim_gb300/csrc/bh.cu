@@ -1,22 +1,1068 @@
-// bh.cu -- Barnes-Hut on the GPU (placeholder until the tree kernels land).
+// bh.cu -- Barnes-Hut gravity on the GPU: the astro2 (octree) and astro
+// (quadtree) elements, astro/src/transformers.rs:31-69,122-160, over the
+// reference's tree semantics (astro/src/octree.rs, astro/src/quadtree.rs).
+//
+// Pipeline, all on the device (no host round trip, so it can be captured):
+//   1. extent    X = max_i max(|x_i|,|y_i|,|z_i|) in f64 (transformers.rs:126-131);
+//                the root cell is centred at the origin with half-width X.
+//   2. keys      per axis the cell index q at the finest level D, with the
+//                reference's octant rule (p > centre goes high, ties low,
+//                octree.rs:160-165), interleaved x-lowest into a Morton key:
+//                octree 21 levels x 3 bits = 63 bits, quadtree 31 x 2 = 62.
+//                Bodies within a rounding margin of a cell boundary re-derive
+//                q by replaying the reference's f64 centre arithmetic.
+//   3. sort      stable LSD radix sort of (key, body) pairs, 8-bit digits.
+//   4. tree      level-by-level, not path-compressed (as the reference's
+//                pointer tree): a cell with more than leaf_size bodies that
+//                are not all at one key splits into its non-empty children;
+//                children are contiguous, levels are contiguous, and node
+//                order is deterministic (per-level scans, no atomics).
+//                Geometric centres are computed exactly as the reference does
+//                (child = parent +- extent/2, octree.rs:167-215).
+//   5. moments   mass and centre of mass of every cell from f64 prefix sums
+//                over the sorted bodies.
+//   6. traversal one warp per 32 consecutive sorted bodies, DFS with a shared
+//                stack, the reference's opening rule extent/|x - centre| < theta
+//                (octree.rs:137-144).  EXACT: every body keeps its own
+//                interaction list (the reference's); WARP: a cell is accepted
+//                only if all 32 bodies accept it, and the common list is
+//                batched through shared memory.  Pair law in FP32 with one
+//                MUFU.RSQ per pair and compensated per-body sums.
+#include <stdio.h>
+#include <string.h>
+
 #include "common.cuh"
 #include "engine.h"
 #include "plugin_state.h"
 
 namespace pg {
-struct BhWorkspace {
-    int dummy;
+
+namespace {
+
+constexpr int kRadixBits = 8;
+constexpr int kRadixBuckets = 1 << kRadixBits;
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 keys per block
+constexpr int kSortWarps = kSortThreads / 32;
+
+constexpr int kBuildThreads = 256;
+constexpr int kScanThreads = 1024;
+constexpr int kMaxLevels = 31;
+
+constexpr int kTravWarps = 4;
+constexpr int kStack = 192;
+constexpr int kBuf = 128;
+
+// flags[0]: node capacity exceeded (tree truncated; results stay exact)
+// flags[1]: traversal stack overflow (results of the affected warp invalid)
+constexpr int kFlagNodes = 0;
+constexpr int kFlagStack = 1;
+
+struct LevelInfo {
+    int32_t begin[kMaxLevels + 2];
+    int32_t count[kMaxLevels + 2];
+    int32_t total;  // nodes in the tree
 };
-int bh_reserve(BhWorkspace *&ws, size_t, int)
+
+__host__ __device__ inline int tree_levels(int nchild) { return nchild == 8 ? 21 : 31; }
+__host__ __device__ inline int level_bits(int nchild) { return nchild == 8 ? 3 : 2; }
+
+// ---------------------------------------------------------------------------
+// 1. extent
+// ---------------------------------------------------------------------------
+__global__ void extent_kernel(const double *__restrict__ x, const double *__restrict__ y,
+                              const double *__restrict__ z, int n,
+                              unsigned long long *__restrict__ out_bits)
 {
-    if (!ws) ws = new BhWorkspace();
+    double m = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        m = fmax(m, fabs(x[i]));
+        m = fmax(m, fabs(y[i]));
+        m = fmax(m, fabs(z[i]));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ double wm[32];
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? wm[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        // non-negative doubles order like their bit patterns
+        if (threadIdx.x == 0) atomicMax(out_bits, (unsigned long long)__double_as_longlong(m));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 2. keys
+// ---------------------------------------------------------------------------
+// Cell index of coordinate p at the finest level D: the reference descends
+// from centre 0 / half-width X deciding `p > centre` at every level.
+__device__ __forceinline__ uint32_t axis_cell(double p, double X, double scale, int D)
+{
+    const double lim = (double)((1u << D) - 1u);
+    double u = __dmul_rn(__dadd_rn(p, X), scale);  // (p + X) / (2X) * 2^D
+    double r = rint(u);
+    const double margin = ldexp(1.0, D - 40);
+    if (fabs(u - r) >= margin || !(u == u)) {
+        double q = ceil(u) - 1.0;
+        q = fmin(fmax(q, 0.0), lim);
+        return (uint32_t)q;
+    }
+    // Close to a boundary: replay the reference's centre arithmetic.
+    double c = 0.0, ext = X;
+    uint32_t q = 0;
+    for (int d = 0; d < D; ++d) {
+        const bool hi = p > c;
+        const double h = __ddiv_rn(ext, 2.0);
+        c = hi ? __dadd_rn(c, h) : __dsub_rn(c, h);
+        ext = h;
+        q = (q << 1) | (hi ? 1u : 0u);
+    }
+    return q;
+}
+
+__device__ __forceinline__ uint64_t spread3(uint32_t v)
+{
+    uint64_t x = v & 0x1fffffu;
+    x = (x | x << 32) & 0x1f00000000ffffull;
+    x = (x | x << 16) & 0x1f0000ff0000ffull;
+    x = (x | x << 8) & 0x100f00f00f00f00full;
+    x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+    x = (x | x << 2) & 0x1249249249249249ull;
+    return x;
+}
+
+__device__ __forceinline__ uint64_t spread2(uint32_t v)
+{
+    uint64_t x = v & 0x7fffffffu;
+    x = (x | x << 16) & 0x0000ffff0000ffffull;
+    x = (x | x << 8) & 0x00ff00ff00ff00ffull;
+    x = (x | x << 4) & 0x0f0f0f0f0f0f0f0full;
+    x = (x | x << 2) & 0x3333333333333333ull;
+    x = (x | x << 1) & 0x5555555555555555ull;
+    return x;
+}
+
+__global__ void keys_kernel(const double *__restrict__ x, const double *__restrict__ y,
+                            const double *__restrict__ z, int n, int nchild,
+                            const unsigned long long *__restrict__ extent_bits,
+                            uint64_t *__restrict__ keys, uint32_t *__restrict__ vals)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double X = __longlong_as_double((long long)*extent_bits);
+    const int D = tree_levels(nchild);
+    uint64_t key = 0;
+    if (X > 0.0) {
+        const double scale = __ddiv_rn(ldexp(1.0, D - 1), X);
+        const uint32_t qx = axis_cell(x[i], X, scale, D);
+        const uint32_t qy = axis_cell(y[i], X, scale, D);
+        if (nchild == 8) {
+            const uint32_t qz = axis_cell(z[i], X, scale, D);
+            key = spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2);
+        } else {
+            key = spread2(qx) | (spread2(qy) << 1);
+        }
+    }
+    keys[i] = key;
+    vals[i] = (uint32_t)i;
+}
+
+// ---------------------------------------------------------------------------
+// 3. radix sort (stable, LSD, 8-bit digits)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t lanemask_lt()
+{
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__global__ void __launch_bounds__(kSortThreads)
+radix_hist_kernel(const uint64_t *__restrict__ keys, int n, int shift, uint32_t *__restrict__ hist,
+                  int n_tiles)
+{
+    __shared__ uint32_t h[kSortWarps][kRadixBuckets];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = threadIdx.x; k < kSortWarps * kRadixBuckets; k += kSortThreads)
+        (&h[0][0])[k] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kSortTile + warp * (kSortItems * 32);
+    for (int r = 0; r < kSortItems; ++r) {
+        const int idx = base + r * 32 + lane;
+        const bool valid = idx < n;
+        const uint32_t d = valid ? (uint32_t)(keys[idx] >> shift) & (kRadixBuckets - 1) : 0xffffffffu;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        if (valid && (peers & lanemask_lt()) == 0) h[warp][d] += __popc(peers);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kRadixBuckets; d += kSortThreads) {
+        uint32_t s = 0;
+        for (int w = 0; w < kSortWarps; ++w) s += h[w][d];
+        hist[(size_t)d * n_tiles + blockIdx.x] = s;
+    }
+}
+
+// Exclusive scan of `count` uint32 values in place, one block.
+__global__ void __launch_bounds__(kScanThreads) scan_u32_kernel(uint32_t *__restrict__ v, int count)
+{
+    __shared__ uint32_t part[kScanThreads];
+    const int per = (count + kScanThreads - 1) / kScanThreads;
+    const int b = threadIdx.x * per, e = min(b + per, count);
+    uint32_t s = 0;
+    for (int k = b; k < e; ++k) s += v[k];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < kScanThreads; off <<= 1) {
+        uint32_t t = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+        __syncthreads();
+        part[threadIdx.x] += t;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - s;
+    for (int k = b; k < e; ++k) {
+        uint32_t t = v[k];
+        v[k] = run;
+        run += t;
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads)
+radix_scatter_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
+                     uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int n,
+                     int shift, const uint32_t *__restrict__ offsets, int n_tiles)
+{
+    __shared__ uint32_t h[kSortWarps][kRadixBuckets];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = threadIdx.x; k < kSortWarps * kRadixBuckets; k += kSortThreads)
+        (&h[0][0])[k] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kSortTile + warp * (kSortItems * 32);
+    uint64_t kk[kSortItems];
+    uint32_t vv[kSortItems];
+    uint32_t rank[kSortItems];
+    for (int r = 0; r < kSortItems; ++r) {
+        const int idx = base + r * 32 + lane;
+        const bool valid = idx < n;
+        kk[r] = valid ? keys_in[idx] : 0;
+        vv[r] = valid ? (vals_in ? vals_in[idx] : (uint32_t)idx) : 0;
+        const uint32_t d = valid ? (uint32_t)(kk[r] >> shift) & (kRadixBuckets - 1) : 0xffffffffu;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t before = __popc(peers & lanemask_lt());
+        uint32_t cur = 0;
+        if (valid) cur = h[warp][d];
+        __syncwarp();
+        if (valid && before == 0) h[warp][d] = cur + __popc(peers);
+        __syncwarp();
+        rank[r] = cur + before;
+    }
+    __syncthreads();
+    // exclusive prefix over warps, per digit, plus the global offset
+    for (int d = threadIdx.x; d < kRadixBuckets; d += kSortThreads) {
+        uint32_t run = offsets[(size_t)d * n_tiles + blockIdx.x];
+        for (int w = 0; w < kSortWarps; ++w) {
+            uint32_t c = h[w][d];
+            h[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    for (int r = 0; r < kSortItems; ++r) {
+        const int idx = base + r * 32 + lane;
+        if (idx >= n) continue;
+        const uint32_t d = (uint32_t)(kk[r] >> shift) & (kRadixBuckets - 1);
+        const uint32_t pos = h[warp][d] + rank[r];
+        keys_out[pos] = kk[r];
+        vals_out[pos] = vv[r];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// gather of sorted bodies
+// ---------------------------------------------------------------------------
+__global__ void gather_kernel(const uint32_t *__restrict__ order, int n,
+                              const float4 *__restrict__ body4, const double *__restrict__ x,
+                              const double *__restrict__ y, const double *__restrict__ z,
+                              const double *__restrict__ m, float4 *__restrict__ sbody,
+                              double *__restrict__ spos, double *__restrict__ smass)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t i = order[k];
+    sbody[k] = body4[i];
+    spos[k] = x[i];
+    spos[n + k] = y[i];
+    spos[2 * (size_t)n + k] = z[i];
+    smass[k] = m[i];
+}
+
+// ---------------------------------------------------------------------------
+// 4. tree build
+// ---------------------------------------------------------------------------
+struct NodeArrays {
+    int32_t *begin, *count, *child;
+    uint8_t *nchild, *level;
+    double *c64;   // 4 x cap: cx, cy, cz, extent
+    float4 *geo;   // cx, cy, cz, extent (f32)
+    float4 *com;   // x, y, z, mass (f32)
+    int cap;
+};
+
+__global__ void root_kernel(NodeArrays nd, LevelInfo *lv, int n,
+                            const unsigned long long *__restrict__ extent_bits)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double X = __longlong_as_double((long long)*extent_bits);
+    for (int d = 0; d < kMaxLevels + 2; ++d) {
+        lv->begin[d] = 0;
+        lv->count[d] = 0;
+    }
+    lv->total = n > 0 ? 1 : 0;
+    lv->count[0] = n > 0 ? 1 : 0;
+    lv->begin[1] = 1;
+    nd.begin[0] = 0;
+    nd.count[0] = n;
+    nd.child[0] = -1;
+    nd.nchild[0] = 0;
+    nd.level[0] = 0;
+    nd.c64[0] = 0.0;
+    nd.c64[nd.cap] = 0.0;
+    nd.c64[2 * (size_t)nd.cap] = 0.0;
+    nd.c64[3 * (size_t)nd.cap] = X;
+}
+
+// Child ranges of a node: bounds[c] = first sorted index in [b, e) whose
+// digit at `shift` is >= c; bounds[nchild] = e.
+__device__ __forceinline__ void child_bounds(const uint64_t *__restrict__ keys, int b, int e,
+                                             int shift, int nchild, int *bounds)
+{
+    const uint32_t mask = nchild - 1;
+    bounds[0] = b;
+    for (int c = 1; c < nchild; ++c) {
+        int lo = bounds[c - 1], hi = e;
+        while (lo < hi) {
+            int mid = (lo + hi) >> 1;
+            if (((uint32_t)(keys[mid] >> shift) & mask) < (uint32_t)c)
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        bounds[c] = lo;
+    }
+    bounds[nchild] = e;
+}
+
+__device__ __forceinline__ bool node_splits(const uint64_t *__restrict__ keys, int b, int cnt,
+                                            int leaf, int level, int D)
+{
+    return level < D && cnt > leaf && keys[b] != keys[b + cnt - 1];
+}
+
+__device__ int node_child_count(const uint64_t *__restrict__ keys, const NodeArrays &nd, int node,
+                                int leaf, int level, int D, int bits, int nchild)
+{
+    const int b = nd.begin[node], cnt = nd.count[node];
+    if (!node_splits(keys, b, cnt, leaf, level, D)) return 0;
+    int bounds[9];
+    child_bounds(keys, b, b + cnt, bits * (D - level - 1), nchild, bounds);
+    int k = 0;
+    for (int c = 0; c < nchild; ++c) k += bounds[c + 1] > bounds[c];
+    return k;
+}
+
+// Per-block sums of child counts over the level's nodes (block b takes a
+// contiguous chunk).
+__global__ void __launch_bounds__(kBuildThreads)
+level_count_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, const LevelInfo *__restrict__ lv,
+                   int level, int leaf, int nchild, int32_t *__restrict__ bsum)
+{
+    const int D = tree_levels(nchild), bits = level_bits(nchild);
+    const int cnt = lv->count[level], first = lv->begin[level];
+    const int chunk = (cnt + gridDim.x - 1) / gridDim.x;
+    const int cb = blockIdx.x * chunk, ce = min(cb + chunk, cnt);
+    int s = 0;
+    for (int k = cb + threadIdx.x; k < ce; k += blockDim.x)
+        s += node_child_count(keys, nd, first + k, leaf, level, D, bits, nchild);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ int ws[kBuildThreads / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < kBuildThreads / 32; ++w) t += ws[w];
+        bsum[blockIdx.x] = t;
+    }
+}
+
+// Exclusive scan of the block sums; sizes the next level (truncating the
+// tree if the node arrays would overflow).
+__global__ void __launch_bounds__(kScanThreads)
+level_scan_kernel(int32_t *__restrict__ bsum, int nblocks, LevelInfo *lv, int level, int cap,
+                  uint32_t *__restrict__ flags)
+{
+    __shared__ int32_t part[kScanThreads];
+    const int per = (nblocks + kScanThreads - 1) / kScanThreads;
+    const int b = threadIdx.x * per, e = min(b + per, nblocks);
+    int32_t s = 0;
+    for (int k = b; k < e; ++k) s += bsum[k];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < kScanThreads; off <<= 1) {
+        int32_t t = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+        __syncthreads();
+        part[threadIdx.x] += t;
+        __syncthreads();
+    }
+    int32_t run = part[threadIdx.x] - s;
+    for (int k = b; k < e; ++k) {
+        int32_t t = bsum[k];
+        bsum[k] = run;
+        run += t;
+    }
+    if (threadIdx.x == kScanThreads - 1) {
+        const int32_t total = part[kScanThreads - 1];
+        const int32_t nb = lv->begin[level] + lv->count[level];
+        int32_t take = total;
+        if ((long long)nb + total > cap) {
+            take = 0;  // leave this level's nodes as leaves: exact, slower
+            atomicOr(&flags[kFlagNodes], 1u);
+        }
+        lv->begin[level + 1] = nb;
+        lv->count[level + 1] = take;
+        lv->total = nb + take;
+    }
+}
+
+__global__ void __launch_bounds__(kBuildThreads)
+level_write_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, const LevelInfo *__restrict__ lv,
+                   int level, int leaf, int nchild, const int32_t *__restrict__ boff)
+{
+    const int D = tree_levels(nchild), bits = level_bits(nchild);
+    const int cnt = lv->count[level], first = lv->begin[level];
+    if (lv->count[level + 1] == 0) return;  // nothing to write (or truncated)
+    const int child_base = lv->begin[level + 1];
+    const int chunk = (cnt + gridDim.x - 1) / gridDim.x;
+    const int cb = blockIdx.x * chunk, ce = min(cb + chunk, cnt);
+    __shared__ int32_t ws[kBuildThreads / 32];
+    __shared__ int32_t carry;
+    if (threadIdx.x == 0) carry = boff[blockIdx.x];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k0 = cb; k0 < ce; k0 += blockDim.x) {
+        const int k = k0 + threadIdx.x;
+        const int node = first + k;
+        int bounds[9];
+        int nc = 0;
+        bool split = false;
+        if (k < ce) {
+            const int b = nd.begin[node], c = nd.count[node];
+            split = node_splits(keys, b, c, leaf, level, D);
+            if (split) {
+                child_bounds(keys, b, b + c, bits * (D - level - 1), nchild, bounds);
+                for (int q = 0; q < nchild; ++q) nc += bounds[q + 1] > bounds[q];
+            }
+        }
+        // block-wide exclusive scan of nc
+        int incl = nc;
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) ws[warp] = incl;
+        __syncthreads();
+        int wbase = 0;
+        for (int w = 0; w < warp; ++w) wbase += ws[w];
+        const int excl = carry + wbase + incl - nc;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = excl + nc;
+        if (k < ce) {
+            if (split) {
+                const int fc = child_base + excl;
+                nd.child[node] = fc;
+                nd.nchild[node] = (uint8_t)nc;
+                const size_t cap = nd.cap;
+                const double pcx = nd.c64[node], pcy = nd.c64[cap + node];
+                const double pcz = nd.c64[2 * cap + node], pext = nd.c64[3 * cap + node];
+                const double h = __ddiv_rn(pext, 2.0);
+                int w = 0;
+                for (int q = 0; q < nchild; ++q) {
+                    if (bounds[q + 1] <= bounds[q]) continue;
+                    const int ci = fc + w++;
+                    nd.begin[ci] = bounds[q];
+                    nd.count[ci] = bounds[q + 1] - bounds[q];
+                    nd.child[ci] = -1;
+                    nd.nchild[ci] = 0;
+                    nd.level[ci] = (uint8_t)(level + 1);
+                    nd.c64[ci] = (q & 1) ? __dadd_rn(pcx, h) : __dsub_rn(pcx, h);
+                    nd.c64[cap + ci] = (q & 2) ? __dadd_rn(pcy, h) : __dsub_rn(pcy, h);
+                    nd.c64[2 * cap + ci] =
+                        nchild == 8 ? ((q & 4) ? __dadd_rn(pcz, h) : __dsub_rn(pcz, h)) : pcz;
+                    nd.c64[3 * cap + ci] = h;
+                }
+            } else {
+                nd.child[node] = -1;
+                nd.nchild[node] = 0;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 5. moments: exclusive prefix sums of m, m x, m y, m z over sorted bodies
+// ---------------------------------------------------------------------------
+constexpr int kMomThreads = 256;
+
+__global__ void __launch_bounds__(kMomThreads)
+moment_partial_kernel(const double *__restrict__ spos, const double *__restrict__ smass, int n,
+                      double *__restrict__ bsum)
+{
+    const int chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int cb = blockIdx.x * chunk, ce = min(cb + chunk, n);
+    double s[4] = {0, 0, 0, 0};
+    for (int k = cb + threadIdx.x; k < ce; k += blockDim.x) {
+        const double m = smass[k];
+        s[0] += m;
+        s[1] += m * spos[k];
+        s[2] += m * spos[n + k];
+        s[3] += m * spos[2 * (size_t)n + k];
+    }
+    __shared__ double red[4][kMomThreads];
+    for (int c = 0; c < 4; ++c) red[c][threadIdx.x] = s[c];
+    __syncthreads();
+    for (int off = kMomThreads / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off)
+            for (int c = 0; c < 4; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x < 4) bsum[threadIdx.x * gridDim.x + blockIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void moment_blockscan_kernel(double *__restrict__ bsum, int nblocks)
+{
+    // 4 sequential exclusive scans of nblocks values (nblocks <= a few thousand)
+    const int c = threadIdx.x;
+    if (c >= 4) return;
+    double run = 0.0;
+    for (int b = 0; b < nblocks; ++b) {
+        double t = bsum[c * nblocks + b];
+        bsum[c * nblocks + b] = run;
+        run += t;
+    }
+}
+
+__global__ void __launch_bounds__(kMomThreads)
+moment_scan_kernel(const double *__restrict__ spos, const double *__restrict__ smass, int n,
+                   const double *__restrict__ boff, double *__restrict__ pref)
+{
+    const int chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int cb = blockIdx.x * chunk, ce = min(cb + chunk, n);
+    const size_t stride = (size_t)n + 1;
+    __shared__ double carry[4];
+    __shared__ double ws[4][kMomThreads / 32];
+    if (threadIdx.x < 4) carry[threadIdx.x] = boff[threadIdx.x * gridDim.x + blockIdx.x];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k0 = cb; k0 < ce; k0 += blockDim.x) {
+        const int k = k0 + threadIdx.x;
+        double v[4] = {0, 0, 0, 0};
+        if (k < ce) {
+            const double m = smass[k];
+            v[0] = m;
+            v[1] = m * spos[k];
+            v[2] = m * spos[n + k];
+            v[3] = m * spos[2 * (size_t)n + k];
+        }
+        double incl[4];
+        for (int c = 0; c < 4; ++c) {
+            incl[c] = v[c];
+            for (int o = 1; o < 32; o <<= 1) {
+                double t = __shfl_up_sync(0xffffffffu, incl[c], o);
+                if (lane >= o) incl[c] += t;
+            }
+            if (lane == 31) ws[c][warp] = incl[c];
+        }
+        __syncthreads();
+        double excl[4];
+        for (int c = 0; c < 4; ++c) {
+            double wb = 0.0;
+            for (int w = 0; w < warp; ++w) wb += ws[c][w];
+            excl[c] = carry[c] + wb + incl[c] - v[c];
+        }
+        __syncthreads();
+        if (k < ce)
+            for (int c = 0; c < 4; ++c) pref[c * stride + k] = excl[c];
+        if (threadIdx.x == blockDim.x - 1)
+            for (int c = 0; c < 4; ++c) carry[c] = excl[c] + v[c];
+        __syncthreads();
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
+        for (int c = 0; c < 4; ++c) pref[c * stride + n] = carry[c];
+}
+
+__global__ void node_finish_kernel(NodeArrays nd, const LevelInfo *__restrict__ lv,
+                                   const double *__restrict__ pref, int n,
+                                   const float4 *__restrict__ sbody, const double *__restrict__ spos)
+{
+    const int total = lv->total;
+    const size_t stride = (size_t)n + 1;
+    const size_t cap = nd.cap;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int b = nd.begin[i], e = b + nd.count[i];
+        nd.geo[i] = make_float4((float)nd.c64[i], (float)nd.c64[cap + i], (float)nd.c64[2 * cap + i],
+                                (float)nd.c64[3 * cap + i]);
+        float4 com;
+        const bool same_pos = spos[b] == spos[e - 1] && spos[n + b] == spos[n + e - 1] &&
+                              spos[2 * (size_t)n + b] == spos[2 * (size_t)n + e - 1];
+        const double M = pref[e] - pref[b];
+        if (e - b == 1) {
+            // a single body: the body itself, so it cancels against itself in
+            // the pair law as the reference's equal-centre skip does
+            com = sbody[b];
+        } else if (same_pos) {
+            com = sbody[b];
+            com.w = (float)M;
+        } else if (M != 0.0) {
+            com = make_float4((float)((pref[stride + e] - pref[stride + b]) / M),
+                              (float)((pref[2 * stride + e] - pref[2 * stride + b]) / M),
+                              (float)((pref[3 * stride + e] - pref[3 * stride + b]) / M), (float)M);
+        } else {
+            com = make_float4((float)nd.c64[i], (float)nd.c64[cap + i], (float)nd.c64[2 * cap + i],
+                              0.f);
+        }
+        nd.com[i] = com;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 6. traversal
+// ---------------------------------------------------------------------------
+struct TravArgs {
+    NodeArrays nd;
+    const float4 *sbody;
+    const double *spos;
+    const uint32_t *order;
+    const LevelInfo *lv;
+    int n;
+    float theta, e;
+    double theta64;
+    uint32_t *flags;
+    double *partial;
+};
+
+// The reference's opening rule `extent / r < theta` (octree.rs:137-144):
+// FP32, re-evaluated in f64 with the reference's arithmetic near the edge.
+__device__ __forceinline__ bool accept_cell(const TravArgs &a, int node, float4 geo, float qx,
+                                            float qy, float qz, int k)
+{
+    const float dx = qx - geo.x, dy = qy - geo.y, dz = qz - geo.z;
+    const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float ratio = geo.w / r;
+    const float band = 1e-4f * fabsf(a.theta) + 1e-30f;
+    if (fabsf(ratio - a.theta) > band && ratio == ratio) return ratio < a.theta;
+    const size_t cap = a.nd.cap;
+    const double d0 = a.spos[k] - a.nd.c64[node];
+    const double d1 = a.spos[a.n + k] - a.nd.c64[cap + node];
+    const double d2 = a.spos[2 * (size_t)a.n + k] - a.nd.c64[2 * cap + node];
+    const double r64 = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    return a.nd.c64[3 * cap + node] / r64 < a.theta64;
+}
+
+__device__ __forceinline__ void pair_acc(float qx, float qy, float qz, float4 b, float e,
+                                         float &ax, float &ay, float &az)
+{
+    const float dx = b.x - qx, dy = b.y - qy, dz = b.z - qz;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float w = r2 + e;
+    const float q = fmaf(r2, w * w, kPairGuard);
+    const float s = b.w * rsqrt_approx(q);
+    ax = fmaf(dx, s, ax);
+    ay = fmaf(dy, s, ay);
+    az = fmaf(dz, s, az);
+}
+
+__device__ __forceinline__ void fold(float &hi, float &lo, float &t)
+{
+    float s, err;
+    two_sum(hi, t, s, err);
+    hi = s;
+    lo += err;
+    t = 0.f;
+}
+
+struct StackEntry {
+    int32_t node;
+    uint32_t mask;
+};
+
+__global__ void __launch_bounds__(kTravWarps * 32)
+traverse_exact_kernel(TravArgs a)
+{
+    __shared__ StackEntry stack[kTravWarps][kStack];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int k0 = (blockIdx.x * kTravWarps + warp) * 32;
+    if (k0 >= a.n) return;
+    const int k = k0 + lane;
+    const bool valid = k < a.n;
+    const uint32_t active = __ballot_sync(0xffffffffu, valid);
+    const float4 q = valid ? a.sbody[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float ax = 0.f, ay = 0.f, az = 0.f, hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+    int sp = 0;
+    if (lane == 0) stack[warp][0] = {0, active};
+    sp = 1;
+    int since_fold = 0;
+    __syncwarp();
+    while (sp > 0) {
+        const StackEntry top = stack[warp][sp - 1];
+        --sp;
+        __syncwarp();
+        const int node = top.node;
+        const bool in = (top.mask >> lane) & 1u;
+        const float4 geo = a.nd.geo[node];
+        const int child = a.nd.child[node];
+        bool acc = false;
+        if (in) acc = accept_cell(a, node, geo, q.x, q.y, q.z, k);
+        const uint32_t open = top.mask & ~__ballot_sync(0xffffffffu, acc);
+        if (acc) {
+            pair_acc(q.x, q.y, q.z, a.nd.com[node], a.e, ax, ay, az);
+        }
+        ++since_fold;
+        if (child < 0) {
+            if (open) {
+                const int b = a.nd.begin[node], c = a.nd.count[node];
+                const bool mine = (open >> lane) & 1u;
+                for (int j = b; j < b + c; ++j) {
+                    const float4 bj = a.sbody[j];
+                    if (mine) pair_acc(q.x, q.y, q.z, bj, a.e, ax, ay, az);
+                }
+                since_fold += c;
+            }
+        } else if (open) {
+            const int nc = a.nd.nchild[node];
+            if (sp + nc > kStack) {
+                if (lane == 0) atomicOr(&a.flags[kFlagStack], 1u);
+                break;
+            }
+            // push children 0..nc-1 so the last child is popped first, the
+            // reference's pop order (octree.rs:152-154)
+            if (lane < nc) stack[warp][sp + lane] = {child + lane, open};
+            sp += nc;
+            __syncwarp();
+        }
+        if (since_fold >= 64) {
+            fold(hx, lx, ax);
+            fold(hy, ly, ay);
+            fold(hz, lz, az);
+            since_fold = 0;
+        }
+    }
+    fold(hx, lx, ax);
+    fold(hy, ly, ay);
+    fold(hz, lz, az);
+    if (valid) {
+        const uint32_t i = a.order[k];
+        a.partial[i] = (double)hx + (double)lx;
+        a.partial[a.n + i] = (double)hy + (double)ly;
+        a.partial[2 * (size_t)a.n + i] = (double)hz + (double)lz;
+    }
+}
+
+__global__ void __launch_bounds__(kTravWarps * 32)
+traverse_warp_kernel(TravArgs a)
+{
+    __shared__ int32_t stack[kTravWarps][kStack];
+    __shared__ float4 buf[kTravWarps][kBuf];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int k0 = (blockIdx.x * kTravWarps + warp) * 32;
+    if (k0 >= a.n) return;
+    const int k = k0 + lane;
+    const bool valid = k < a.n;
+    const float4 q = valid ? a.sbody[k] : a.sbody[k0];
+    float ax = 0.f, ay = 0.f, az = 0.f, hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+    int nb = 0;
+    int sp = 1;
+    if (lane == 0) stack[warp][0] = 0;
+    __syncwarp();
+    auto flush = [&]() {
+        __syncwarp();
+        for (int j = 0; j < nb; ++j) pair_acc(q.x, q.y, q.z, buf[warp][j], a.e, ax, ay, az);
+        fold(hx, lx, ax);
+        fold(hy, ly, ay);
+        fold(hz, lz, az);
+        nb = 0;
+        __syncwarp();
+    };
+    while (sp > 0) {
+        const int node = stack[warp][--sp];
+        __syncwarp();
+        const float4 geo = a.nd.geo[node];
+        const int child = a.nd.child[node];
+        const bool acc = valid ? accept_cell(a, node, geo, q.x, q.y, q.z, k) : true;
+        if (__all_sync(0xffffffffu, acc)) {
+            if (nb + 1 > kBuf) flush();
+            if (lane == 0) buf[warp][nb] = a.nd.com[node];
+            nb += 1;
+        } else if (child < 0) {
+            const int b = a.nd.begin[node], c = a.nd.count[node];
+            for (int j0 = 0; j0 < c; j0 += 32) {
+                const int m = min(32, c - j0);
+                if (nb + m > kBuf) flush();
+                if (lane < m) buf[warp][nb + lane] = a.sbody[b + j0 + lane];
+                nb += m;
+            }
+        } else {
+            const int nc = a.nd.nchild[node];
+            if (sp + nc > kStack) {
+                if (lane == 0) atomicOr(&a.flags[kFlagStack], 1u);
+                break;
+            }
+            if (lane < nc) stack[warp][sp + lane] = child + lane;
+            sp += nc;
+        }
+        __syncwarp();
+        if (nb >= 64) flush();
+    }
+    flush();
+    if (valid) {
+        const uint32_t i = a.order[k];
+        a.partial[i] = (double)hx + (double)lx;
+        a.partial[a.n + i] = (double)hy + (double)ly;
+        a.partial[2 * (size_t)a.n + i] = (double)hz + (double)lz;
+    }
+}
+
+inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// workspace + host driver
+// ---------------------------------------------------------------------------
+struct BhWorkspace {
+    int device = 0;
+    size_t cap_n = 0;
+    int grid_build = 0;  // blocks of the per-level build kernels
+    int grid_mom = 0;
+    uint64_t *keys[2] = {nullptr, nullptr};
+    uint32_t *vals[2] = {nullptr, nullptr};
+    uint32_t *hist = nullptr;
+    float4 *sbody = nullptr;
+    double *spos = nullptr, *smass = nullptr, *pref = nullptr, *mom_bsum = nullptr;
+    NodeArrays nd = {};
+    LevelInfo *lv = nullptr;
+    int32_t *bsum = nullptr;
+    unsigned long long *extent_bits = nullptr;
+    uint32_t *flags = nullptr;
+    int launches = 0;
+    // which key/val buffer holds the sorted result
+    int sorted = 0;
+};
+
+static void ws_release(BhWorkspace *ws)
+{
+    void *p[] = {ws->keys[0],  ws->keys[1],   ws->vals[0],       ws->vals[1],     ws->hist,
+                 ws->sbody,    ws->spos,      ws->smass,         ws->pref,        ws->mom_bsum,
+                 ws->nd.begin, ws->nd.count,  ws->nd.child,      ws->nd.nchild,   ws->nd.level,
+                 ws->nd.c64,   ws->nd.geo,    ws->nd.com,        ws->lv,          ws->bsum,
+                 ws->extent_bits, ws->flags};
+    for (void *q : p)
+        if (q) cudaFree(q);
+}
+
+template <typename T>
+static int wsalloc(T *&p, size_t count)
+{
+    PG_CUDA(cudaMalloc((void **)&p, (count ? count : 1) * sizeof(T)));
     return PHYSIM_OK;
 }
-void bh_free(BhWorkspace *ws) { delete ws; }
-int bh_accelerations(BhWorkspace *, const DeviceBodies &, const BhParams &, double *, cudaStream_t)
+
+int bh_reserve(BhWorkspace *&ws, size_t n, int device)
 {
-    set_error("Barnes-Hut kernels are not built yet");
-    return PHYSIM_ERR_ARGUMENT;
+    if (ws && n <= ws->cap_n) return PHYSIM_OK;
+    if (ws) {
+        ws_release(ws);
+        delete ws;
+        ws = nullptr;
+    }
+    BhWorkspace *w = new (std::nothrow) BhWorkspace();
+    PG_CHECK(w, PHYSIM_ERR_MEMORY, "out of host memory");
+    w->device = device;
+    const size_t cap = n < 64 ? 64 : n;
+    w->cap_n = cap;
+    const int sms = device_sm_count(device);
+    w->grid_build = sms * 4;
+    w->grid_mom = sms * 2;
+    const int tiles = cdiv((long long)cap, kSortTile);
+    // Node capacity: about 4N nodes holds every non-degenerate distribution
+    // even with leaf size 1; deeper chains only truncate the tree (exact,
+    // slower) and raise a flag.
+    const size_t ncap = 4 * cap + 64 * kMaxLevels;
+    int rc = PHYSIM_OK;
+#define PG_WA(ptr, cnt)                                                                     \
+    if (rc == PHYSIM_OK) rc = wsalloc(ptr, cnt)
+    PG_WA(w->keys[0], cap);
+    PG_WA(w->keys[1], cap);
+    PG_WA(w->vals[0], cap);
+    PG_WA(w->vals[1], cap);
+    PG_WA(w->hist, (size_t)kRadixBuckets * tiles);
+    PG_WA(w->sbody, cap);
+    PG_WA(w->spos, 3 * cap);
+    PG_WA(w->smass, cap);
+    PG_WA(w->pref, 4 * (cap + 1));
+    PG_WA(w->mom_bsum, 4 * (size_t)w->grid_mom);
+    PG_WA(w->nd.begin, ncap);
+    PG_WA(w->nd.count, ncap);
+    PG_WA(w->nd.child, ncap);
+    PG_WA(w->nd.nchild, ncap);
+    PG_WA(w->nd.level, ncap);
+    PG_WA(w->nd.c64, 4 * ncap);
+    PG_WA(w->nd.geo, ncap);
+    PG_WA(w->nd.com, ncap);
+    PG_WA(w->lv, 1);
+    PG_WA(w->bsum, (size_t)w->grid_build);
+    PG_WA(w->extent_bits, 1);
+    PG_WA(w->flags, 4);
+#undef PG_WA
+    w->nd.cap = (int)ncap;
+    if (rc == PHYSIM_OK) rc = cudaMemset(w->flags, 0, 4 * sizeof(uint32_t)) == cudaSuccess
+                                  ? PHYSIM_OK
+                                  : PHYSIM_ERR_CUDA;
+    if (rc != PHYSIM_OK) {
+        ws_release(w);
+        delete w;
+        return rc;
+    }
+    ws = w;
+    return PHYSIM_OK;
 }
-int bh_launches(const BhWorkspace *) { return 0; }
+
+void bh_free(BhWorkspace *ws)
+{
+    if (!ws) return;
+    ws_release(ws);
+    delete ws;
+}
+
+int bh_launches(const BhWorkspace *ws) { return ws ? ws->launches : 0; }
+
+static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, cudaStream_t st)
+{
+    const int n = (int)b.n;
+    int launches = 0;
+    PG_CUDA(cudaMemsetAsync(ws->extent_bits, 0, sizeof(unsigned long long), st));
+    const int sms = device_sm_count(ws->device);
+    extent_kernel<<<sms * 2, 256, 0, st>>>(b.x, b.y, b.z, n, ws->extent_bits);
+    keys_kernel<<<cdiv(n, 256), 256, 0, st>>>(b.x, b.y, b.z, n, p.nchild, ws->extent_bits,
+                                              ws->keys[0], ws->vals[0]);
+    launches += 2;
+    // radix sort
+    const int tiles = cdiv(n, kSortTile);
+    const int key_bits = tree_levels(p.nchild) * level_bits(p.nchild);
+    int cur = 0;
+    for (int shift = 0; shift < key_bits; shift += kRadixBits) {
+        radix_hist_kernel<<<tiles, kSortThreads, 0, st>>>(ws->keys[cur], n, shift, ws->hist, tiles);
+        scan_u32_kernel<<<1, kScanThreads, 0, st>>>(ws->hist, kRadixBuckets * tiles);
+        radix_scatter_kernel<<<tiles, kSortThreads, 0, st>>>(
+            ws->keys[cur], shift == 0 ? nullptr : ws->vals[cur], ws->keys[cur ^ 1],
+            ws->vals[cur ^ 1], n, shift, ws->hist, tiles);
+        cur ^= 1;
+        launches += 3;
+    }
+    ws->sorted = cur;
+    gather_kernel<<<cdiv(n, 256), 256, 0, st>>>(ws->vals[cur], n, b.body4, b.x, b.y, b.z, b.m,
+                                                ws->sbody, ws->spos, ws->smass);
+    root_kernel<<<1, 32, 0, st>>>(ws->nd, ws->lv, n, ws->extent_bits);
+    launches += 2;
+    const int D = tree_levels(p.nchild);
+    for (int level = 0; level < D; ++level) {
+        level_count_kernel<<<ws->grid_build, kBuildThreads, 0, st>>>(
+            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->bsum);
+        level_scan_kernel<<<1, kScanThreads, 0, st>>>(ws->bsum, ws->grid_build, ws->lv, level,
+                                                      ws->nd.cap, ws->flags);
+        level_write_kernel<<<ws->grid_build, kBuildThreads, 0, st>>>(
+            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->bsum);
+        launches += 3;
+    }
+    moment_partial_kernel<<<ws->grid_mom, kMomThreads, 0, st>>>(ws->spos, ws->smass, n,
+                                                                ws->mom_bsum);
+    moment_blockscan_kernel<<<1, 32, 0, st>>>(ws->mom_bsum, ws->grid_mom);
+    moment_scan_kernel<<<ws->grid_mom, kMomThreads, 0, st>>>(ws->spos, ws->smass, n, ws->mom_bsum,
+                                                             ws->pref);
+    node_finish_kernel<<<sms * 4, 256, 0, st>>>(ws->nd, ws->lv, ws->pref, n, ws->sbody, ws->spos);
+    launches += 4;
+    PG_CUDA(cudaGetLastError());
+    ws->launches = launches;
+    return PHYSIM_OK;
+}
+
+int bh_accelerations(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, double *partial,
+                     cudaStream_t st)
+{
+    PG_CHECK(ws && b.x, PHYSIM_ERR_ARGUMENT, "Barnes-Hut needs the f64 body state");
+    PG_CHECK(p.nchild == 8 || p.nchild == 4, PHYSIM_ERR_ARGUMENT, "nchild must be 8 or 4");
+    PG_CHECK(b.n <= ws->cap_n, PHYSIM_ERR_ARGUMENT, "workspace too small");
+    const int n = (int)b.n;
+    if (n == 0) return PHYSIM_OK;
+    PG_TRY(bh_build(ws, b, p, st));
+    TravArgs a;
+    a.nd = ws->nd;
+    a.sbody = ws->sbody;
+    a.spos = ws->spos;
+    a.order = ws->vals[ws->sorted];
+    a.lv = ws->lv;
+    a.n = n;
+    a.theta = (float)p.theta;
+    a.theta64 = p.theta;
+    a.e = (float)p.e;
+    a.flags = ws->flags;
+    a.partial = partial;
+    const int blocks = cdiv(cdiv(n, 32), kTravWarps);
+    if (p.traversal == PHYSIM_TRAVERSAL_WARP)
+        traverse_warp_kernel<<<blocks, kTravWarps * 32, 0, st>>>(a);
+    else
+        traverse_exact_kernel<<<blocks, kTravWarps * 32, 0, st>>>(a);
+    PG_CUDA(cudaGetLastError());
+    ws->launches += 1;
+    return PHYSIM_OK;
+}
+
+// Copies the tree of the last build to host arrays (tests / diagnostics).
+int bh_snapshot(BhWorkspace *ws, size_t n, cudaStream_t st, PhysimTreeSnapshot *out)
+{
+    PG_CHECK(ws && out, PHYSIM_ERR_ARGUMENT, "null argument");
+    LevelInfo lv;
+    uint32_t flags[4];
+    unsigned long long xb = 0;
+    PG_CUDA(cudaMemcpyAsync(&lv, ws->lv, sizeof lv, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaMemcpyAsync(flags, ws->flags, sizeof flags, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaMemcpyAsync(&xb, ws->extent_bits, sizeof xb, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    double X;
+    memcpy(&X, &xb, sizeof X);
+    out->extent = X;
+    out->n_bodies = n;
+    out->n_nodes = (size_t)lv.total;
+    out->flags = flags[kFlagNodes] | (flags[kFlagStack] << 1);
+    const size_t nn = out->n_nodes < out->cap_nodes ? out->n_nodes : out->cap_nodes;
+    auto cp = [&](void *dst, const void *src, size_t bytes) -> int {
+        if (dst && bytes) PG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+        return PHYSIM_OK;
+    };
+    PG_TRY(cp(out->keys, ws->keys[ws->sorted], n * sizeof(uint64_t)));
+    PG_TRY(cp(out->order, ws->vals[ws->sorted], n * sizeof(uint32_t)));
+    PG_TRY(cp(out->node_begin, ws->nd.begin, nn * sizeof(int32_t)));
+    PG_TRY(cp(out->node_count, ws->nd.count, nn * sizeof(int32_t)));
+    PG_TRY(cp(out->node_child, ws->nd.child, nn * sizeof(int32_t)));
+    PG_TRY(cp(out->node_nchild, ws->nd.nchild, nn));
+    PG_TRY(cp(out->node_level, ws->nd.level, nn));
+    if (out->node_centre)
+        for (int c = 0; c < 4; ++c)
+            PG_TRY(cp(out->node_centre + c * nn, ws->nd.c64 + (size_t)c * ws->nd.cap,
+                      nn * sizeof(double)));
+    PG_TRY(cp(out->node_com, ws->nd.com, nn * sizeof(float4)));
+    PG_CUDA(cudaStreamSynchronize(st));
+    return PHYSIM_OK;
+}
+
 }  // namespace pg

@@ -57,5 +57,7 @@ int bh_accelerations(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, 
                      cudaStream_t stream);
 // Kernel launches one bh_accelerations call makes.
 int bh_launches(const BhWorkspace *ws);
+// Copies keys, sort order and tree of the last build to host arrays.
+int bh_snapshot(BhWorkspace *ws, size_t n, cudaStream_t stream, PhysimTreeSnapshot *out);
 
 }  // namespace pg

@@ -235,6 +235,18 @@ int physim_gpu_sim_accelerations(PhysimSim *s, Acceleration *acc, size_t n)
     return PHYSIM_OK;
 }
 
+int physim_gpu_sim_tree_snapshot(PhysimSim *s, PhysimTreeSnapshot *out)
+{
+    PG_CHECK(s && out, PHYSIM_ERR_ARGUMENT, "null argument");
+    PG_CHECK(s->cfg.gravity != PHYSIM_GRAVITY_SIMPLE_ASTRO, PHYSIM_ERR_ARGUMENT,
+             "simple_astro builds no tree");
+    PG_CHECK(s->uploaded, PHYSIM_ERR_ARGUMENT, "snapshot before upload");
+    PG_CUDA(cudaSetDevice(s->cfg.device));
+    int splits = 1;
+    if (s->n) PG_TRY(sim_forces(s, &splits));
+    return bh_snapshot(s->bh, s->n, s->stream, out);
+}
+
 int physim_gpu_sim_synchronize(PhysimSim *s)
 {
     PG_CHECK(s, PHYSIM_ERR_ARGUMENT, "null simulation");

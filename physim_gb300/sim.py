@@ -78,6 +78,30 @@ class Simulation:
               "physim_gpu_sim_accelerations")
         return out
 
+    def tree_snapshot(self) -> dict:
+        """Keys, sort order and tree of the current state (astro/astro2 only)."""
+        from ._lib import PhysimTreeSnapshot
+        cap = 4 * max(self.n, 64) + 64 * 31
+        keys = np.zeros(self.n, np.uint64)
+        order = np.zeros(self.n, np.uint32)
+        nb, nc, ch = (np.zeros(cap, np.int32) for _ in range(3))
+        nn, lvl = np.zeros(cap, np.uint8), np.zeros(cap, np.uint8)
+        cen = np.zeros(4 * cap, np.float64)
+        com = np.zeros(4 * cap, np.float32)
+        s = PhysimTreeSnapshot()
+        s.cap_nodes = cap
+        for name, arr in (("keys", keys), ("order", order), ("node_begin", nb),
+                          ("node_count", nc), ("node_child", ch), ("node_nchild", nn),
+                          ("node_level", lvl), ("node_centre", cen), ("node_com", com)):
+            setattr(s, name, arr.ctypes.data)
+        check(lib.physim_gpu_sim_tree_snapshot(self.handle, C.byref(s)),
+              "physim_gpu_sim_tree_snapshot")
+        m = min(s.n_nodes, cap)
+        return {"keys": keys, "order": order, "begin": nb[:m], "count": nc[:m], "child": ch[:m],
+                "nchild": nn[:m], "level": lvl[:m], "centre": cen[:4 * m].reshape(4, m),
+                "com": com[:4 * m].reshape(m, 4), "n_nodes": int(s.n_nodes),
+                "extent": s.extent, "flags": int(s.flags)}
+
     def set_profiling(self, enable: bool = True) -> None:
         check(lib.physim_gpu_sim_set_profiling(self.handle, 1 if enable else 0),
               "physim_gpu_sim_set_profiling")

@@ -1,0 +1,218 @@
+"""Barnes-Hut on the GPU (astro2 octree, astro quadtree).
+
+  * keys, sort order and tree topology: bit-exact against the CPU model of the
+    same build (oracle/bh_model.c) on the same f64 inputs;
+  * leaf size 1 with exact traversal uses the reference's interaction lists,
+    so accelerations match the oracle's astro2/astro (transformers.rs:31-69,
+    122-160) to the FP32 tolerance, 1e-5 relative per body;
+  * leaf size 16 and warp traversal open at least the cells the reference
+    opens, so their error against the f64 direct sum is at most the
+    reference's own error (RMS over a sample, 5% slack).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5
+
+
+def _vec(acc):
+    return np.stack([acc["x"], acc["y"], acc["z"]], axis=1)
+
+
+def rel_err(got, want):
+    g, w = _vec(got), _vec(want)
+    return np.linalg.norm(g - w, axis=1) / np.maximum(np.linalg.norm(w, axis=1), 1e-300)
+
+
+def rms(x):
+    return float(np.sqrt(np.mean(np.asarray(x) ** 2)))
+
+
+def _states():
+    from physim_gb300 import ics
+    a = ics.cube_with_stars(20000, seed=31, stars=ics.STARS_4)
+    b = ics.plummer(20000, seed=7, a=0.1)
+    c = ics.cube_with_stars(3000, seed=32)
+    # boundary points and a coincident group
+    c[0]["x"], c[0]["y"], c[0]["z"] = 0.0, 0.0, 0.0
+    c[1]["x"] = c[2]["x"] = 0.25
+    for k in range(3, 9):
+        c[k]["x"], c[k]["y"], c[k]["z"] = 0.125, -0.125, 0.0625
+    c[9]["x"] = -np.abs(c["x"]).max()
+    return {"cube": a, "plummer": b, "edges": c}
+
+
+STATES = None
+
+
+def states():
+    global STATES
+    if STATES is None:
+        STATES = _states()
+    return STATES
+
+
+def _sim(state, gravity, leaf, theta=0.5, e=0.01, traversal="exact"):
+    import physim_gb300 as pg
+    return pg.Simulation(state, pg.SimConfig(gravity=gravity, theta=theta, e=e, leaf_size=leaf,
+                                             traversal=traversal))
+
+
+@pytest.mark.parametrize("name", ["cube", "plummer", "edges"])
+@pytest.mark.parametrize("gravity,nchild", [("astro2", 8), ("astro", 4)])
+@pytest.mark.parametrize("leaf", [1, 16])
+def test_tree_bit_exact_vs_model(oracle_mod, name, gravity, nchild, leaf):
+    s = states()[name]
+    with _sim(s, gravity, leaf) as sim:
+        g = sim.tree_snapshot()
+    m = oracle_mod.bh_model(s, nchild, leaf)
+    assert g["flags"] == 0
+    assert g["extent"] == m["extent"]
+    assert np.array_equal(g["keys"], m["keys"])
+    assert np.array_equal(g["order"], m["order"])
+    assert g["n_nodes"] == len(m["begin"])
+    for f in ("begin", "count", "child", "nchild", "level"):
+        assert np.array_equal(g[f], m[f]), f
+    assert g["centre"].tobytes() == m["centre"].tobytes()
+    # node masses: f64 prefix sums on the GPU, f32 stored
+    mass = s["mass"][g["order"]]
+    want = np.array([mass[b:b + c].sum() for b, c in zip(g["begin"][:500], g["count"][:500])])
+    np.testing.assert_allclose(g["com"][:500, 3], want, rtol=1e-6)
+
+
+@pytest.mark.parametrize("theta", [0.3, 0.5, 1.0, 1.5])
+@pytest.mark.parametrize("name,nchild", [("astro2", 8), ("astro", 4)])
+def test_reference_lists_match_oracle(oracle_mod, theta, name, nchild):
+    """Leaf 1 + exact traversal through the plugin vs the reference restatement."""
+    import physim_gb300 as pg
+    from physim_gb300 import ics
+    s = ics.cube_with_stars(3000, seed=41, stars=ics.STARS_2)
+    s["fixed"][17] = 1
+    acc = pg.accelerations(len(s))
+    acc["y"] = 0.5
+    with pg.TransformElementHandler(name, {"theta": theta, "e": 0.01}) as el:
+        el.transform(s, acc)
+    want = oracle_mod.barnes_hut(s, theta, 0.01, nchild=nchild)
+    want["y"] += 0.5
+    fixed = s["fixed"].astype(bool)
+    assert np.all(acc["y"][fixed] == 0.5)
+    err = rel_err(acc[~fixed], want[~fixed])
+    assert err.max() < RTOL, (err.max(), int(np.argmax(err)))
+
+
+def test_edge_states_match_oracle(oracle_mod):
+    import physim_gb300 as pg
+    s = states()["edges"]
+    acc = pg.accelerations(len(s))
+    with pg.TransformElementHandler("astro2", {"theta": 0.7, "e": 0.02}) as el:
+        el.transform(s, acc)
+    want = oracle_mod.barnes_hut(s, 0.7, 0.02, nchild=8)
+    assert rel_err(acc, want).max() < RTOL
+
+
+@pytest.mark.parametrize("n", [1, 2, 3])
+def test_tiny_states(oracle_mod, n):
+    import physim_gb300 as pg
+    from physim_gb300 import ics
+    s = ics.cube_with_stars(n, seed=50 + n)
+    for name, nchild in (("astro2", 8), ("astro", 4)):
+        acc = pg.accelerations(n)
+        with pg.TransformElementHandler(name, {"theta": 0.5, "e": 0.01}) as el:
+            el.transform(s, acc)
+        want = oracle_mod.barnes_hut(s, 0.5, 0.01, nchild=nchild)
+        assert np.allclose(_vec(acc), _vec(want), rtol=RTOL, atol=1e-12)
+
+
+def test_all_bodies_at_origin(oracle_mod):
+    """X = 0: one cell, every pair coincident, zero force (octree.rs:253-268)."""
+    import physim_gb300 as pg
+    s = pg.entities(10)
+    s["mass"] = 1.0
+    acc = pg.accelerations(10)
+    with pg.TransformElementHandler("astro2", {"theta": 0.5}) as el:
+        el.transform(s, acc)
+    assert np.all(_vec(acc) == 0.0)
+
+
+def test_negative_theta_is_direct_sum(oracle_mod):
+    import physim_gb300 as pg
+    from physim_gb300 import ics
+    s = ics.cube_with_stars(2000, seed=52, stars=ics.STARS_2)
+    want = oracle_mod.simple_astro(s, 0.01)
+    for leaf, trav in ((1, "exact"), (16, "exact"), (16, "warp")):
+        acc = pg.accelerations(len(s))
+        with pg.TransformElementHandler("astro2", {"theta": -0.1, "e": 0.01, "leaf_size": leaf,
+                                                   "traversal": trav}) as el:
+            el.transform(s, acc)
+        assert rel_err(acc, want).max() < RTOL, (leaf, trav)
+
+
+def test_massless_body_is_nan(oracle_mod):
+    import physim_gb300 as pg
+    from physim_gb300 import ics
+    s = ics.cube_with_stars(500, seed=53)
+    s["mass"][11] = 0.0
+    acc = pg.accelerations(len(s))
+    with pg.TransformElementHandler("astro2", {"theta": 0.5, "e": 0.01}) as el:
+        el.transform(s, acc)
+    assert np.isnan(acc["x"][11])
+    ok = np.ones(len(s), bool)
+    ok[11] = False
+    want = oracle_mod.barnes_hut(s, 0.5, 0.01)
+    assert rel_err(acc[ok], want[ok]).max() < RTOL
+
+
+@pytest.mark.parametrize("leaf,traversal", [(16, "exact"), (16, "warp"), (1, "warp"),
+                                            (8, "warp")])
+@pytest.mark.parametrize("theta", [0.5, 1.0])
+def test_accuracy_not_worse_than_reference(oracle_mod, leaf, traversal, theta):
+    import physim_gb300 as pg
+    from physim_gb300 import ics
+    s = ics.cube_with_stars(30000, seed=61, stars=ics.STARS_4)
+    idx = np.random.default_rng(2).choice(len(s), 400, replace=False)
+    exact = oracle_mod.simple_astro_sample(s, 0.01, idx)
+    ref = oracle_mod.barnes_hut(s, theta, 0.01, nchild=8, idx=idx)
+    with _sim(s, "astro2", leaf, theta=theta, traversal=traversal) as sim:
+        got = sim.accelerations()[idx]
+    e_ref, e_gpu = rms(rel_err(ref, exact)), rms(rel_err(got, exact))
+    assert e_gpu <= 1.05 * e_ref + 1e-6, (e_gpu, e_ref)
+
+
+def test_bh_pipeline_matches_oracle(oracle_mod):
+    """Device-resident astro2 + verlet, 5 steps, reference tree and lists."""
+    import physim_gb300 as pg
+    from physim_gb300 import ics
+    from test_verlet_gpu import trajectory_errors
+    s = ics.cube_with_stars(4000, seed=71, stars=ics.STARS_2)
+    with _sim(s, "astro2", 1, theta=0.5) as sim:
+        sim.step(5)
+        got = sim.download()
+    want = oracle_mod.run_pipeline(s, "astro2", 5, 1e-6, 0.01, theta=0.5)
+    err = trajectory_errors(s, got, want)
+    assert err["pos_rel_l2"] < 1e-5 and err["vel_rel_l2"] < 1e-5, err
+
+
+def test_full_size_workload(oracle_mod):
+    """1,048,580 bodies, theta 0.5, leaf 16, warp traversal: keys/order/tree
+    bit-exact against the model, RMS relative error vs f64 direct <= 1e-3 on a
+    1,024-body sample, and not worse than the reference algorithm's."""
+    from physim_gb300 import ics
+    s = ics.workload_large()
+    with _sim(s, "astro2", 16, theta=0.5, traversal="warp") as sim:
+        g = sim.tree_snapshot()
+        a = sim.accelerations()
+    m = oracle_mod.bh_model(s, 8, 16)
+    assert np.array_equal(g["keys"], m["keys"]) and np.array_equal(g["order"], m["order"])
+    for f in ("begin", "count", "child", "nchild", "level"):
+        assert np.array_equal(g[f], m[f]), f
+    idx = np.random.default_rng(5).choice(len(s), 1024, replace=False)
+    exact = oracle_mod.simple_astro_sample(s, 0.01, idx)
+    e_gpu = rms(rel_err(a[idx], exact))
+    assert e_gpu <= 1e-3, e_gpu
+    ref = oracle_mod.barnes_hut(s, 0.5, 0.01, nchild=8, idx=idx[:256])
+    e_ref = rms(rel_err(ref, exact[:256]))
+    assert rms(rel_err(a[idx[:256]], exact[:256])) <= 1.05 * e_ref + 1e-6
