@@ -57,6 +57,9 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--skip-e2e", action="store_true", help="profiling runs: device path only")
+    p.add_argument("--only", default="", help="comma list of parts: direct, bh")
+    p.add_argument("--bh-steps", type=int, default=1000)
+    p.add_argument("--bh-e2e-steps", type=int, default=5)
     p.add_argument("--bodies", type=int, default=N_CUBE,
                    help="cube bodies (profiling of smaller cases; the reported workload is "
                         "the default 1,048,576)")
@@ -238,82 +241,96 @@ def run_reference(args, dist: Dist):
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
-def run_ours(args, dist: Dist):
+def _device_context(dist: Dist):
+    import torch
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    device = dist.local
+    torch.cuda.set_device(device)
+    props = torch.cuda.get_device_properties(device)
+    return device, props.multi_processor_count
+
+
+def _timed_steps(sim, stream, steps: int, flush) -> tuple[list[float], list[float]]:
+    """Per-step CUDA-event times on the simulation's stream, L2 flushed between
+    steps outside the events.  Returns (step ms, gravity-kernel ms)."""
+    import torch
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    grav = []
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            starts[k].record(stream)
+            sim.step(1)
+            ends[k].record(stream)
+        grav.append(sim.last_step_ms()[0])
+    torch.cuda.synchronize()
+    return [s.elapsed_time(e) for s, e in zip(starts, ends)], grav
+
+
+def measure_direct(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict:
     import torch
 
     import physim_gb300 as pg
     from physim_gb300 import ics
 
-    if not torch.cuda.is_available():
-        raise SystemExit("bench.py needs a CUDA GPU")
-    device = dist.local
-    torch.cuda.set_device(device)
     state = ics.workload_large(args.bodies)
     n = len(state)
-    pairs_step = n * (n - 1) - 0  # no fixed bodies in this workload
-    props = torch.cuda.get_device_properties(device)
-    sms = props.multi_processor_count
-    peaks = measured_peaks()
+    pairs_step = n * (n - 1)  # no fixed bodies in this workload
     stream = torch.cuda.Stream(device=device)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
-
     sim = pg.Simulation(state, pg.SimConfig(gravity="simple_astro", e=E, dt=DT, device=device,
                                             stream=stream.cuda_stream))
     sim.set_profiling(True)
     with torch.cuda.stream(stream):
         sim.step(args.warmup)
     sim.synchronize()
-
     clocks = Clocks(device)
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    grav_ms = []
     dist.barrier()
     torch.cuda.synchronize()
     clocks.start()
     t_wall = time.perf_counter()
-    for k in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.zero_()  # L2 flush between timed steps (outside the events)
-            starts[k].record(stream)
-            sim.step(1)
-            ends[k].record(stream)
-        g, _ = sim.last_step_ms()
-        grav_ms.append(g)
-    torch.cuda.synchronize()
+    step_ms, grav_ms = _timed_steps(sim, stream, args.steps, flush)
     wall = time.perf_counter() - t_wall
     dist.barrier()
     clk = clocks.stop()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = dist.max(sum(step_ms))
     all_pairs = dist.sum(float(pairs_step * args.steps))
-    value = all_pairs / (total_ms / 1e3) / 1e9
-    ms_per_step = total_ms / args.steps
     launches = sim.launches_per_step * args.steps
     sim.close()
 
-    # kernel roofline (pair kernel only)
     kern_ms = statistics.mean(grav_ms)
-    achieved_tflops = FLOP_PER_PAIR * pairs_step / (kern_ms / 1e3) / 1e12
+    achieved = FLOP_PER_PAIR * pairs_step / (kern_ms / 1e3) / 1e12
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
-    peak_tflops = sms * FP32_LANES_PER_SM * 2 * sm_max * 1e6 / 1e12
+    peak = sms * FP32_LANES_PER_SM * 2 * sm_max * 1e6 / 1e12
     traffic = None
     tfile = ROOT / "profiles" / "direct_forces_traffic.json"
-    if tfile.exists():
+    if tfile.exists() and args.bodies == N_CUBE:
         try:
             traffic = json.loads(tfile.read_text()).get("bytes_per_launch")
         except ValueError:
             traffic = None
+    out = {"value": all_pairs / (total_ms / 1e3) / 1e9, "ms_per_step": total_ms / args.steps,
+           "bodies": n, "pairs_per_step": pairs_step, "wall_s": wall, "gpu_launches": launches,
+           "roofline": {"bound": "fp32", "kernel": "direct_forces_kernel", "achieved": achieved,
+                        "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                        "traffic": traffic,
+                        "peak_basis": f"{sms} SMs x {FP32_LANES_PER_SM} FP32 lanes x 2 x "
+                                      f"{sm_max:.0f} MHz (max SM clock, measured-peaks file)",
+                        "flop_per_pair": FLOP_PER_PAIR, "kernel_ms": kern_ms}}
+    if clk:
+        out["clocks"] = clk
+        if clk.get("sm_mhz"):
+            out["roofline"]["frac_at_observed_clock"] = achieved / (
+                sms * FP32_LANES_PER_SM * 2 * clk["sm_mhz"] * 1e6 / 1e12)
 
-    # e2e through the plugin C ABI with host arrays
-    e2e = None
     if not args.skip_e2e:
         e2e_steps = args.e2e_steps or max(2, min(args.steps, 3))
         el = pg.TransformElementHandler("simple_astro", {"e": E, "device": device})
         verlet = pg.GpuVerlet(device)
         cur = state.copy()
-        acc = pg.accelerations(n)
-        el.transform(cur, acc)  # warm: allocations and module load
+        el.transform(cur, pg.accelerations(n))  # warm: allocations, module load
         times = []
         for _ in range(e2e_steps):
             t0 = time.perf_counter()
@@ -324,43 +341,159 @@ def run_ours(args, dist: Dist):
         el.destroy()
         verlet.close()
         t_e2e = dist.max(sum(times))
-        e2e = {"value": dist.sum(float(pairs_step * e2e_steps)) / t_e2e / 1e9,
-               "unit": "Gpair-interactions/s",
-               "h2d_bytes_per_step": n * (80 + 24) + n * (80 + 24),
-               "d2h_bytes_per_step": n * 24 + n * 80,
-               "steps": e2e_steps,
-               "path": "simple_astro_transform + physim_gpu_verlet_integrate on host Entity arrays"}
-
-    cpu = None
+        out["e2e"] = {"value": dist.sum(float(pairs_step * e2e_steps)) / t_e2e / 1e9,
+                      "unit": "Gpair-interactions/s",
+                      "h2d_bytes_per_step": n * (80 + 24) + n * (80 + 24),
+                      "d2h_bytes_per_step": n * 24 + n * 80, "steps": e2e_steps,
+                      "path": "simple_astro_transform + physim_gpu_verlet_integrate on host "
+                              "Entity arrays (pipeline.rs:137-173)"}
     if dist.rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_sample_rate(state, 1, args.cpu_seconds)
         cpu.pop("seconds", None)
         cpu["kind"] = "port"
+        out["cpu_baseline"] = cpu
+    return out
 
-    if dist.rank == 0:
-        line = {
-            "metric": METRIC, "value": value, "unit": "Gpair-interactions/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "fp32 pairs, f64 integration", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "bodies": n, "pairs_per_step": pairs_step,
-                       "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU",
-                       "l2": "flushed between timed steps (256 MiB write, outside the events)",
-                       "compensated_sums": True, "wall_s": wall},
-            "roofline": {"bound": "fp32", "kernel": "direct_forces_kernel",
-                         "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",
-                         "frac": achieved_tflops / peak_tflops, "traffic": traffic,
-                         "peak_basis": f"{sms} SMs x {FP32_LANES_PER_SM} FP32 lanes x 2 x "
-                                       f"{sm_max:.0f} MHz (max SM clock of measured peaks)",
-                         "flop_per_pair": FLOP_PER_PAIR, "kernel_ms": kern_ms},
-            "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu,
-        }
-        if clk:
-            line["clocks"] = clk
-            if clk.get("sm_mhz"):
-                line["roofline"]["frac_at_observed_clock"] = achieved_tflops / (
-                    sms * FP32_LANES_PER_SM * 2 * clk["sm_mhz"] * 1e6 / 1e12)
-        print(json.dumps(line), flush=True)
+
+# Algorithmic HBM bytes per body per Barnes-Hut step (f64 state, f32 bodies,
+# 63-bit keys, 32-bit body indices, 8 radix passes), by kernel:
+BH_BYTES_PER_BODY = {
+    "extent": 24,                 # read x, y, z (f64)
+    "keys": 24 + 12,              # read x, y, z; write key + index
+    "sort": 8 * (8 + 12 + 12),    # per pass: histogram read, scatter read + write
+    "gather": 4 + 16 + 32 + 16 + 24 + 8,  # order, f32 body, f64 x,y,z,m -> sorted copies
+    "moments": 32 + 32 + 32,      # partial sums read, scan read + prefix write
+    "traversal": 16 + 4 + 24,     # own body, order, acceleration partial
+    "verlet": 24 + 8 + 1 + 72 + 16 + 72 + 16,  # partial, m, fixed, state in, body4, state out
+}
+
+
+def cpu_bh_step_time(state, theta: float, target_s: float) -> dict:
+    """The reference astro2 restated (single thread): full tree build plus the
+    traversal/force of a sample of bodies, scaled to all bodies."""
+    import oracle
+    n = len(state)
+    rng = np.random.default_rng(11)
+    k = 64
+    t0 = time.perf_counter()
+    oracle.barnes_hut(state, theta, E, nchild=8, idx=np.array([0]), threads=1)
+    t_build = time.perf_counter() - t0  # build + one body
+    while True:
+        idx = rng.choice(n, k, replace=False)
+        t0 = time.perf_counter()
+        oracle.barnes_hut(state, theta, E, nchild=8, idx=idx, threads=1)
+        t = time.perf_counter() - t0
+        if t - t_build > target_s / 2 or k >= n:
+            break
+        k = min(n, k * 4)
+    per_body = max(t - t_build, 1e-9) / k
+    step_s = t_build + per_body * n
+    return {"value": 1.0 / step_s, "unit": "steps/s", "cores": 1, "kind": "port",
+            "sample": f"astro2 restatement (transformers.rs:122-160), theta {theta}: tree build "
+                      f"of all {n} bodies ({t_build:.2f} s) + traversal/force of {k} bodies, "
+                      f"scaled to {n} bodies"}
+
+
+def measure_bh(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict:
+    import torch
+
+    import physim_gb300 as pg
+    from physim_gb300 import ics
+
+    state = ics.workload_large(args.bodies)
+    n = len(state)
+    stream = torch.cuda.Stream(device=device)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    results = {}
+    for theta, steps in ((0.5, args.bh_steps), (1.0, max(args.bh_steps // 4, 10)),
+                         (1.5, max(args.bh_steps // 4, 10))):
+        sim = pg.Simulation(state, pg.SimConfig(gravity="astro2", theta=theta, e=E, dt=DT,
+                                                leaf_size=16, traversal="warp", device=device,
+                                                stream=stream.cuda_stream))
+        sim.set_profiling(True)
+        with torch.cuda.stream(stream):
+            sim.step(max(args.warmup, 3))
+        sim.synchronize()
+        dist.barrier()
+        step_ms, grav_ms = _timed_steps(sim, stream, steps, flush)
+        total = dist.max(sum(step_ms))
+        results[theta] = {"steps_per_s": dist.sum(float(steps)) / (total / 1e3),
+                          "ms_per_step": total / steps, "steps": steps,
+                          "gravity_ms": statistics.mean(grav_ms),
+                          "gpu_launches": sim.launches_per_step * steps}
+        sim.close()
+    main = results[0.5]
+    bytes_step = sum(BH_BYTES_PER_BODY.values()) * n
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = bytes_step / (main["ms_per_step"] / 1e3) / 1e9
+    out = {"metric": "BH steps/s at N=1M (astro2, theta 0.5, leaf 16, warp traversal)",
+           "value": main["steps_per_s"], "unit": "steps/s", "ms_per_step": main["ms_per_step"],
+           "bodies": n, "theta": {str(k): v for k, v in results.items()},
+           "roofline": {"bound": "hbm", "kernel": "whole step", "achieved": achieved,
+                        "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                        "algorithmic_bytes_per_body": BH_BYTES_PER_BODY,
+                        "note": "interaction-list node reads (L2-resident tree) excluded"}}
+    if not args.skip_e2e:
+        el = pg.TransformElementHandler("astro2", {"theta": 0.5, "e": E, "leaf_size": 16,
+                                                   "traversal": "warp", "device": device})
+        verlet = pg.GpuVerlet(device)
+        cur = state.copy()
+        el.transform(cur, pg.accelerations(n))
+        times = []
+        for _ in range(args.bh_e2e_steps):
+            t0 = time.perf_counter()
+            acc = np.zeros(n, dtype=pg.ACCELERATION)
+            el.transform(cur, acc)
+            cur = verlet.integrate(cur, acc, DT)
+            times.append(time.perf_counter() - t0)
+        el.destroy()
+        verlet.close()
+        t_e2e = dist.max(sum(times))
+        out["e2e"] = {"value": dist.sum(float(args.bh_e2e_steps)) / t_e2e, "unit": "steps/s",
+                      "h2d_bytes_per_step": n * (80 + 24) * 2, "d2h_bytes_per_step": n * 104,
+                      "steps": args.bh_e2e_steps,
+                      "path": "astro2_transform (leaf_size 16, warp) + physim_gpu_verlet_integrate "
+                              "on host Entity arrays"}
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_bh_step_time(state, 0.5, args.cpu_seconds)
+    return out
+
+
+def run_ours(args, dist: Dist):
+    device, sms = _device_context(dist)
+    peaks = measured_peaks()
+    parts = args.only.split(",") if args.only else ["direct", "bh"]
+    direct = measure_direct(args, dist, device, sms, peaks) if "direct" in parts else None
+    bh = measure_bh(args, dist, device, sms, peaks) if "bh" in parts else None
+    if dist.rank != 0:
+        return
+    base = direct if direct else bh
+    line = {
+        "metric": METRIC if direct else bh["metric"],
+        "value": base["value"],
+        "unit": "Gpair-interactions/s" if direct else "steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": base["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 pairs, f64 integration", "data": "synthetic",
+        "config": {"workload": WORKLOAD if direct else "astro2 " + WORKLOAD,
+                   "bodies": base["bodies"],
+                   "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU",
+                   "l2": "flushed between timed steps (256 MiB write, outside the events)",
+                   "compensated_sums": True},
+    }
+    if direct:
+        line["config"]["pairs_per_step"] = direct["pairs_per_step"]
+        for k in ("roofline", "e2e", "gpu_launches", "cpu_baseline", "clocks"):
+            if k in direct:
+                line[k] = direct[k]
+    if bh:
+        line["bh"] = bh
+        if not direct:
+            for k in ("roofline", "e2e", "cpu_baseline"):
+                if k in bh:
+                    line[k] = bh[k]
+            line["gpu_launches"] = bh["theta"]["0.5"]["gpu_launches"]
+    print(json.dumps(line), flush=True)
 
 
 def main():

@@ -73,6 +73,7 @@ def load() -> C.CDLL:
         "oracle_verlet_step": (i32, [vp, vp, vp, sz, vp, dbl]),
         "oracle_run_pipeline": (i32, [vp, sz, i32, dbl, dbl, dbl, i32, i32]),
         "oracle_max_threads": (i32, []),
+        "oracle_tree_dump": (sz, [vp, vp, vp, sz]),
         "bh_model_extent": (dbl, [vp, sz]),
         "bh_model_keys": (None, [vp, sz, i32, vp]),
         "bh_model_build": (C.c_long, [vp, sz, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, sz]),

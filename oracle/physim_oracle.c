@@ -161,6 +161,23 @@ void oracle_tree_free(Tree *t)
 
 size_t oracle_tree_node_count(const Tree *t) { return t->len; }
 
+/* Node geometry of the arena (centre x,y,z and half-width per node, and the
+ * number of children), for comparing tree topologies.  Returns the count. */
+size_t oracle_tree_dump(const Tree *t, double *geom4, int32_t *nchildren, size_t cap)
+{
+    for (size_t i = 0; i < t->len && i < cap; ++i) {
+        const Node *n = &t->nodes[i];
+        geom4[4 * i + 0] = n->centre[0];
+        geom4[4 * i + 1] = n->centre[1];
+        geom4[4 * i + 2] = n->centre[2];
+        geom4[4 * i + 3] = n->extent;
+        int k = 0;
+        for (int c = 0; c < t->nchild; ++c) k += n->child[c] >= 0;
+        nchildren[i] = k;
+    }
+    return t->len;
+}
+
 static int node_is_leaf(const Tree *t, const Node *n)
 {
     for (int i = 0; i < t->nchild; ++i)

@@ -32,6 +32,12 @@ struct PhysimSim {
     // integrator of the most recent step.
     bool profiling = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    // The gravity phase of a step, captured once and replayed: the
+    // Barnes-Hut build is ~100 short kernels whose launch cost would
+    // otherwise dominate at small N.
+    bool use_graph = true;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
 };
 
 struct PhysimVerlet {
@@ -66,6 +72,41 @@ int sim_forces(PhysimSim *s, int *splits_out)
     *splits_out = 1;
     (void)n;
     return bh_accelerations(s->bh, s->b, p, s->partial, s->stream);
+}
+
+// Captures the gravity phase into a graph.  If the stream cannot be captured
+// (e.g. the caller is itself capturing), the simulation stays eager.
+int sim_capture(PhysimSim *s)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    PG_CUDA(cudaStreamIsCapturing(s->stream, &cs));
+    if (cs != cudaStreamCaptureStatusNone) {
+        s->use_graph = false;
+        return PHYSIM_OK;
+    }
+    PG_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    int splits = 1;
+    int rc = sim_forces(s, &splits);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+    if (rc != PHYSIM_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (ce != cudaSuccess || !g) {
+        (void)cudaGetLastError();
+        s->use_graph = false;
+        return PHYSIM_OK;
+    }
+    if (cudaGraphInstantiate(&s->graph_exec, g, 0) != cudaSuccess) {
+        (void)cudaGetLastError();
+        cudaGraphDestroy(g);
+        s->graph_exec = nullptr;
+        s->use_graph = false;
+        return PHYSIM_OK;
+    }
+    s->graph = g;
+    return PHYSIM_OK;
 }
 
 }  // namespace
@@ -164,7 +205,13 @@ int physim_gpu_sim_step(PhysimSim *s, uint32_t steps)
         if (s->n == 0) break;
         int splits = 1;
         if (s->profiling) PG_CUDA(cudaEventRecord(s->ev[0], s->stream));
-        PG_TRY(sim_forces(s, &splits));
+        if (s->use_graph && !s->graph_exec) PG_TRY(sim_capture(s));
+        if (s->graph_exec) {
+            PG_CUDA(cudaGraphLaunch(s->graph_exec, s->stream));
+            splits = s->cfg.gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO ? s->plan.splits : 1;
+        } else {
+            PG_TRY(sim_forces(s, &splits));
+        }
         if (s->profiling) PG_CUDA(cudaEventRecord(s->ev[1], s->stream));
         PG_TRY(launch_verlet(s->b, s->partial, splits, s->cfg.dt, !s->history, s->stream));
         if (s->profiling) PG_CUDA(cudaEventRecord(s->ev[2], s->stream));
@@ -273,6 +320,8 @@ void physim_gpu_sim_destroy(PhysimSim *s)
     if (s->partial) cudaFree(s->partial);
     if (s->acc_soa) cudaFree(s->acc_soa);
     bh_free(s->bh);
+    if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+    if (s->graph) cudaGraphDestroy(s->graph);
     for (cudaEvent_t e : s->ev)
         if (e) cudaEventDestroy(e);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
