@@ -417,22 +417,36 @@ def measure_bh(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict:
         dist.barrier()
         step_ms, grav_ms = _timed_steps(sim, stream, steps, flush)
         total = dist.max(sum(step_ms))
+        st = sim.bh_stats()
         results[theta] = {"steps_per_s": dist.sum(float(steps)) / (total / 1e3),
                           "ms_per_step": total / steps, "steps": steps,
                           "gravity_ms": statistics.mean(grav_ms),
+                          "traversal_ms_last_step": st["traversal_ms"],
+                          "interactions_per_step": st["interactions"],
+                          "node_visits_per_step": st["node_visits"],
                           "gpu_launches": sim.launches_per_step * steps}
         sim.close()
     main = results[0.5]
     bytes_step = sum(BH_BYTES_PER_BODY.values()) * n
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     achieved = bytes_step / (main["ms_per_step"] / 1e3) / 1e9
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = sms * FP32_LANES_PER_SM * 2 * sm_max * 1e6 / 1e12
+    trav_ms = main["traversal_ms_last_step"]
+    trav_tflops = (FLOP_PER_PAIR * main["interactions_per_step"] / (trav_ms / 1e3) / 1e12
+                   if trav_ms and trav_ms > 0 else None)
     out = {"metric": "BH steps/s at N=1M (astro2, theta 0.5, leaf 16, warp traversal)",
            "value": main["steps_per_s"], "unit": "steps/s", "ms_per_step": main["ms_per_step"],
            "bodies": n, "theta": {str(k): v for k, v in results.items()},
            "roofline": {"bound": "hbm", "kernel": "whole step", "achieved": achieved,
                         "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
                         "algorithmic_bytes_per_body": BH_BYTES_PER_BODY,
-                        "note": "interaction-list node reads (L2-resident tree) excluded"}}
+                        "note": "interaction-list node reads (L2-resident tree) excluded"},
+           "traversal_roofline": {"bound": "fp32", "kernel": "traverse_warp_kernel",
+                                  "achieved": trav_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+                                  "frac": trav_tflops / fp32_peak if trav_tflops else None,
+                                  "flop_per_interaction": FLOP_PER_PAIR,
+                                  "kernel_ms": trav_ms}}
     if not args.skip_e2e:
         el = pg.TransformElementHandler("astro2", {"theta": 0.5, "e": E, "leaf_size": 16,
                                                    "traversal": "warp", "device": device})

@@ -278,6 +278,11 @@ typedef struct PhysimTreeSnapshot {
 /* Builds the tree of the current state of an astro/astro2 simulation and
  * copies it out. */
 int physim_gpu_sim_tree_snapshot(PhysimSim *sim, PhysimTreeSnapshot *out);
+/* Waits for the stream, then reports the most recent Barnes-Hut traversal:
+ * node visits (one per warp and node), pair interactions (per body) and,
+ * with profiling on, the traversal kernel's device time (else -1). */
+int physim_gpu_sim_bh_stats(PhysimSim *sim, uint64_t *node_visits, uint64_t *interactions,
+                            double *traversal_ms);
 
 /* Verlet integrator over host arrays (integrators/src/verlet.rs:19-121).
  * A Rust IntegratorElement shim evaluates acc_fn itself and hands the

@@ -98,6 +98,8 @@ def _load() -> C.CDLL:
         "physim_gpu_sim_last_step_ms": (C.c_int, [vp, C.POINTER(dbl), C.POINTER(dbl)]),
         "physim_gpu_sim_destroy": (None, [vp]),
         "physim_gpu_sim_tree_snapshot": (C.c_int, [vp, C.POINTER(PhysimTreeSnapshot)]),
+        "physim_gpu_sim_bh_stats": (C.c_int, [vp, C.POINTER(C.c_uint64),
+                                              C.POINTER(C.c_uint64), C.POINTER(dbl)]),
         "physim_gpu_verlet_create": (C.c_int, [i32, C.POINTER(vp)]),
         "physim_gpu_verlet_integrate": (C.c_int, [vp, vp, vp, sz, vp, dbl]),
         "physim_gpu_verlet_destroy": (None, [vp]),

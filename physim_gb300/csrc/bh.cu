@@ -47,7 +47,6 @@ constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 keys per block
 constexpr int kSortWarps = kSortThreads / 32;
 
 constexpr int kBuildThreads = 256;
-constexpr int kScanThreads = 1024;
 constexpr int kMaxLevels = 31;
 
 constexpr int kTravWarps = 4;
@@ -98,16 +97,17 @@ __global__ void extent_kernel(const double *__restrict__ x, const double *__rest
 // ---------------------------------------------------------------------------
 // Cell index of coordinate p at the finest level D: the reference descends
 // from centre 0 / half-width X deciding `p > centre` at every level.
-__device__ __forceinline__ uint32_t axis_cell(double p, double X, double scale, int D)
+__device__ __forceinline__ uint32_t axis_cell(double p, double X, double scale, int D,
+                                              double margin)
 {
-    const double lim = (double)((1u << D) - 1u);
-    double u = __dmul_rn(__dadd_rn(p, X), scale);  // (p + X) / (2X) * 2^D
-    double r = rint(u);
-    const double margin = ldexp(1.0, D - 40);
-    if (fabs(u - r) >= margin || !(u == u)) {
-        double q = ceil(u) - 1.0;
-        q = fmin(fmax(q, 0.0), lim);
-        return (uint32_t)q;
+    const int lim = (int)((1u << D) - 1u);
+    const double u = __dmul_rn(__dadd_rn(p, X), scale);  // (p + X) / (2X) * 2^D
+    const double fl = trunc(u);
+    const double frac = u - fl;  // exact
+    if (!(u == u)) return 0;
+    if (frac >= margin && frac <= 1.0 - margin) {
+        // u is not within `margin` of a cell boundary: ceil(u) - 1 = floor(u)
+        return (uint32_t)min(max((int)fl, 0), lim);
     }
     // Close to a boundary: replay the reference's centre arithmetic.
     double c = 0.0, ext = X;
@@ -149,17 +149,21 @@ __global__ void keys_kernel(const double *__restrict__ x, const double *__restri
                             const unsigned long long *__restrict__ extent_bits,
                             uint64_t *__restrict__ keys, uint32_t *__restrict__ vals)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    __shared__ double s_scale;
     const double X = __longlong_as_double((long long)*extent_bits);
     const int D = tree_levels(nchild);
+    if (threadIdx.x == 0) s_scale = X > 0.0 ? __ddiv_rn(ldexp(1.0, D - 1), X) : 0.0;
+    __syncthreads();
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double scale = s_scale;
+    const double margin = ldexp(1.0, D - 40);
     uint64_t key = 0;
     if (X > 0.0) {
-        const double scale = __ddiv_rn(ldexp(1.0, D - 1), X);
-        const uint32_t qx = axis_cell(x[i], X, scale, D);
-        const uint32_t qy = axis_cell(y[i], X, scale, D);
+        const uint32_t qx = axis_cell(x[i], X, scale, D, margin);
+        const uint32_t qy = axis_cell(y[i], X, scale, D, margin);
         if (nchild == 8) {
-            const uint32_t qz = axis_cell(z[i], X, scale, D);
+            const uint32_t qz = axis_cell(z[i], X, scale, D, margin);
             key = spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2);
         } else {
             key = spread2(qx) | (spread2(qy) << 1);
@@ -204,39 +208,71 @@ radix_hist_kernel(const uint64_t *__restrict__ keys, int n, int shift, uint32_t 
     }
 }
 
-// Exclusive scan of `count` uint32 values in place, one block.
-__global__ void __launch_bounds__(kScanThreads) scan_u32_kernel(uint32_t *__restrict__ v, int count)
+// Block-wide exclusive scan of one value per thread (blockDim.x <= 1024).
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *warp_sums,
+                                                         uint32_t &total)
 {
-    __shared__ uint32_t part[kScanThreads];
-    const int per = (count + kScanThreads - 1) / kScanThreads;
-    const int b = threadIdx.x * per, e = min(b + per, count);
-    uint32_t s = 0;
-    for (int k = b; k < e; ++k) s += v[k];
-    part[threadIdx.x] = s;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
     __syncthreads();
-    for (int off = 1; off < kScanThreads; off <<= 1) {
-        uint32_t t = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
-        __syncthreads();
-        part[threadIdx.x] += t;
-        __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < nw ? warp_sums[lane] : 0;
+        uint32_t wi = w;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += t;
+        }
+        if (lane < nw) warp_sums[lane] = wi - w;
+        if (lane == 31) warp_sums[32] = wi;
     }
-    uint32_t run = part[threadIdx.x] - s;
-    for (int k = b; k < e; ++k) {
-        uint32_t t = v[k];
-        v[k] = run;
-        run += t;
+    __syncthreads();
+    const uint32_t r = warp_sums[warp] + incl - v;
+    total = warp_sums[32];
+    __syncthreads();
+    return r;
+}
+
+// Per digit (one block each), the exclusive prefix over tiles of that
+// digit's counts, in place; the digit's total goes to totals[digit].
+__global__ void __launch_bounds__(kSortThreads)
+radix_digit_scan_kernel(uint32_t *__restrict__ hist, int n_tiles, uint32_t *__restrict__ totals)
+{
+    __shared__ uint32_t ws[33];
+    uint32_t *row = hist + (size_t)blockIdx.x * n_tiles;
+    uint32_t carry = 0;
+    for (int t0 = 0; t0 < n_tiles; t0 += blockDim.x) {
+        const int t = t0 + threadIdx.x;
+        const uint32_t v = t < n_tiles ? row[t] : 0;
+        uint32_t total;
+        const uint32_t ex = block_exclusive_scan(v, ws, total);
+        if (t < n_tiles) row[t] = carry + ex;
+        carry += total;
     }
+    if (threadIdx.x == 0) totals[blockIdx.x] = carry;
 }
 
 __global__ void __launch_bounds__(kSortThreads)
 radix_scatter_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
                      uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int n,
-                     int shift, const uint32_t *__restrict__ offsets, int n_tiles)
+                     int shift, const uint32_t *__restrict__ offsets, int n_tiles,
+                     const uint32_t *__restrict__ totals)
 {
+    static_assert(kSortThreads == kRadixBuckets, "one thread per digit");
     __shared__ uint32_t h[kSortWarps][kRadixBuckets];
+    __shared__ uint32_t digit_base[kRadixBuckets];
+    __shared__ uint32_t ws[33];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int k = threadIdx.x; k < kSortWarps * kRadixBuckets; k += kSortThreads)
         (&h[0][0])[k] = 0;
+    {
+        uint32_t total;
+        digit_base[threadIdx.x] = block_exclusive_scan(totals[threadIdx.x], ws, total);
+    }
     __syncthreads();
     const int base = blockIdx.x * kSortTile + warp * (kSortItems * 32);
     uint64_t kk[kSortItems];
@@ -260,7 +296,7 @@ radix_scatter_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__res
     __syncthreads();
     // exclusive prefix over warps, per digit, plus the global offset
     for (int d = threadIdx.x; d < kRadixBuckets; d += kSortThreads) {
-        uint32_t run = offsets[(size_t)d * n_tiles + blockIdx.x];
+        uint32_t run = digit_base[d] + offsets[(size_t)d * n_tiles + blockIdx.x];
         for (int w = 0; w < kSortWarps; ++w) {
             uint32_t c = h[w][d];
             h[w][d] = run;
@@ -306,6 +342,7 @@ struct NodeArrays {
     double *c64;   // 4 x cap: cx, cy, cz, extent
     float4 *geo;   // cx, cy, cz, extent (f32)
     float4 *com;   // x, y, z, mass (f32)
+    int4 *meta;    // (id | nchild << 28, first child, first body, body count)
     int cap;
 };
 
@@ -395,60 +432,61 @@ level_count_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, const Level
     }
 }
 
-// Exclusive scan of the block sums; sizes the next level (truncating the
-// tree if the node arrays would overflow).
-__global__ void __launch_bounds__(kScanThreads)
-level_scan_kernel(int32_t *__restrict__ bsum, int nblocks, LevelInfo *lv, int level, int cap,
-                  uint32_t *__restrict__ flags)
-{
-    __shared__ int32_t part[kScanThreads];
-    const int per = (nblocks + kScanThreads - 1) / kScanThreads;
-    const int b = threadIdx.x * per, e = min(b + per, nblocks);
-    int32_t s = 0;
-    for (int k = b; k < e; ++k) s += bsum[k];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    for (int off = 1; off < kScanThreads; off <<= 1) {
-        int32_t t = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
-        __syncthreads();
-        part[threadIdx.x] += t;
-        __syncthreads();
-    }
-    int32_t run = part[threadIdx.x] - s;
-    for (int k = b; k < e; ++k) {
-        int32_t t = bsum[k];
-        bsum[k] = run;
-        run += t;
-    }
-    if (threadIdx.x == kScanThreads - 1) {
-        const int32_t total = part[kScanThreads - 1];
-        const int32_t nb = lv->begin[level] + lv->count[level];
-        int32_t take = total;
-        if ((long long)nb + total > cap) {
-            take = 0;  // leave this level's nodes as leaves: exact, slower
-            atomicOr(&flags[kFlagNodes], 1u);
-        }
-        lv->begin[level + 1] = nb;
-        lv->count[level + 1] = take;
-        lv->total = nb + take;
-    }
-}
-
+// Writes the children of the level's nodes.  Every block sums the per-block
+// child counts of level_count_kernel itself (its offset = the sum over
+// earlier blocks), so the next level is sized without a separate scan; the
+// level is left unsplit (its nodes stay leaves: exact, slower) if the node
+// arrays would overflow.
 __global__ void __launch_bounds__(kBuildThreads)
-level_write_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, const LevelInfo *__restrict__ lv,
-                   int level, int leaf, int nchild, const int32_t *__restrict__ boff)
+level_write_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, LevelInfo *lv, int level,
+                   int leaf, int nchild, const int32_t *__restrict__ bsum, int nblocks,
+                   uint32_t *__restrict__ flags)
 {
     const int D = tree_levels(nchild), bits = level_bits(nchild);
     const int cnt = lv->count[level], first = lv->begin[level];
-    if (lv->count[level + 1] == 0) return;  // nothing to write (or truncated)
-    const int child_base = lv->begin[level + 1];
+    __shared__ int32_t ws[kBuildThreads / 32];
+    __shared__ int32_t red_mine[kBuildThreads / 32], red_all[kBuildThreads / 32];
+    __shared__ int32_t carry, level_total;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    {
+        int32_t mine = 0, all = 0;
+        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+            const int32_t v = bsum[b];
+            all += v;
+            if (b < (int)blockIdx.x) mine += v;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            mine += __shfl_xor_sync(0xffffffffu, mine, o);
+            all += __shfl_xor_sync(0xffffffffu, all, o);
+        }
+        if (lane == 0) {
+            red_mine[warp] = mine;
+            red_all[warp] = all;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int32_t m = 0, a = 0;
+            for (int w = 0; w < kBuildThreads / 32; ++w) {
+                m += red_mine[w];
+                a += red_all[w];
+            }
+            carry = m;
+            level_total = a;
+        }
+        __syncthreads();
+    }
+    const int32_t next_begin = first + cnt;
+    const bool fits = (long long)next_begin + level_total <= (long long)nd.cap;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        lv->begin[level + 1] = next_begin;
+        lv->count[level + 1] = fits ? level_total : 0;
+        lv->total = next_begin + (fits ? level_total : 0);
+        if (!fits) atomicOr(&flags[kFlagNodes], 1u);
+    }
+    if (!fits || level_total == 0) return;
+    const int child_base = next_begin;
     const int chunk = (cnt + gridDim.x - 1) / gridDim.x;
     const int cb = blockIdx.x * chunk, ce = min(cb + chunk, cnt);
-    __shared__ int32_t ws[kBuildThreads / 32];
-    __shared__ int32_t carry;
-    if (threadIdx.x == 0) carry = boff[blockIdx.x];
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int k0 = cb; k0 < ce; k0 += blockDim.x) {
         const int k = k0 + threadIdx.x;
         const int node = first + k;
@@ -632,6 +670,7 @@ __global__ void node_finish_kernel(NodeArrays nd, const LevelInfo *__restrict__ 
                               0.f);
         }
         nd.com[i] = com;
+        nd.meta[i] = make_int4(i | ((int)nd.nchild[i] << 28), nd.child[i], b, e - b);
     }
 }
 
@@ -647,9 +686,17 @@ struct TravArgs {
     int n;
     float theta, e;
     double theta64;
+    float extent;  // root half-width X (set on the device before the traversal)
     uint32_t *flags;
     double *partial;
+    const unsigned long long *extent_bits;
+    unsigned long long *stats;  // [0] node visits, [1] pair interactions (lanes)
 };
+
+__device__ __forceinline__ float load_extent(const TravArgs &a)
+{
+    return (float)__longlong_as_double((long long)*a.extent_bits);
+}
 
 // The reference's opening rule `extent / r < theta` (octree.rs:137-144):
 // FP32, re-evaluated in f64 with the reference's arithmetic near the edge.
@@ -657,10 +704,17 @@ __device__ __forceinline__ bool accept_cell(const TravArgs &a, int node, float4 
                                             float qy, float qz, int k)
 {
     const float dx = qx - geo.x, dy = qy - geo.y, dz = qz - geo.z;
-    const float r = sqrtf(dx * dx + dy * dy + dz * dz);
-    const float ratio = geo.w / r;
-    const float band = 1e-4f * fabsf(a.theta) + 1e-30f;
-    if (fabsf(ratio - a.theta) > band && ratio == ratio) return ratio < a.theta;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float inv = rsqrt_approx(r2);
+    const float ratio = geo.w * inv;
+    // Bound on the relative error of `ratio` against the reference's f64
+    // value: rounding positions and centres (|.| <= X) to f32 perturbs each
+    // difference by <= 3 * 2^-24 * X, i.e. r by <= 3.1e-7 X; rsqrt.approx and
+    // the f32 extent add ~3e-7.  Decisions inside twice that band are redone
+    // in f64 with the reference's operations.
+    const float band = fabsf(a.theta) * (6.4e-7f * a.extent * inv + 1e-6f) + 1e-30f;
+    if (fabsf(ratio - a.theta) > band && ratio == ratio && r2 > 1e-30f)
+        return ratio < a.theta;
     const size_t cap = a.nd.cap;
     const double d0 = a.spos[k] - a.nd.c64[node];
     const double d1 = a.spos[a.n + k] - a.nd.c64[cap + node];
@@ -697,9 +751,12 @@ struct StackEntry {
 };
 
 __global__ void __launch_bounds__(kTravWarps * 32)
-traverse_exact_kernel(TravArgs a)
+traverse_exact_kernel(TravArgs a_in)
 {
     __shared__ StackEntry stack[kTravWarps][kStack];
+    TravArgs a = a_in;
+    a.extent = load_extent(a_in);
+    unsigned long long visits = 0, pairs = 0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int k0 = (blockIdx.x * kTravWarps + warp) * 32;
     if (k0 >= a.n) return;
@@ -724,8 +781,10 @@ traverse_exact_kernel(TravArgs a)
         bool acc = false;
         if (in) acc = accept_cell(a, node, geo, q.x, q.y, q.z, k);
         const uint32_t open = top.mask & ~__ballot_sync(0xffffffffu, acc);
+        ++visits;
         if (acc) {
             pair_acc(q.x, q.y, q.z, a.nd.com[node], a.e, ax, ay, az);
+            ++pairs;
         }
         ++since_fold;
         if (child < 0) {
@@ -736,6 +795,7 @@ traverse_exact_kernel(TravArgs a)
                     const float4 bj = a.sbody[j];
                     if (mine) pair_acc(q.x, q.y, q.z, bj, a.e, ax, ay, az);
                 }
+                if (mine) pairs += c;
                 since_fold += c;
             }
         } else if (open) {
@@ -760,6 +820,11 @@ traverse_exact_kernel(TravArgs a)
     fold(hx, lx, ax);
     fold(hy, ly, ay);
     fold(hz, lz, az);
+    for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+    if (lane == 0) {
+        atomicAdd(&a.stats[0], visits);
+        atomicAdd(&a.stats[1], pairs);
+    }
     if (valid) {
         const uint32_t i = a.order[k];
         a.partial[i] = (double)hx + (double)lx;
@@ -768,62 +833,97 @@ traverse_exact_kernel(TravArgs a)
     }
 }
 
+// Warp traversal.  The shared stack holds, per pending node, its id, its
+// geometry and its metadata (first child, first body, body count), loaded
+// when the node is pushed (one lane per child, in parallel), so popping a
+// node needs no global load.  Accepted cells and the bodies of opened leaves
+// are queued as indices (>= 0 body, < 0 cell) and gathered 32 at a time
+// into shared memory when the queue is flushed.
+constexpr int kQueue = 96;
+
 __global__ void __launch_bounds__(kTravWarps * 32)
-traverse_warp_kernel(TravArgs a)
+traverse_warp_kernel(TravArgs a_in)
 {
-    __shared__ int32_t stack[kTravWarps][kStack];
-    __shared__ float4 buf[kTravWarps][kBuf];
+    __shared__ float4 sgeo[kTravWarps][kStack];
+    __shared__ int4 smeta[kTravWarps][kStack];  // node, first child, first body, count
+    __shared__ int32_t queue[kTravWarps][kQueue];
+    __shared__ float4 tile[kTravWarps][32];
+    TravArgs a = a_in;
+    a.extent = load_extent(a_in);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int k0 = (blockIdx.x * kTravWarps + warp) * 32;
     if (k0 >= a.n) return;
     const int k = k0 + lane;
     const bool valid = k < a.n;
+    const int nvalid = __popc(__ballot_sync(0xffffffffu, valid));
     const float4 q = valid ? a.sbody[k] : a.sbody[k0];
     float ax = 0.f, ay = 0.f, az = 0.f, hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
-    int nb = 0;
+    unsigned long long visits = 0, pairs = 0;
+    int nq = 0;
     int sp = 1;
-    if (lane == 0) stack[warp][0] = 0;
+    if (lane == 0) {
+        sgeo[warp][0] = a.nd.geo[0];
+        smeta[warp][0] = a.nd.meta[0];
+    }
     __syncwarp();
     auto flush = [&]() {
-        __syncwarp();
-        for (int j = 0; j < nb; ++j) pair_acc(q.x, q.y, q.z, buf[warp][j], a.e, ax, ay, az);
+        for (int j0 = 0; j0 < nq; j0 += 32) {
+            const int m = min(32, nq - j0);
+            __syncwarp();
+            if (lane < m) {
+                const int r = queue[warp][j0 + lane];
+                tile[warp][lane] = r >= 0 ? a.sbody[r] : a.nd.com[-r - 1];
+            }
+            __syncwarp();
+            for (int j = 0; j < m; ++j) pair_acc(q.x, q.y, q.z, tile[warp][j], a.e, ax, ay, az);
+        }
+        pairs += nq;
         fold(hx, lx, ax);
         fold(hy, ly, ay);
         fold(hz, lz, az);
-        nb = 0;
+        nq = 0;
         __syncwarp();
     };
     while (sp > 0) {
-        const int node = stack[warp][--sp];
+        --sp;
+        const float4 geo = sgeo[warp][sp];
+        const int4 meta = smeta[warp][sp];  // node, child, begin, count
         __syncwarp();
-        const float4 geo = a.nd.geo[node];
-        const int child = a.nd.child[node];
+        ++visits;
+        const int node = meta.x & 0x0fffffff;
         const bool acc = valid ? accept_cell(a, node, geo, q.x, q.y, q.z, k) : true;
         if (__all_sync(0xffffffffu, acc)) {
-            if (nb + 1 > kBuf) flush();
-            if (lane == 0) buf[warp][nb] = a.nd.com[node];
-            nb += 1;
-        } else if (child < 0) {
-            const int b = a.nd.begin[node], c = a.nd.count[node];
-            for (int j0 = 0; j0 < c; j0 += 32) {
-                const int m = min(32, c - j0);
-                if (nb + m > kBuf) flush();
-                if (lane < m) buf[warp][nb + lane] = a.sbody[b + j0 + lane];
-                nb += m;
+            if (nq + 1 > kQueue) flush();
+            if (lane == 0) queue[warp][nq] = -node - 1;
+            nq += 1;
+        } else if (meta.y < 0) {
+            for (int j0 = 0; j0 < meta.w; j0 += 32) {
+                const int m = min(32, meta.w - j0);
+                if (nq + m > kQueue) flush();
+                if (lane < m) queue[warp][nq + lane] = meta.z + j0 + lane;
+                nq += m;
             }
         } else {
-            const int nc = a.nd.nchild[node];
+            const int nc = (int)((uint32_t)meta.x >> 28);
             if (sp + nc > kStack) {
                 if (lane == 0) atomicOr(&a.flags[kFlagStack], 1u);
                 break;
             }
-            if (lane < nc) stack[warp][sp + lane] = child + lane;
+            if (lane < nc) {
+                const int c = meta.y + lane;
+                sgeo[warp][sp + lane] = a.nd.geo[c];
+                smeta[warp][sp + lane] = a.nd.meta[c];
+            }
             sp += nc;
         }
         __syncwarp();
-        if (nb >= 64) flush();
+        if (nq >= 64) flush();
     }
     flush();
+    if (lane == 0) {
+        atomicAdd(&a.stats[0], visits);
+        atomicAdd(&a.stats[1], pairs * (unsigned long long)nvalid);
+    }
     if (valid) {
         const uint32_t i = a.order[k];
         a.partial[i] = (double)hx + (double)lx;
@@ -847,25 +947,31 @@ struct BhWorkspace {
     uint64_t *keys[2] = {nullptr, nullptr};
     uint32_t *vals[2] = {nullptr, nullptr};
     uint32_t *hist = nullptr;
+    uint32_t *digit_totals = nullptr;
     float4 *sbody = nullptr;
     double *spos = nullptr, *smass = nullptr, *pref = nullptr, *mom_bsum = nullptr;
     NodeArrays nd = {};
     LevelInfo *lv = nullptr;
     int32_t *bsum = nullptr;
     unsigned long long *extent_bits = nullptr;
+    unsigned long long *stats = nullptr;  // node visits, pair interactions of the last traversal
     uint32_t *flags = nullptr;
     int launches = 0;
     // which key/val buffer holds the sorted result
     int sorted = 0;
+    // optional events around the traversal kernel (recorded into graphs too)
+    bool profiling = false;
+    cudaEvent_t trav_ev[2] = {nullptr, nullptr};
 };
 
 static void ws_release(BhWorkspace *ws)
 {
     void *p[] = {ws->keys[0],  ws->keys[1],   ws->vals[0],       ws->vals[1],     ws->hist,
+                 ws->digit_totals,
                  ws->sbody,    ws->spos,      ws->smass,         ws->pref,        ws->mom_bsum,
                  ws->nd.begin, ws->nd.count,  ws->nd.child,      ws->nd.nchild,   ws->nd.level,
                  ws->nd.c64,   ws->nd.geo,    ws->nd.com,        ws->lv,          ws->bsum,
-                 ws->extent_bits, ws->flags};
+                 ws->extent_bits, ws->flags, ws->nd.meta, ws->stats};
     for (void *q : p)
         if (q) cudaFree(q);
 }
@@ -906,6 +1012,7 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device)
     PG_WA(w->vals[0], cap);
     PG_WA(w->vals[1], cap);
     PG_WA(w->hist, (size_t)kRadixBuckets * tiles);
+    PG_WA(w->digit_totals, kRadixBuckets);
     PG_WA(w->sbody, cap);
     PG_WA(w->spos, 3 * cap);
     PG_WA(w->smass, cap);
@@ -919,6 +1026,8 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device)
     PG_WA(w->nd.c64, 4 * ncap);
     PG_WA(w->nd.geo, ncap);
     PG_WA(w->nd.com, ncap);
+    PG_WA(w->nd.meta, ncap);
+    PG_WA(w->stats, 4);
     PG_WA(w->lv, 1);
     PG_WA(w->bsum, (size_t)w->grid_build);
     PG_WA(w->extent_bits, 1);
@@ -940,11 +1049,43 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device)
 void bh_free(BhWorkspace *ws)
 {
     if (!ws) return;
+    for (cudaEvent_t e : ws->trav_ev)
+        if (e) cudaEventDestroy(e);
     ws_release(ws);
     delete ws;
 }
 
+int bh_set_profiling(BhWorkspace *ws, bool enable)
+{
+    PG_CHECK(ws, PHYSIM_ERR_ARGUMENT, "null workspace");
+    if (enable && !ws->trav_ev[0])
+        for (cudaEvent_t &e : ws->trav_ev) PG_CUDA(cudaEventCreate(&e));
+    ws->profiling = enable;
+    return PHYSIM_OK;
+}
+
+int bh_traversal_ms(BhWorkspace *ws, double *ms)
+{
+    PG_CHECK(ws && ms && ws->profiling, PHYSIM_ERR_ARGUMENT, "profiling is off");
+    PG_CUDA(cudaEventSynchronize(ws->trav_ev[1]));
+    float t = 0.f;
+    PG_CUDA(cudaEventElapsedTime(&t, ws->trav_ev[0], ws->trav_ev[1]));
+    *ms = t;
+    return PHYSIM_OK;
+}
+
 int bh_launches(const BhWorkspace *ws) { return ws ? ws->launches : 0; }
+
+int bh_stats(BhWorkspace *ws, cudaStream_t st, uint64_t out[2])
+{
+    PG_CHECK(ws && out, PHYSIM_ERR_ARGUMENT, "null argument");
+    unsigned long long h[2] = {0, 0};
+    PG_CUDA(cudaMemcpyAsync(h, ws->stats, sizeof h, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    out[0] = h[0];
+    out[1] = h[1];
+    return PHYSIM_OK;
+}
 
 static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, cudaStream_t st)
 {
@@ -962,10 +1103,11 @@ static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, c
     int cur = 0;
     for (int shift = 0; shift < key_bits; shift += kRadixBits) {
         radix_hist_kernel<<<tiles, kSortThreads, 0, st>>>(ws->keys[cur], n, shift, ws->hist, tiles);
-        scan_u32_kernel<<<1, kScanThreads, 0, st>>>(ws->hist, kRadixBuckets * tiles);
+        radix_digit_scan_kernel<<<kRadixBuckets, kSortThreads, 0, st>>>(ws->hist, tiles,
+                                                                        ws->digit_totals);
         radix_scatter_kernel<<<tiles, kSortThreads, 0, st>>>(
             ws->keys[cur], shift == 0 ? nullptr : ws->vals[cur], ws->keys[cur ^ 1],
-            ws->vals[cur ^ 1], n, shift, ws->hist, tiles);
+            ws->vals[cur ^ 1], n, shift, ws->hist, tiles, ws->digit_totals);
         cur ^= 1;
         launches += 3;
     }
@@ -978,11 +1120,10 @@ static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, c
     for (int level = 0; level < D; ++level) {
         level_count_kernel<<<ws->grid_build, kBuildThreads, 0, st>>>(
             ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->bsum);
-        level_scan_kernel<<<1, kScanThreads, 0, st>>>(ws->bsum, ws->grid_build, ws->lv, level,
-                                                      ws->nd.cap, ws->flags);
         level_write_kernel<<<ws->grid_build, kBuildThreads, 0, st>>>(
-            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->bsum);
-        launches += 3;
+            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->bsum, ws->grid_build,
+            ws->flags);
+        launches += 2;
     }
     moment_partial_kernel<<<ws->grid_mom, kMomThreads, 0, st>>>(ws->spos, ws->smass, n,
                                                                 ws->mom_bsum);
@@ -1017,12 +1158,18 @@ int bh_accelerations(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, 
     a.e = (float)p.e;
     a.flags = ws->flags;
     a.partial = partial;
+    a.extent = 0.f;  // read on the device from extent_bits
+    a.extent_bits = ws->extent_bits;
+    a.stats = ws->stats;
+    PG_CUDA(cudaMemsetAsync(ws->stats, 0, 2 * sizeof(unsigned long long), st));
     const int blocks = cdiv(cdiv(n, 32), kTravWarps);
+    if (ws->profiling) PG_CUDA(cudaEventRecord(ws->trav_ev[0], st));
     if (p.traversal == PHYSIM_TRAVERSAL_WARP)
         traverse_warp_kernel<<<blocks, kTravWarps * 32, 0, st>>>(a);
     else
         traverse_exact_kernel<<<blocks, kTravWarps * 32, 0, st>>>(a);
     PG_CUDA(cudaGetLastError());
+    if (ws->profiling) PG_CUDA(cudaEventRecord(ws->trav_ev[1], st));
     ws->launches += 1;
     return PHYSIM_OK;
 }

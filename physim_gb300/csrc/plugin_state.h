@@ -57,6 +57,11 @@ int bh_accelerations(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, 
                      cudaStream_t stream);
 // Kernel launches one bh_accelerations call makes.
 int bh_launches(const BhWorkspace *ws);
+// Events around the traversal kernel; its last duration in milliseconds.
+int bh_set_profiling(BhWorkspace *ws, bool enable);
+int bh_traversal_ms(BhWorkspace *ws, double *ms);
+// Node visits (per warp) and pair interactions (per body) of the last traversal.
+int bh_stats(BhWorkspace *ws, cudaStream_t stream, uint64_t out[2]);
 // Copies keys, sort order and tree of the last build to host arrays.
 int bh_snapshot(BhWorkspace *ws, size_t n, cudaStream_t stream, PhysimTreeSnapshot *out);
 

@@ -227,6 +227,15 @@ int physim_gpu_sim_set_profiling(PhysimSim *s, int enable)
     if (enable && !s->ev[0])
         for (cudaEvent_t &e : s->ev) PG_CUDA(cudaEventCreate(&e));
     s->profiling = enable != 0;
+    if (s->bh) {
+        PG_TRY(bh_set_profiling(s->bh, s->profiling));
+        // the captured gravity phase must be re-captured with (or without)
+        // the traversal events
+        if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+        if (s->graph) cudaGraphDestroy(s->graph);
+        s->graph_exec = nullptr;
+        s->graph = nullptr;
+    }
     return PHYSIM_OK;
 }
 
@@ -292,6 +301,24 @@ int physim_gpu_sim_tree_snapshot(PhysimSim *s, PhysimTreeSnapshot *out)
     int splits = 1;
     if (s->n) PG_TRY(sim_forces(s, &splits));
     return bh_snapshot(s->bh, s->n, s->stream, out);
+}
+
+int physim_gpu_sim_bh_stats(PhysimSim *s, uint64_t *node_visits, uint64_t *interactions,
+                            double *traversal_ms)
+{
+    PG_CHECK(s && node_visits && interactions, PHYSIM_ERR_ARGUMENT, "null argument");
+    PG_CHECK(s->cfg.gravity != PHYSIM_GRAVITY_SIMPLE_ASTRO, PHYSIM_ERR_ARGUMENT,
+             "simple_astro has no traversal");
+    PG_CUDA(cudaSetDevice(s->cfg.device));
+    uint64_t v[2];
+    PG_TRY(bh_stats(s->bh, s->stream, v));
+    *node_visits = v[0];
+    *interactions = v[1];
+    if (traversal_ms) {
+        *traversal_ms = -1.0;
+        if (s->profiling) PG_TRY(bh_traversal_ms(s->bh, traversal_ms));
+    }
+    return PHYSIM_OK;
 }
 
 int physim_gpu_sim_synchronize(PhysimSim *s)

@@ -102,6 +102,13 @@ class Simulation:
                 "com": com[:4 * m].reshape(m, 4), "n_nodes": int(s.n_nodes),
                 "extent": s.extent, "flags": int(s.flags)}
 
+    def bh_stats(self) -> dict:
+        """Node visits and pair interactions of the most recent traversal."""
+        v, i, t = C.c_uint64(), C.c_uint64(), C.c_double()
+        check(lib.physim_gpu_sim_bh_stats(self.handle, C.byref(v), C.byref(i), C.byref(t)),
+              "physim_gpu_sim_bh_stats")
+        return {"node_visits": v.value, "interactions": i.value, "traversal_ms": t.value}
+
     def set_profiling(self, enable: bool = True) -> None:
         check(lib.physim_gpu_sim_set_profiling(self.handle, 1 if enable else 0),
               "physim_gpu_sim_set_profiling")
