@@ -409,13 +409,24 @@ __device__ int node_child_count(const uint64_t *__restrict__ keys, const NodeArr
 }
 
 // Per-block sums of child counts over the level's nodes (block b takes a
-// contiguous chunk).
+// contiguous chunk).  The last block to finish (atomic ticket after a
+// memory fence; nothing waits) turns the block sums into exclusive offsets
+// and sizes the next level, leaving it empty (the level's nodes stay
+// leaves: exact, slower) if the node arrays would overflow.
 __global__ void __launch_bounds__(kBuildThreads)
-level_count_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, const LevelInfo *__restrict__ lv,
-                   int level, int leaf, int nchild, int32_t *__restrict__ bsum)
+level_count_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, LevelInfo *lv, int level,
+                   int leaf, int nchild, int32_t *__restrict__ bsum,
+                   unsigned int *__restrict__ ticket, uint32_t *__restrict__ flags)
 {
     const int D = tree_levels(nchild), bits = level_bits(nchild);
     const int cnt = lv->count[level], first = lv->begin[level];
+    if (cnt == 0) {  // empty level: the tree is complete
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            lv->begin[level + 1] = first;
+            lv->count[level + 1] = 0;
+        }
+        return;
+    }
     const int chunk = (cnt + gridDim.x - 1) / gridDim.x;
     const int cb = blockIdx.x * chunk, ce = min(cb + chunk, cnt);
     int s = 0;
@@ -423,68 +434,51 @@ level_count_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, const Level
         s += node_child_count(keys, nd, first + k, leaf, level, D, bits, nchild);
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     __shared__ int ws[kBuildThreads / 32];
+    __shared__ bool last;
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
     __syncthreads();
     if (threadIdx.x == 0) {
         int t = 0;
         for (int w = 0; w < kBuildThreads / 32; ++w) t += ws[w];
         bsum[blockIdx.x] = t;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x == 0) {
+        int32_t run = 0;
+        for (int b = 0; b < (int)gridDim.x; ++b) {
+            const int32_t v = ((volatile int32_t *)bsum)[b];
+            bsum[b] = run;
+            run += v;
+        }
+        const int32_t next_begin = first + cnt;
+        const bool fits = (long long)next_begin + run <= (long long)nd.cap;
+        lv->begin[level + 1] = next_begin;
+        lv->count[level + 1] = fits ? run : 0;
+        lv->total = next_begin + (fits ? run : 0);
+        if (!fits) atomicOr(&flags[kFlagNodes], 1u);
+        *ticket = 0;
     }
 }
 
-// Writes the children of the level's nodes.  Every block sums the per-block
-// child counts of level_count_kernel itself (its offset = the sum over
-// earlier blocks), so the next level is sized without a separate scan; the
-// level is left unsplit (its nodes stay leaves: exact, slower) if the node
-// arrays would overflow.
+// Writes the children of the level's nodes at the offsets level_count_kernel
+// produced.
 __global__ void __launch_bounds__(kBuildThreads)
-level_write_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, LevelInfo *lv, int level,
-                   int leaf, int nchild, const int32_t *__restrict__ bsum, int nblocks,
-                   uint32_t *__restrict__ flags)
+level_write_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, const LevelInfo *__restrict__ lv,
+                   int level, int leaf, int nchild, const int32_t *__restrict__ boff)
 {
     const int D = tree_levels(nchild), bits = level_bits(nchild);
     const int cnt = lv->count[level], first = lv->begin[level];
+    if (cnt == 0 || lv->count[level + 1] == 0) return;
     __shared__ int32_t ws[kBuildThreads / 32];
-    __shared__ int32_t red_mine[kBuildThreads / 32], red_all[kBuildThreads / 32];
-    __shared__ int32_t carry, level_total;
+    __shared__ int32_t carry;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    {
-        int32_t mine = 0, all = 0;
-        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
-            const int32_t v = bsum[b];
-            all += v;
-            if (b < (int)blockIdx.x) mine += v;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            mine += __shfl_xor_sync(0xffffffffu, mine, o);
-            all += __shfl_xor_sync(0xffffffffu, all, o);
-        }
-        if (lane == 0) {
-            red_mine[warp] = mine;
-            red_all[warp] = all;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int32_t m = 0, a = 0;
-            for (int w = 0; w < kBuildThreads / 32; ++w) {
-                m += red_mine[w];
-                a += red_all[w];
-            }
-            carry = m;
-            level_total = a;
-        }
-        __syncthreads();
-    }
-    const int32_t next_begin = first + cnt;
-    const bool fits = (long long)next_begin + level_total <= (long long)nd.cap;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        lv->begin[level + 1] = next_begin;
-        lv->count[level + 1] = fits ? level_total : 0;
-        lv->total = next_begin + (fits ? level_total : 0);
-        if (!fits) atomicOr(&flags[kFlagNodes], 1u);
-    }
-    if (!fits || level_total == 0) return;
-    const int child_base = next_begin;
+    if (threadIdx.x == 0) carry = boff[blockIdx.x];
+    __syncthreads();
+    const int child_base = lv->begin[level + 1];
     const int chunk = (cnt + gridDim.x - 1) / gridDim.x;
     const int cb = blockIdx.x * chunk, ce = min(cb + chunk, cnt);
     for (int k0 = cb; k0 < ce; k0 += blockDim.x) {
@@ -833,20 +827,38 @@ traverse_exact_kernel(TravArgs a_in)
     }
 }
 
-// Warp traversal.  The shared stack holds, per pending node, its id, its
-// geometry and its metadata (first child, first body, body count), loaded
-// when the node is pushed (one lane per child, in parallel), so popping a
-// node needs no global load.  Accepted cells and the bodies of opened leaves
-// are queued as indices (>= 0 body, < 0 cell) and gathered 32 at a time
-// into shared memory when the queue is flushed.
-constexpr int kQueue = 96;
+// Warp traversal: the 32 bodies of a warp (consecutive in Morton order) walk
+// the tree together, and the lanes work on different cells.  Each iteration
+// takes up to 32 pending cells from the top of a shared stack, one per lane,
+// and tests each against the warp's bounding box: a cell is accepted when
+//     extent * (1 + 2e-6) < theta * (r_min - 6e-7 X),
+// r_min = distance from the cell centre to the box.  Every body of the warp
+// is at least r_min (less f32 rounding of positions and centres, <= 2.1e-7 X)
+// from the centre, so an accepted cell passes every body's own f64 reference
+// test extent / r < theta; cells that some body would open are opened.
+// Accepted cells and the bodies of opened leaves are queued (>= 0 body,
+// < 0 cell) and gathered 32 at a time into shared memory, where all lanes
+// evaluate them against their own body.
+constexpr int kGStack = 1024;                 // pending cells per warp
+constexpr int kGWide = kGStack - 256 - 8 * 22;  // above this, pop one cell at a time
+constexpr int kGQueue = 640;                  // queued interactions per warp
+
+__device__ __forceinline__ int warp_exclusive_scan(int v, int lane, int &total)
+{
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += t;
+    }
+    total = __shfl_sync(0xffffffffu, x, 31);
+    return x - v;
+}
 
 __global__ void __launch_bounds__(kTravWarps * 32)
 traverse_warp_kernel(TravArgs a_in)
 {
-    __shared__ float4 sgeo[kTravWarps][kStack];
-    __shared__ int4 smeta[kTravWarps][kStack];  // node, first child, first body, count
-    __shared__ int32_t queue[kTravWarps][kQueue];
+    __shared__ int32_t gstack[kTravWarps][kGStack];
+    __shared__ int32_t queue[kTravWarps][kGQueue];
     __shared__ float4 tile[kTravWarps][32];
     TravArgs a = a_in;
     a.extent = load_extent(a_in);
@@ -857,14 +869,22 @@ traverse_warp_kernel(TravArgs a_in)
     const bool valid = k < a.n;
     const int nvalid = __popc(__ballot_sync(0xffffffffu, valid));
     const float4 q = valid ? a.sbody[k] : a.sbody[k0];
+    float lo_x = q.x, hi_x = q.x, lo_y = q.y, hi_y = q.y, lo_z = q.z, hi_z = q.z;
+    for (int o = 16; o > 0; o >>= 1) {
+        lo_x = fminf(lo_x, __shfl_xor_sync(0xffffffffu, lo_x, o));
+        hi_x = fmaxf(hi_x, __shfl_xor_sync(0xffffffffu, hi_x, o));
+        lo_y = fminf(lo_y, __shfl_xor_sync(0xffffffffu, lo_y, o));
+        hi_y = fmaxf(hi_y, __shfl_xor_sync(0xffffffffu, hi_y, o));
+        lo_z = fminf(lo_z, __shfl_xor_sync(0xffffffffu, lo_z, o));
+        hi_z = fmaxf(hi_z, __shfl_xor_sync(0xffffffffu, hi_z, o));
+    }
+    const float slack = 6.0e-7f * a.extent;
+    const float theta = a.theta;
     float ax = 0.f, ay = 0.f, az = 0.f, hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
     unsigned long long visits = 0, pairs = 0;
     int nq = 0;
     int sp = 1;
-    if (lane == 0) {
-        sgeo[warp][0] = a.nd.geo[0];
-        smeta[warp][0] = a.nd.meta[0];
-    }
+    if (lane == 0) gstack[warp][0] = 0;
     __syncwarp();
     auto flush = [&]() {
         for (int j0 = 0; j0 < nq; j0 += 32) {
@@ -884,43 +904,64 @@ traverse_warp_kernel(TravArgs a_in)
         nq = 0;
         __syncwarp();
     };
+    bool overflow = false;
     while (sp > 0) {
-        --sp;
-        const float4 geo = sgeo[warp][sp];
-        const int4 meta = smeta[warp][sp];  // node, child, begin, count
+        const int m = sp > kGWide ? 1 : min(32, sp);
+        int cell = 0;
+        if (lane < m) cell = gstack[warp][sp - m + lane];
         __syncwarp();
-        ++visits;
-        const int node = meta.x & 0x0fffffff;
-        const bool acc = valid ? accept_cell(a, node, geo, q.x, q.y, q.z, k) : true;
-        if (__all_sync(0xffffffffu, acc)) {
-            if (nq + 1 > kQueue) flush();
-            if (lane == 0) queue[warp][nq] = -node - 1;
-            nq += 1;
-        } else if (meta.y < 0) {
-            for (int j0 = 0; j0 < meta.w; j0 += 32) {
-                const int m = min(32, meta.w - j0);
-                if (nq + m > kQueue) flush();
-                if (lane < m) queue[warp][nq + lane] = meta.z + j0 + lane;
-                nq += m;
+        sp -= m;
+        visits += m;
+        int qref = 0, qcnt = 0, nchild = 0, first_child = 0;
+        if (lane < m) {
+            const float4 geo = a.nd.geo[cell];
+            const int4 meta = a.nd.meta[cell];
+            const float dx = fmaxf(fmaxf(lo_x - geo.x, geo.x - hi_x), 0.f);
+            const float dy = fmaxf(fmaxf(lo_y - geo.y, geo.y - hi_y), 0.f);
+            const float dz = fmaxf(fmaxf(lo_z - geo.z, geo.z - hi_z), 0.f);
+            const float rmin = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - slack;
+            const bool acc = theta > 0.f && rmin > 0.f && geo.w * (1.f + 2e-6f) < theta * rmin;
+            if (acc) {
+                qref = -cell - 1;
+                qcnt = 1;
+            } else if (meta.y < 0) {
+                qref = meta.z;  // first body of the leaf
+                qcnt = meta.w;
+            } else {
+                nchild = (int)((uint32_t)meta.x >> 28);
+                first_child = meta.y;
             }
-        } else {
-            const int nc = (int)((uint32_t)meta.x >> 28);
-            if (sp + nc > kStack) {
-                if (lane == 0) atomicOr(&a.flags[kFlagStack], 1u);
-                break;
+        }
+        // push the children of opened cells
+        int ctotal;
+        const int coff = warp_exclusive_scan(nchild, lane, ctotal);
+        if (sp + ctotal > kGStack) {
+            overflow = true;
+            break;
+        }
+        for (int c = 0; c < nchild; ++c) gstack[warp][sp + coff + c] = first_child + c;
+        sp += ctotal;
+        // queue cells and leaf bodies, at most 16 entries per lane per round
+        while (__any_sync(0xffffffffu, qcnt > 0)) {
+            const int take = min(qcnt, 16);
+            int qtotal;
+            const int qoff = warp_exclusive_scan(take, lane, qtotal);
+            if (nq + qtotal > kGQueue) flush();
+            if (qref < 0) {
+                if (take) queue[warp][nq + qoff] = qref;
+            } else {
+                for (int j = 0; j < take; ++j) queue[warp][nq + qoff + j] = qref + j;
+                qref += take;
             }
-            if (lane < nc) {
-                const int c = meta.y + lane;
-                sgeo[warp][sp + lane] = a.nd.geo[c];
-                smeta[warp][sp + lane] = a.nd.meta[c];
-            }
-            sp += nc;
+            qcnt -= take;
+            nq += qtotal;
         }
         __syncwarp();
-        if (nq >= 64) flush();
+        if (nq >= 256) flush();
     }
     flush();
     if (lane == 0) {
+        if (overflow) atomicOr(&a.flags[kFlagStack], 1u);
         atomicAdd(&a.stats[0], visits);
         atomicAdd(&a.stats[1], pairs * (unsigned long long)nvalid);
     }
@@ -955,6 +996,7 @@ struct BhWorkspace {
     int32_t *bsum = nullptr;
     unsigned long long *extent_bits = nullptr;
     unsigned long long *stats = nullptr;  // node visits, pair interactions of the last traversal
+    unsigned int *ticket = nullptr;       // last-block ticket of level_count_kernel (kept at 0)
     uint32_t *flags = nullptr;
     int launches = 0;
     // which key/val buffer holds the sorted result
@@ -971,7 +1013,7 @@ static void ws_release(BhWorkspace *ws)
                  ws->sbody,    ws->spos,      ws->smass,         ws->pref,        ws->mom_bsum,
                  ws->nd.begin, ws->nd.count,  ws->nd.child,      ws->nd.nchild,   ws->nd.level,
                  ws->nd.c64,   ws->nd.geo,    ws->nd.com,        ws->lv,          ws->bsum,
-                 ws->extent_bits, ws->flags, ws->nd.meta, ws->stats};
+                 ws->extent_bits, ws->flags, ws->nd.meta, ws->stats, ws->ticket};
     for (void *q : p)
         if (q) cudaFree(q);
 }
@@ -997,7 +1039,7 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device)
     const size_t cap = n < 64 ? 64 : n;
     w->cap_n = cap;
     const int sms = device_sm_count(device);
-    w->grid_build = sms * 4;
+    w->grid_build = sms * 2;
     w->grid_mom = sms * 2;
     const int tiles = cdiv((long long)cap, kSortTile);
     // Node capacity: about 4N nodes holds every non-degenerate distribution
@@ -1028,15 +1070,16 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device)
     PG_WA(w->nd.com, ncap);
     PG_WA(w->nd.meta, ncap);
     PG_WA(w->stats, 4);
+    PG_WA(w->ticket, 1);
     PG_WA(w->lv, 1);
     PG_WA(w->bsum, (size_t)w->grid_build);
     PG_WA(w->extent_bits, 1);
     PG_WA(w->flags, 4);
 #undef PG_WA
     w->nd.cap = (int)ncap;
-    if (rc == PHYSIM_OK) rc = cudaMemset(w->flags, 0, 4 * sizeof(uint32_t)) == cudaSuccess
-                                  ? PHYSIM_OK
-                                  : PHYSIM_ERR_CUDA;
+    if (rc == PHYSIM_OK && (cudaMemset(w->flags, 0, 4 * sizeof(uint32_t)) != cudaSuccess ||
+                            cudaMemset(w->ticket, 0, sizeof(unsigned int)) != cudaSuccess))
+        rc = PHYSIM_ERR_CUDA;
     if (rc != PHYSIM_OK) {
         ws_release(w);
         delete w;
@@ -1119,10 +1162,10 @@ static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, c
     const int D = tree_levels(p.nchild);
     for (int level = 0; level < D; ++level) {
         level_count_kernel<<<ws->grid_build, kBuildThreads, 0, st>>>(
-            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->bsum);
-        level_write_kernel<<<ws->grid_build, kBuildThreads, 0, st>>>(
-            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->bsum, ws->grid_build,
+            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->bsum, ws->ticket,
             ws->flags);
+        level_write_kernel<<<ws->grid_build, kBuildThreads, 0, st>>>(
+            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->bsum);
         launches += 2;
     }
     moment_partial_kernel<<<ws->grid_mom, kMomThreads, 0, st>>>(ws->spos, ws->smass, n,
@@ -1163,13 +1206,16 @@ int bh_accelerations(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, 
     a.stats = ws->stats;
     PG_CUDA(cudaMemsetAsync(ws->stats, 0, 2 * sizeof(unsigned long long), st));
     const int blocks = cdiv(cdiv(n, 32), kTravWarps);
-    if (ws->profiling) PG_CUDA(cudaEventRecord(ws->trav_ev[0], st));
+    // external records, so they also time the kernel when replayed from a graph
+    if (ws->profiling)
+        PG_CUDA(cudaEventRecordWithFlags(ws->trav_ev[0], st, cudaEventRecordExternal));
     if (p.traversal == PHYSIM_TRAVERSAL_WARP)
         traverse_warp_kernel<<<blocks, kTravWarps * 32, 0, st>>>(a);
     else
         traverse_exact_kernel<<<blocks, kTravWarps * 32, 0, st>>>(a);
     PG_CUDA(cudaGetLastError());
-    if (ws->profiling) PG_CUDA(cudaEventRecord(ws->trav_ev[1], st));
+    if (ws->profiling)
+        PG_CUDA(cudaEventRecordWithFlags(ws->trav_ev[1], st, cudaEventRecordExternal));
     ws->launches += 1;
     return PHYSIM_OK;
 }
