@@ -369,11 +369,67 @@ __global__ void root_kernel(NodeArrays nd, LevelInfo *lv, int n,
     nd.c64[3 * (size_t)nd.cap] = X;
 }
 
-// Child ranges of a node: bounds[c] = first sorted index in [b, e) whose
-// digit at `shift` is >= c; bounds[nchild] = e.
-__device__ __forceinline__ void child_bounds(const uint64_t *__restrict__ keys, int b, int e,
-                                             int shift, int nchild, int *bounds)
+// The top levels hold few, large nodes whose child ranges would take long
+// binary searches.  For levels <= kTop, child ranges come from a table of
+// cell starts at level kTop instead: top[p] = first sorted index whose
+// level-kTop prefix is >= p (so empty cells point at the next cell), top[cells] = n.
+__host__ __device__ inline int top_levels(int nchild) { return nchild == 8 ? 5 : 7; }
+
+__global__ void top_mark_kernel(const uint64_t *__restrict__ keys, int n, int shift,
+                                int32_t *__restrict__ top)
 {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint64_t p = keys[k] >> shift;
+    if (k == 0 || (keys[k - 1] >> shift) != p) top[p] = k;
+}
+
+// Suffix minimum over the marks (-1 = empty cell): fills empty cells with the
+// start of the next non-empty one.  One block; cells is a power of two.
+__global__ void __launch_bounds__(1024) top_fill_kernel(int32_t *__restrict__ top, int cells, int n)
+{
+    __shared__ int32_t part[1024];
+    const int per = cells / 1024;
+    const int b = threadIdx.x * per;
+    int32_t m = n;
+    for (int p = b + per - 1; p >= b; --p) {
+        const int32_t v = top[p];
+        if (v >= 0) m = min(m, v);
+    }
+    part[threadIdx.x] = m;
+    __syncthreads();
+    // suffix min over threads (inclusive), Hillis-Steele
+    for (int off = 1; off < 1024; off <<= 1) {
+        const int32_t t = threadIdx.x + off < 1024 ? part[threadIdx.x + off] : n;
+        __syncthreads();
+        part[threadIdx.x] = min(part[threadIdx.x], t);
+        __syncthreads();
+    }
+    int32_t run = threadIdx.x + 1 < 1024 ? part[threadIdx.x + 1] : n;
+    for (int p = b + per - 1; p >= b; --p) {
+        const int32_t v = top[p];
+        if (v >= 0) run = min(run, v);
+        top[p] = run;
+    }
+    if (threadIdx.x == 0) top[cells] = n;
+}
+
+// Child ranges of a node at `level` covering [b, e): bounds[c] = first sorted
+// index in [b, e) whose digit at `shift` is >= c; bounds[nchild] = e.
+__device__ __forceinline__ void child_bounds(const uint64_t *__restrict__ keys, int b, int e,
+                                             int shift, int nchild, int *bounds,
+                                             const int32_t *__restrict__ top, int level, int D,
+                                             int bits)
+{
+    const int K = top_levels(nchild);
+    if (level < K) {
+        const uint64_t prefix = keys[b] >> (bits * (D - level));
+        for (int c = 0; c < nchild; ++c)
+            bounds[c] = top[((prefix << bits) | (uint64_t)c) << (bits * (K - level - 1))];
+        bounds[0] = b;
+        bounds[nchild] = e;
+        return;
+    }
     const uint32_t mask = nchild - 1;
     bounds[0] = b;
     for (int c = 1; c < nchild; ++c) {
@@ -397,12 +453,13 @@ __device__ __forceinline__ bool node_splits(const uint64_t *__restrict__ keys, i
 }
 
 __device__ int node_child_count(const uint64_t *__restrict__ keys, const NodeArrays &nd, int node,
-                                int leaf, int level, int D, int bits, int nchild)
+                                int leaf, int level, int D, int bits, int nchild,
+                                const int32_t *__restrict__ top)
 {
     const int b = nd.begin[node], cnt = nd.count[node];
     if (!node_splits(keys, b, cnt, leaf, level, D)) return 0;
     int bounds[9];
-    child_bounds(keys, b, b + cnt, bits * (D - level - 1), nchild, bounds);
+    child_bounds(keys, b, b + cnt, bits * (D - level - 1), nchild, bounds, top, level, D, bits);
     int k = 0;
     for (int c = 0; c < nchild; ++c) k += bounds[c + 1] > bounds[c];
     return k;
@@ -415,7 +472,7 @@ __device__ int node_child_count(const uint64_t *__restrict__ keys, const NodeArr
 // leaves: exact, slower) if the node arrays would overflow.
 __global__ void __launch_bounds__(kBuildThreads)
 level_count_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, LevelInfo *lv, int level,
-                   int leaf, int nchild, int32_t *__restrict__ bsum,
+                   int leaf, int nchild, const int32_t *__restrict__ top, int32_t *__restrict__ bsum,
                    unsigned int *__restrict__ ticket, uint32_t *__restrict__ flags)
 {
     const int D = tree_levels(nchild), bits = level_bits(nchild);
@@ -431,7 +488,7 @@ level_count_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, LevelInfo *
     const int cb = blockIdx.x * chunk, ce = min(cb + chunk, cnt);
     int s = 0;
     for (int k = cb + threadIdx.x; k < ce; k += blockDim.x)
-        s += node_child_count(keys, nd, first + k, leaf, level, D, bits, nchild);
+        s += node_child_count(keys, nd, first + k, leaf, level, D, bits, nchild, top);
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     __shared__ int ws[kBuildThreads / 32];
     __shared__ bool last;
@@ -468,7 +525,8 @@ level_count_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, LevelInfo *
 // produced.
 __global__ void __launch_bounds__(kBuildThreads)
 level_write_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, const LevelInfo *__restrict__ lv,
-                   int level, int leaf, int nchild, const int32_t *__restrict__ boff)
+                   int level, int leaf, int nchild, const int32_t *__restrict__ top,
+                   const int32_t *__restrict__ boff)
 {
     const int D = tree_levels(nchild), bits = level_bits(nchild);
     const int cnt = lv->count[level], first = lv->begin[level];
@@ -491,7 +549,8 @@ level_write_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, const Level
             const int b = nd.begin[node], c = nd.count[node];
             split = node_splits(keys, b, c, leaf, level, D);
             if (split) {
-                child_bounds(keys, b, b + c, bits * (D - level - 1), nchild, bounds);
+                child_bounds(keys, b, b + c, bits * (D - level - 1), nchild, bounds, top, level, D,
+                             bits);
                 for (int q = 0; q < nchild; ++q) nc += bounds[q + 1] > bounds[q];
             }
         }
@@ -571,19 +630,33 @@ moment_partial_kernel(const double *__restrict__ spos, const double *__restrict_
     if (threadIdx.x < 4) bsum[threadIdx.x * gridDim.x + blockIdx.x] = red[threadIdx.x][0];
 }
 
-__global__ void moment_blockscan_kernel(double *__restrict__ bsum, int nblocks)
+// Exclusive scan of the per-block sums, one warp per component.
+__global__ void __launch_bounds__(128) moment_blockscan_kernel(double *__restrict__ bsum, int nblocks)
 {
-    // 4 sequential exclusive scans of nblocks values (nblocks <= a few thousand)
-    const int c = threadIdx.x;
-    if (c >= 4) return;
-    double run = 0.0;
-    for (int b = 0; b < nblocks; ++b) {
-        double t = bsum[c * nblocks + b];
-        bsum[c * nblocks + b] = run;
+    const int c = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double *v = bsum + (size_t)c * nblocks;
+    const int per = (nblocks + 31) / 32;
+    const int b = lane * per, e = min(b + per, nblocks);
+    double s = 0.0;
+    for (int k = b; k < e; ++k) s += v[k];
+    double incl = s;
+    for (int o = 1; o < 32; o <<= 1) {
+        const double t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    double run = incl - s;
+    for (int k = b; k < e; ++k) {
+        const double t = v[k];
+        v[k] = run;
         run += t;
     }
 }
 
+constexpr int kMomItems = 4;
+
+// Exclusive prefix sums pref[c][k] of (m, m x, m y, m z) over the sorted
+// bodies.  Block b covers a contiguous chunk starting from its block offset;
+// each thread takes kMomItems consecutive bodies per tile.
 __global__ void __launch_bounds__(kMomThreads)
 moment_scan_kernel(const double *__restrict__ spos, const double *__restrict__ smass, int n,
                    const double *__restrict__ boff, double *__restrict__ pref)
@@ -596,37 +669,59 @@ moment_scan_kernel(const double *__restrict__ spos, const double *__restrict__ s
     if (threadIdx.x < 4) carry[threadIdx.x] = boff[threadIdx.x * gridDim.x + blockIdx.x];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int k0 = cb; k0 < ce; k0 += blockDim.x) {
-        const int k = k0 + threadIdx.x;
-        double v[4] = {0, 0, 0, 0};
-        if (k < ce) {
-            const double m = smass[k];
-            v[0] = m;
-            v[1] = m * spos[k];
-            v[2] = m * spos[n + k];
-            v[3] = m * spos[2 * (size_t)n + k];
+    constexpr int kTile = kMomThreads * kMomItems;
+    for (int t0 = cb; t0 < ce; t0 += kTile) {
+        const int k0 = t0 + threadIdx.x * kMomItems;
+        double v[kMomItems][4];
+        double tot[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int j = 0; j < kMomItems; ++j) {
+            const int k = k0 + j;
+            double m = 0.0, px = 0.0, py = 0.0, pz = 0.0;
+            if (k < ce) {
+                m = smass[k];
+                px = spos[k];
+                py = spos[n + k];
+                pz = spos[2 * (size_t)n + k];
+            }
+            v[j][0] = m;
+            v[j][1] = m * px;
+            v[j][2] = m * py;
+            v[j][3] = m * pz;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) tot[c] += v[j][c];
         }
         double incl[4];
+#pragma unroll
         for (int c = 0; c < 4; ++c) {
-            incl[c] = v[c];
+            incl[c] = tot[c];
             for (int o = 1; o < 32; o <<= 1) {
-                double t = __shfl_up_sync(0xffffffffu, incl[c], o);
+                const double t = __shfl_up_sync(0xffffffffu, incl[c], o);
                 if (lane >= o) incl[c] += t;
             }
             if (lane == 31) ws[c][warp] = incl[c];
         }
         __syncthreads();
-        double excl[4];
+        double run[4];
+#pragma unroll
         for (int c = 0; c < 4; ++c) {
             double wb = 0.0;
             for (int w = 0; w < warp; ++w) wb += ws[c][w];
-            excl[c] = carry[c] + wb + incl[c] - v[c];
+            run[c] = carry[c] + wb + incl[c] - tot[c];
         }
         __syncthreads();
-        if (k < ce)
-            for (int c = 0; c < 4; ++c) pref[c * stride + k] = excl[c];
-        if (threadIdx.x == blockDim.x - 1)
-            for (int c = 0; c < 4; ++c) carry[c] = excl[c] + v[c];
+#pragma unroll
+        for (int j = 0; j < kMomItems; ++j) {
+            const int k = k0 + j;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (k < ce) pref[c * stride + k] = run[c];
+                run[c] += v[j][c];
+            }
+        }
+        if (threadIdx.x == kMomThreads - 1)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) carry[c] = run[c];
         __syncthreads();
     }
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
@@ -878,7 +973,11 @@ traverse_warp_kernel(TravArgs a_in)
         lo_z = fminf(lo_z, __shfl_xor_sync(0xffffffffu, lo_z, o));
         hi_z = fmaxf(hi_z, __shfl_xor_sync(0xffffffffu, hi_z, o));
     }
-    const float slack = 6.0e-7f * a.extent;
+    // largest coordinate magnitude in the box: bounds the f32 rounding of the
+    // warp's positions
+    const float bmax = fmaxf(fmaxf(fmaxf(fabsf(lo_x), fabsf(hi_x)), fmaxf(fabsf(lo_y), fabsf(hi_y))),
+                             fmaxf(fabsf(lo_z), fabsf(hi_z)));
+    const float pmax = fmaxf(fmaxf(fabsf(q.x), fabsf(q.y)), fabsf(q.z));
     const float theta = a.theta;
     float ax = 0.f, ay = 0.f, az = 0.f, hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
     unsigned long long visits = 0, pairs = 0;
@@ -913,14 +1012,20 @@ traverse_warp_kernel(TravArgs a_in)
         sp -= m;
         visits += m;
         int qref = 0, qcnt = 0, nchild = 0, first_child = 0;
+        float4 geo = make_float4(0.f, 0.f, 0.f, 0.f);
+        bool acc = false, maybe = false;
         if (lane < m) {
-            const float4 geo = a.nd.geo[cell];
+            geo = a.nd.geo[cell];
             const int4 meta = a.nd.meta[cell];
+            const float cmax = fmaxf(fmaxf(fabsf(geo.x), fabsf(geo.y)), fabsf(geo.z));
             const float dx = fmaxf(fmaxf(lo_x - geo.x, geo.x - hi_x), 0.f);
             const float dy = fmaxf(fmaxf(lo_y - geo.y, geo.y - hi_y), 0.f);
             const float dz = fmaxf(fmaxf(lo_z - geo.z, geo.z - hi_z), 0.f);
-            const float rmin = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - slack;
-            const bool acc = theta > 0.f && rmin > 0.f && geo.w * (1.f + 2e-6f) < theta * rmin;
+            const float r = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+            // f32 rounding of positions and centre moves r by at most
+            // 1.1e-7 (|p| + |c|) + 3.5e-7 r against the reference's f64 value
+            const float rmin = r - (2e-7f * (bmax + cmax) + 5e-7f * r);
+            acc = theta > 0.f && rmin > 0.f && geo.w * (1.f + 2e-6f) < theta * rmin;
             if (acc) {
                 qref = -cell - 1;
                 qcnt = 1;
@@ -930,6 +1035,29 @@ traverse_warp_kernel(TravArgs a_in)
             } else {
                 nchild = (int)((uint32_t)meta.x >> 28);
                 first_child = meta.y;
+                maybe = theta > 0.f;
+            }
+        }
+        // Internal cells the box test rejects: accept them if every body of
+        // the warp passes its own test (with the same rounding margin).
+        uint32_t pend = __ballot_sync(0xffffffffu, maybe);
+        while (pend) {
+            const int src = __ffs(pend) - 1;
+            pend &= pend - 1;
+            const float gx = __shfl_sync(0xffffffffu, geo.x, src);
+            const float gy = __shfl_sync(0xffffffffu, geo.y, src);
+            const float gz = __shfl_sync(0xffffffffu, geo.z, src);
+            const float gw = __shfl_sync(0xffffffffu, geo.w, src);
+            const float ddx = q.x - gx, ddy = q.y - gy, ddz = q.z - gz;
+            const float r2 = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz));
+            const float r = r2 * rsqrt_approx(r2);
+            const float cm = fmaxf(fmaxf(fabsf(gx), fabsf(gy)), fabsf(gz));
+            const float rl = r - (2e-7f * (pmax + cm) + 5e-7f * r);
+            const bool ok = !valid || (rl > 0.f && gw * (1.f + 2e-6f) < theta * rl);
+            if (__all_sync(0xffffffffu, ok) && lane == src) {
+                qref = -cell - 1;
+                qcnt = 1;
+                nchild = 0;
             }
         }
         // push the children of opened cells
@@ -997,6 +1125,7 @@ struct BhWorkspace {
     unsigned long long *extent_bits = nullptr;
     unsigned long long *stats = nullptr;  // node visits, pair interactions of the last traversal
     unsigned int *ticket = nullptr;       // last-block ticket of level_count_kernel (kept at 0)
+    int32_t *top = nullptr;               // cell starts of the top tree level (see top_levels)
     uint32_t *flags = nullptr;
     int launches = 0;
     // which key/val buffer holds the sorted result
@@ -1013,7 +1142,8 @@ static void ws_release(BhWorkspace *ws)
                  ws->sbody,    ws->spos,      ws->smass,         ws->pref,        ws->mom_bsum,
                  ws->nd.begin, ws->nd.count,  ws->nd.child,      ws->nd.nchild,   ws->nd.level,
                  ws->nd.c64,   ws->nd.geo,    ws->nd.com,        ws->lv,          ws->bsum,
-                 ws->extent_bits, ws->flags, ws->nd.meta, ws->stats, ws->ticket};
+                 ws->extent_bits, ws->flags, ws->nd.meta, ws->stats, ws->ticket,
+                 ws->top};
     for (void *q : p)
         if (q) cudaFree(q);
 }
@@ -1071,6 +1201,7 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device)
     PG_WA(w->nd.meta, ncap);
     PG_WA(w->stats, 4);
     PG_WA(w->ticket, 1);
+    PG_WA(w->top, (size_t)(1 << 15) + 1);
     PG_WA(w->lv, 1);
     PG_WA(w->bsum, (size_t)w->grid_build);
     PG_WA(w->extent_bits, 1);
@@ -1160,17 +1291,24 @@ static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, c
     root_kernel<<<1, 32, 0, st>>>(ws->nd, ws->lv, n, ws->extent_bits);
     launches += 2;
     const int D = tree_levels(p.nchild);
+    const int K = top_levels(p.nchild);
+    const int top_cells = 1 << (level_bits(p.nchild) * K);
+    PG_CUDA(cudaMemsetAsync(ws->top, 0xff, top_cells * sizeof(int32_t), st));
+    top_mark_kernel<<<cdiv(n, 256), 256, 0, st>>>(ws->keys[cur], n, level_bits(p.nchild) * (D - K),
+                                                  ws->top);
+    top_fill_kernel<<<1, 1024, 0, st>>>(ws->top, top_cells, n);
+    launches += 2;
     for (int level = 0; level < D; ++level) {
         level_count_kernel<<<ws->grid_build, kBuildThreads, 0, st>>>(
-            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->bsum, ws->ticket,
-            ws->flags);
+            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->top, ws->bsum,
+            ws->ticket, ws->flags);
         level_write_kernel<<<ws->grid_build, kBuildThreads, 0, st>>>(
-            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->bsum);
+            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->top, ws->bsum);
         launches += 2;
     }
     moment_partial_kernel<<<ws->grid_mom, kMomThreads, 0, st>>>(ws->spos, ws->smass, n,
                                                                 ws->mom_bsum);
-    moment_blockscan_kernel<<<1, 32, 0, st>>>(ws->mom_bsum, ws->grid_mom);
+    moment_blockscan_kernel<<<1, 128, 0, st>>>(ws->mom_bsum, ws->grid_mom);
     moment_scan_kernel<<<ws->grid_mom, kMomThreads, 0, st>>>(ws->spos, ws->smass, n, ws->mom_bsum,
                                                              ws->pref);
     node_finish_kernel<<<sms * 4, 256, 0, st>>>(ws->nd, ws->lv, ws->pref, n, ws->sbody, ws->spos);
