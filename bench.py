@@ -57,7 +57,9 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--skip-e2e", action="store_true", help="profiling runs: device path only")
-    p.add_argument("--only", default="", help="comma list of parts: direct, bh")
+    p.add_argument("--only", default="", help="comma list of parts: direct, bh, ensemble")
+    p.add_argument("--ens-steps", type=int, default=200)
+    p.add_argument("--ens-members", type=int, default=512)
     p.add_argument("--bh-steps", type=int, default=1000)
     p.add_argument("--bh-e2e-steps", type=int, default=5)
     p.add_argument("--bodies", type=int, default=N_CUBE,
@@ -473,15 +475,88 @@ def measure_bh(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict:
     return out
 
 
+def ensemble_states(count: int = 512, seed: int = 3):
+    """The batched uneven workload: N_k log-uniform in [256, 65536] (seed 3);
+    even members a uniform cube U[-0.5,0.5]^3, odd members a Plummer sphere."""
+    from physim_gb300 import ics
+    sizes = ics.ensemble_sizes(count, seed=seed)
+    states = []
+    for k, n in enumerate(sizes):
+        if k % 2 == 0:
+            states.append(ics.cube_with_stars(int(n), seed=10_000 + k))
+        else:
+            states.append(ics.plummer(int(n), seed=20_000 + k, a=0.1))
+    return states
+
+
+def measure_ensemble(args, dist: Dist, device: int) -> dict:
+    import torch
+
+    import physim_gb300 as pg
+
+    states = ensemble_states(args.ens_members)
+    sizes = [len(s) for s in states]
+    pairs = sum(n * (n - 1) for n in sizes)
+    stream = torch.cuda.Stream(device=device)
+    cfg = pg.SimConfig(gravity="simple_astro", e=E, dt=DT, device=device,
+                       stream=stream.cuda_stream)
+    ens = pg.Ensemble(states, cfg)
+    t0 = time.perf_counter()
+    plan = ens.autotune()
+    tune_s = time.perf_counter() - t0
+    with torch.cuda.stream(stream):
+        ens.step(max(args.warmup, 3))
+    ens.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    with torch.cuda.stream(stream):
+        a.record(stream)
+        ens.step(args.ens_steps)
+        b.record(stream)
+    torch.cuda.synchronize()
+    ens_ms = dist.max(a.elapsed_time(b))
+    launches = ens.launches_per_step * args.ens_steps
+    ens.close()
+
+    # the same members one at a time through the per-simulation path
+    sims = [pg.Simulation(s, pg.SimConfig(gravity="simple_astro", e=E, dt=DT, device=device))
+            for s in states]
+    for sim in sims:
+        sim.step(1)
+        sim.synchronize()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for sim in sims:
+        sim.step(args.ens_steps)
+        sim.synchronize()
+    plain_s = dist.max(time.perf_counter() - t0)
+    for sim in sims:
+        sim.close()
+    member_steps = len(states) * args.ens_steps
+    ens_rate = dist.sum(float(member_steps)) / (ens_ms / 1e3)
+    plain_rate = dist.sum(float(member_steps)) / plain_s
+    return {"metric": "aggregate member-steps/s, 512-member uneven ensemble (direct sum)",
+            "value": ens_rate, "unit": "member-steps/s", "members": len(states),
+            "bodies_total": int(sum(sizes)), "pairs_per_step": pairs,
+            "steps": args.ens_steps, "ms_per_step": ens_ms / args.ens_steps,
+            "gpair_per_s": pairs * args.ens_steps / (ens_ms / 1e3) / 1e9,
+            "plan": plan, "autotune_s": tune_s, "gpu_launches": launches,
+            "plain_one_at_a_time": {"value": plain_rate, "unit": "member-steps/s",
+                                    "seconds": plain_s,
+                                    "path": "physim_gpu_sim_step per member, members in turn"},
+            "speedup_vs_plain": ens_rate / plain_rate}
+
+
 def run_ours(args, dist: Dist):
     device, sms = _device_context(dist)
     peaks = measured_peaks()
-    parts = args.only.split(",") if args.only else ["direct", "bh"]
+    parts = args.only.split(",") if args.only else ["direct", "bh", "ensemble"]
     direct = measure_direct(args, dist, device, sms, peaks) if "direct" in parts else None
     bh = measure_bh(args, dist, device, sms, peaks) if "bh" in parts else None
+    ens = measure_ensemble(args, dist, device) if "ensemble" in parts else None
     if dist.rank != 0:
         return
-    base = direct if direct else bh
+    base = direct if direct else (bh if bh else ens)
     line = {
         "metric": METRIC if direct else bh["metric"],
         "value": base["value"],
@@ -500,6 +575,12 @@ def run_ours(args, dist: Dist):
         for k in ("roofline", "e2e", "gpu_launches", "cpu_baseline", "clocks"):
             if k in direct:
                 line[k] = direct[k]
+    if ens:
+        line["ensemble"] = ens
+        if not direct and not bh:
+            line["metric"] = ens["metric"]
+            line["unit"] = ens["unit"]
+            line["gpu_launches"] = ens["gpu_launches"]
     if bh:
         line["bh"] = bh
         if not direct:

@@ -284,6 +284,46 @@ int physim_gpu_sim_tree_snapshot(PhysimSim *sim, PhysimTreeSnapshot *out);
 int physim_gpu_sim_bh_stats(PhysimSim *sim, uint64_t *node_visits, uint64_t *interactions,
                             double *traversal_ms);
 
+/* ----------------------------------------------------------------------- */
+/* Batched ensembles: many independent simple_astro + verlet simulations of  */
+/* uneven size, advanced together by one persistent pair kernel per step    */
+/* (a work queue of (member, i tile, j chunk) units), captured in a graph.   */
+/* ----------------------------------------------------------------------- */
+typedef struct PhysimEnsemble PhysimEnsemble;
+
+typedef struct PhysimEnsembleTuning {
+    uint32_t block;        /* threads per block of the pair kernel */
+    uint32_t ipt;          /* bodies per thread */
+    uint32_t chunk_bodies; /* j bodies per work unit */
+    uint32_t candidates;   /* plans timed */
+    double force_ms;       /* time of one pair-kernel pass with the chosen plan */
+} PhysimEnsembleTuning;
+
+/* Members 0..count-1 hold sizes[k] bodies each.  cfg supplies the device,
+ * stream, compensated flag and the default e and dt (gravity must be
+ * simple_astro).  Members take no steps until they are uploaded. */
+int physim_gpu_ensemble_create(const PhysimSimConfig *cfg, const size_t *sizes, size_t count,
+                               PhysimEnsemble **out);
+/* Copies a member's state in; its next step is the Taylor first step and it
+ * steps without limit until set_member says otherwise. */
+int physim_gpu_ensemble_upload(PhysimEnsemble *ens, size_t index, const Entity *state, size_t n);
+/* Per-member easing factor, time step and number of steps still to take
+ * (UINT64_MAX: unlimited; 0: the member is skipped by the kernels). */
+int physim_gpu_ensemble_set_member(PhysimEnsemble *ens, size_t index, double e, double dt,
+                                   uint64_t steps_remaining);
+/* Times every candidate kernel shape and j-chunk length on the members' data
+ * (force passes only; the state is not advanced) and keeps the fastest. */
+int physim_gpu_ensemble_autotune(PhysimEnsemble *ens, PhysimEnsembleTuning *out);
+/* Enqueues `steps` steps of every member with steps left (asynchronous). */
+int physim_gpu_ensemble_step(PhysimEnsemble *ens, uint32_t steps);
+int physim_gpu_ensemble_download(PhysimEnsemble *ens, size_t index, Entity *state, size_t n);
+/* Waits, then copies per-member steps taken / steps remaining (either may be NULL). */
+int physim_gpu_ensemble_progress(PhysimEnsemble *ens, uint64_t *steps_done, uint64_t *remaining);
+int physim_gpu_ensemble_synchronize(PhysimEnsemble *ens);
+void *physim_gpu_ensemble_stream(PhysimEnsemble *ens);
+int physim_gpu_ensemble_launches_per_step(PhysimEnsemble *ens);
+void physim_gpu_ensemble_destroy(PhysimEnsemble *ens);
+
 /* Verlet integrator over host arrays (integrators/src/verlet.rs:19-121).
  * A Rust IntegratorElement shim evaluates acc_fn itself and hands the
  * accelerations over; the step runs on the GPU in f64 in the reference's

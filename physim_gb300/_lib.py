@@ -68,6 +68,11 @@ class PhysimTreeSnapshot(C.Structure):
                 ("extent", C.c_double), ("flags", C.c_uint32)]
 
 
+class PhysimEnsembleTuning(C.Structure):
+    _fields_ = [("block", C.c_uint32), ("ipt", C.c_uint32), ("chunk_bodies", C.c_uint32),
+                ("candidates", C.c_uint32), ("force_ms", C.c_double)]
+
+
 ELEMENTS = ("astro", "astro2", "simple_astro")
 ELEMENT_SUFFIXES = ("get_api", "register", "init", "transform", "destroy",
                     "get_property_descriptions", "recv_message", "post_configuration_messages")
@@ -100,6 +105,18 @@ def _load() -> C.CDLL:
         "physim_gpu_sim_tree_snapshot": (C.c_int, [vp, C.POINTER(PhysimTreeSnapshot)]),
         "physim_gpu_sim_bh_stats": (C.c_int, [vp, C.POINTER(C.c_uint64),
                                               C.POINTER(C.c_uint64), C.POINTER(dbl)]),
+        "physim_gpu_ensemble_create": (C.c_int, [C.POINTER(PhysimSimConfig), vp, sz,
+                                                 C.POINTER(vp)]),
+        "physim_gpu_ensemble_upload": (C.c_int, [vp, sz, vp, sz]),
+        "physim_gpu_ensemble_set_member": (C.c_int, [vp, sz, dbl, dbl, C.c_uint64]),
+        "physim_gpu_ensemble_autotune": (C.c_int, [vp, C.POINTER(PhysimEnsembleTuning)]),
+        "physim_gpu_ensemble_step": (C.c_int, [vp, u32]),
+        "physim_gpu_ensemble_download": (C.c_int, [vp, sz, vp, sz]),
+        "physim_gpu_ensemble_progress": (C.c_int, [vp, vp, vp]),
+        "physim_gpu_ensemble_synchronize": (C.c_int, [vp]),
+        "physim_gpu_ensemble_stream": (vp, [vp]),
+        "physim_gpu_ensemble_launches_per_step": (C.c_int, [vp]),
+        "physim_gpu_ensemble_destroy": (None, [vp]),
         "physim_gpu_verlet_create": (C.c_int, [i32, C.POINTER(vp)]),
         "physim_gpu_verlet_integrate": (C.c_int, [vp, vp, vp, sz, vp, dbl]),
         "physim_gpu_verlet_destroy": (None, [vp]),

@@ -384,34 +384,53 @@ __global__ void top_mark_kernel(const uint64_t *__restrict__ keys, int n, int sh
     if (k == 0 || (keys[k - 1] >> shift) != p) top[p] = k;
 }
 
-// Suffix minimum over the marks (-1 = empty cell): fills empty cells with the
-// start of the next non-empty one.  One block; cells is a power of two.
-__global__ void __launch_bounds__(1024) top_fill_kernel(int32_t *__restrict__ top, int cells, int n)
+// Suffix minimum over the marks (-1 = empty cell) fills empty cells with the
+// start of the next non-empty one.  Two passes over blocks of 1024 cells
+// (cells is a power of two >= 1024): per-block minima, then per-block
+// suffix minima plus the minimum of all later blocks.
+__device__ __forceinline__ int32_t mark_value(int32_t v, int n) { return v >= 0 ? v : n; }
+
+__global__ void __launch_bounds__(1024) top_blockmin_kernel(const int32_t *__restrict__ top, int n,
+                                                            int32_t *__restrict__ blockmin)
 {
-    __shared__ int32_t part[1024];
-    const int per = cells / 1024;
-    const int b = threadIdx.x * per;
-    int32_t m = n;
-    for (int p = b + per - 1; p >= b; --p) {
-        const int32_t v = top[p];
-        if (v >= 0) m = min(m, v);
-    }
-    part[threadIdx.x] = m;
+    __shared__ int32_t wm[32];
+    int32_t m = mark_value(top[blockIdx.x * 1024 + threadIdx.x], n);
+    for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
     __syncthreads();
-    // suffix min over threads (inclusive), Hillis-Steele
-    for (int off = 1; off < 1024; off <<= 1) {
-        const int32_t t = threadIdx.x + off < 1024 ? part[threadIdx.x + off] : n;
-        __syncthreads();
-        part[threadIdx.x] = min(part[threadIdx.x], t);
-        __syncthreads();
+    if (threadIdx.x < 32) {
+        m = wm[threadIdx.x];
+        for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) blockmin[blockIdx.x] = m;
     }
-    int32_t run = threadIdx.x + 1 < 1024 ? part[threadIdx.x + 1] : n;
-    for (int p = b + per - 1; p >= b; --p) {
-        const int32_t v = top[p];
-        if (v >= 0) run = min(run, v);
-        top[p] = run;
+}
+
+__global__ void __launch_bounds__(1024) top_fill_kernel(int32_t *__restrict__ top, int cells, int n,
+                                                        const int32_t *__restrict__ blockmin)
+{
+    __shared__ int32_t wm[32];
+    __shared__ int32_t later;
+    const int nb = cells / 1024;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp == 0) {
+        int32_t m = n;
+        for (int b = (int)blockIdx.x + 1 + lane; b < nb; b += 32) m = min(m, blockmin[b]);
+        for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) later = m;
     }
-    if (threadIdx.x == 0) top[cells] = n;
+    const int p = blockIdx.x * 1024 + threadIdx.x;
+    int32_t v = mark_value(top[p], n);
+    // inclusive suffix min within the warp
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t t = __shfl_down_sync(0xffffffffu, v, o);
+        if (lane + o < 32) v = min(v, t);
+    }
+    if (lane == 0) wm[warp] = v;  // minimum of the whole warp
+    __syncthreads();
+    int32_t r = later;
+    for (int w = warp + 1; w < 32; ++w) r = min(r, wm[w]);
+    top[p] = min(v, r);
+    if (blockIdx.x == 0 && threadIdx.x == 0) top[cells] = n;
 }
 
 // Child ranges of a node at `level` covering [b, e): bounds[c] = first sorted
@@ -1126,6 +1145,7 @@ struct BhWorkspace {
     unsigned long long *stats = nullptr;  // node visits, pair interactions of the last traversal
     unsigned int *ticket = nullptr;       // last-block ticket of level_count_kernel (kept at 0)
     int32_t *top = nullptr;               // cell starts of the top tree level (see top_levels)
+    int32_t *top_blockmin = nullptr;      // per-1024-cell minima while filling `top`
     uint32_t *flags = nullptr;
     int launches = 0;
     // which key/val buffer holds the sorted result
@@ -1143,7 +1163,7 @@ static void ws_release(BhWorkspace *ws)
                  ws->nd.begin, ws->nd.count,  ws->nd.child,      ws->nd.nchild,   ws->nd.level,
                  ws->nd.c64,   ws->nd.geo,    ws->nd.com,        ws->lv,          ws->bsum,
                  ws->extent_bits, ws->flags, ws->nd.meta, ws->stats, ws->ticket,
-                 ws->top};
+                 ws->top, ws->top_blockmin};
     for (void *q : p)
         if (q) cudaFree(q);
 }
@@ -1202,6 +1222,7 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device)
     PG_WA(w->stats, 4);
     PG_WA(w->ticket, 1);
     PG_WA(w->top, (size_t)(1 << 15) + 1);
+    PG_WA(w->top_blockmin, 32);
     PG_WA(w->lv, 1);
     PG_WA(w->bsum, (size_t)w->grid_build);
     PG_WA(w->extent_bits, 1);
@@ -1296,8 +1317,9 @@ static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, c
     PG_CUDA(cudaMemsetAsync(ws->top, 0xff, top_cells * sizeof(int32_t), st));
     top_mark_kernel<<<cdiv(n, 256), 256, 0, st>>>(ws->keys[cur], n, level_bits(p.nchild) * (D - K),
                                                   ws->top);
-    top_fill_kernel<<<1, 1024, 0, st>>>(ws->top, top_cells, n);
-    launches += 2;
+    top_blockmin_kernel<<<top_cells / 1024, 1024, 0, st>>>(ws->top, n, ws->top_blockmin);
+    top_fill_kernel<<<top_cells / 1024, 1024, 0, st>>>(ws->top, top_cells, n, ws->top_blockmin);
+    launches += 3;
     for (int level = 0; level < D; ++level) {
         level_count_kernel<<<ws->grid_build, kBuildThreads, 0, st>>>(
             ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->top, ws->bsum,

@@ -21,6 +21,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "direct_tile.cuh"
 #include "engine.h"
 
 namespace pg {
@@ -32,109 +33,12 @@ __global__ void __launch_bounds__(BLOCK, 2)
 direct_forces_kernel(const float4 *__restrict__ body, int n, int n_jtiles, int chunk_tiles, float e,
                      double *__restrict__ partial)
 {
-    static_assert(IPT % 2 == 0, "bodies per thread must be even (packed pairs)");
-    constexpr int P = IPT / 2;
     __shared__ float4 tile[2][BLOCK][2];
-
-    const int tid = threadIdx.x;
-    const int i_base = blockIdx.x * BLOCK * IPT;
     const int split = blockIdx.y;
     const int t0 = split * chunk_tiles;
     const int t1 = min(t0 + chunk_tiles, n_jtiles);
-
-    float2 nx[P], ny[P], nz[P];
-    float2 ax[P], ay[P], az[P];
-    float2 hx[P], hy[P], hz[P], lx[P], ly[P], lz[P];
-#pragma unroll
-    for (int p = 0; p < P; ++p) {
-        // bodies i_base + tid + k*BLOCK, k = 2p, 2p+1 (rows padded, always readable)
-        float4 b0 = body[i_base + tid + (2 * p) * BLOCK];
-        float4 b1 = body[i_base + tid + (2 * p + 1) * BLOCK];
-        nx[p] = make_float2(-b0.x, -b1.x);
-        ny[p] = make_float2(-b0.y, -b1.y);
-        nz[p] = make_float2(-b0.z, -b1.z);
-        ax[p] = ay[p] = az[p] = make_float2(0.f, 0.f);
-        hx[p] = hy[p] = hz[p] = make_float2(0.f, 0.f);
-        lx[p] = ly[p] = lz[p] = make_float2(0.f, 0.f);
-    }
-    const float2 e2 = make_float2(e, e);
-    const float2 g2 = make_float2(kPairGuard, kPairGuard);
-
-    if (t0 < t1) {
-        float4 nxt = body[t0 * BLOCK + tid];
-        for (int t = t0; t < t1; ++t) {
-            const int buf = (t - t0) & 1;
-            tile[buf][tid][0] = make_float4(nxt.x, nxt.x, nxt.y, nxt.y);
-            tile[buf][tid][1] = make_float4(nxt.z, nxt.z, nxt.w, nxt.w);
-            __syncthreads();
-            if (t + 1 < t1) nxt = body[(t + 1) * BLOCK + tid];
-#pragma unroll 4
-            for (int j = 0; j < BLOCK; ++j) {
-                const float4 A = tile[buf][j][0];
-                const float4 B = tile[buf][j][1];
-                const float2 xj = make_float2(A.x, A.y);
-                const float2 yj = make_float2(A.z, A.w);
-                const float2 zj = make_float2(B.x, B.y);
-                const float2 mj = make_float2(B.z, B.w);
-#pragma unroll
-                for (int p = 0; p < P; ++p) {
-                    const float2 dx = add2(xj, nx[p]);
-                    const float2 dy = add2(yj, ny[p]);
-                    const float2 dz = add2(zj, nz[p]);
-                    float2 r2 = mul2(dz, dz);
-                    r2 = fma2(dy, dy, r2);
-                    r2 = fma2(dx, dx, r2);
-                    const float2 w = add2(r2, e2);
-                    const float2 ww = mul2(w, w);
-                    const float2 q = fma2(r2, ww, g2);
-                    const float2 inv = make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y));
-                    const float2 s = mul2(mj, inv);
-                    ax[p] = fma2(dx, s, ax[p]);
-                    ay[p] = fma2(dy, s, ay[p]);
-                    az[p] = fma2(dz, s, az[p]);
-                }
-            }
-            if (COMP) {
-#pragma unroll
-                for (int p = 0; p < P; ++p) {
-                    float s, err;
-                    two_sum(hx[p].x, ax[p].x, s, err); hx[p].x = s; lx[p].x += err;
-                    two_sum(hx[p].y, ax[p].y, s, err); hx[p].y = s; lx[p].y += err;
-                    two_sum(hy[p].x, ay[p].x, s, err); hy[p].x = s; ly[p].x += err;
-                    two_sum(hy[p].y, ay[p].y, s, err); hy[p].y = s; ly[p].y += err;
-                    two_sum(hz[p].x, az[p].x, s, err); hz[p].x = s; lz[p].x += err;
-                    two_sum(hz[p].y, az[p].y, s, err); hz[p].y = s; lz[p].y += err;
-                    ax[p] = ay[p] = az[p] = make_float2(0.f, 0.f);
-                }
-            }
-        }
-    }
-    if (!COMP) {
-#pragma unroll
-        for (int p = 0; p < P; ++p) {
-            hx[p] = ax[p];
-            hy[p] = ay[p];
-            hz[p] = az[p];
-        }
-    }
-    double *px = partial + (size_t)(split * 3 + 0) * n;
-    double *py = partial + (size_t)(split * 3 + 1) * n;
-    double *pz = partial + (size_t)(split * 3 + 2) * n;
-#pragma unroll
-    for (int p = 0; p < P; ++p) {
-        const int i0 = i_base + tid + (2 * p) * BLOCK;
-        const int i1 = i0 + BLOCK;
-        if (i0 < n) {
-            px[i0] = (double)hx[p].x + (double)lx[p].x;
-            py[i0] = (double)hy[p].x + (double)ly[p].x;
-            pz[i0] = (double)hz[p].x + (double)lz[p].x;
-        }
-        if (i1 < n) {
-            px[i1] = (double)hx[p].y + (double)lx[p].y;
-            py[i1] = (double)hy[p].y + (double)ly[p].y;
-            pz[i1] = (double)hz[p].y + (double)lz[p].y;
-        }
-    }
+    direct_tile<BLOCK, IPT, COMP>(body, n, blockIdx.x * BLOCK * IPT, t0, t1, e,
+                                  partial + (size_t)split * 3 * n, tile);
 }
 
 struct Shape {

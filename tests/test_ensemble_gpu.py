@@ -1,0 +1,109 @@
+"""Batched ensembles (physim_gpu_ensemble_*): every member's trajectory equals
+its solo run (the same pair arithmetic, partial sums split differently: FP32
+rounding only, relative L2 error below 1e-6 after 20 steps) and the oracle's
+(below 1e-5), with per-member parameters and step budgets."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _members():
+    from physim_gb300 import ics
+    sizes = [256, 300, 1000, 1025, 4096, 5000, 700, 2048, 257, 12345]
+    out = []
+    for k, n in enumerate(sizes):
+        if k % 2:
+            out.append(ics.plummer(n, seed=100 + k, a=0.1))
+        else:
+            out.append(ics.cube_with_stars(n, seed=100 + k))
+    return out
+
+
+def _solo(state, steps, e=0.01, dt=1e-5):
+    import physim_gb300 as pg
+    with pg.Simulation(state, pg.SimConfig(gravity="simple_astro", e=e, dt=dt)) as sim:
+        sim.step(steps)
+        return sim.download()
+
+
+def test_members_match_solo_runs():
+    import physim_gb300 as pg
+    from test_verlet_gpu import trajectory_errors
+    members = _members()
+    with pg.Ensemble(members, pg.SimConfig(gravity="simple_astro", e=0.01, dt=1e-5)) as ens:
+        ens.step(20)
+        got = [ens.download(k) for k in range(len(members))]
+        done, _ = ens.progress()
+    assert np.all(done == 20)
+    for k, s in enumerate(members):
+        err = trajectory_errors(s, got[k], _solo(s, 20))
+        assert err["pos_rel_l2"] < 1e-6 and err["vel_rel_l2"] < 1e-6, (k, err)
+
+
+def test_member_matches_oracle(oracle_mod):
+    import physim_gb300 as pg
+    from test_verlet_gpu import trajectory_errors
+    members = _members()[:4]
+    with pg.Ensemble(members, pg.SimConfig(gravity="simple_astro", e=0.01, dt=1e-5)) as ens:
+        ens.step(5)
+        got = ens.download(2)
+    want = oracle_mod.run_pipeline(members[2], "simple_astro", 5, 1e-5, 0.01)
+    err = trajectory_errors(members[2], got, want)
+    assert err["pos_rel_l2"] < 1e-5 and err["vel_rel_l2"] < 1e-5, err
+
+
+def test_budgets_and_parameters():
+    import physim_gb300 as pg
+    from test_verlet_gpu import trajectory_errors
+    members = _members()[:6]
+    params = [(0.01, 1e-5), (0.02, 2e-5), (0.01, 1e-5), (0.05, 1e-5), (0.01, 3e-5), (0.01, 1e-5)]
+    budgets = [5, 10, 3, 10, 0, 7]
+    cfg = pg.SimConfig(gravity="simple_astro", e=0.01, dt=1e-5)
+    with pg.Ensemble(members, cfg, steps=budgets, params=params) as ens:
+        ens.step(4)
+        ens.step(6)
+        done, rem = ens.progress()
+        got = [ens.download(k) for k in range(len(members))]
+    assert list(done) == [5, 10, 3, 10, 0, 7]
+    assert np.all(rem == 0)
+    for k, s in enumerate(members):
+        if budgets[k] == 0:
+            assert got[k]["x"].tobytes() == s["x"].tobytes()
+            continue
+        e, dt = params[k]
+        err = trajectory_errors(s, got[k], _solo(s, budgets[k], e=e, dt=dt))
+        assert err["pos_rel_l2"] < 1e-6 and err["vel_rel_l2"] < 1e-6, (k, err)
+
+
+def test_autotune_keeps_results():
+    import physim_gb300 as pg
+    from test_verlet_gpu import trajectory_errors
+    members = _members()
+    cfg = pg.SimConfig(gravity="simple_astro", e=0.01, dt=1e-5)
+    with pg.Ensemble(members, cfg) as ens:
+        plan = ens.autotune()
+        ens.step(10)
+        got = [ens.download(k) for k in range(len(members))]
+    assert plan["candidates"] >= 8 and plan["force_ms"] > 0
+    for k in (0, 5, 9):
+        err = trajectory_errors(members[k], got[k], _solo(members[k], 10))
+        assert err["pos_rel_l2"] < 1e-6, (k, err)
+
+
+def test_upload_resets_member():
+    import physim_gb300 as pg
+    from test_verlet_gpu import trajectory_errors
+    members = _members()[:3]
+    cfg = pg.SimConfig(gravity="simple_astro", e=0.01, dt=1e-5)
+    with pg.Ensemble(members, cfg) as ens:
+        ens.step(3)
+        ens.upload(1, members[1])
+        ens.step(2)
+        got1 = ens.download(1)
+        done, _ = ens.progress()
+    assert list(done) == [5, 2, 5]
+    err = trajectory_errors(members[1], got1, _solo(members[1], 2))
+    assert err["pos_rel_l2"] < 1e-6, err
