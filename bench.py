@@ -558,14 +558,15 @@ def run_ours(args, dist: Dist):
         return
     base = direct if direct else (bh if bh else ens)
     line = {
-        "metric": METRIC if direct else bh["metric"],
+        "metric": METRIC if direct else base["metric"],
         "value": base["value"],
-        "unit": "Gpair-interactions/s" if direct else "steps/s",
+        "unit": "Gpair-interactions/s" if direct else base["unit"],
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": base["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 pairs, f64 integration", "data": "synthetic",
-        "config": {"workload": WORKLOAD if direct else "astro2 " + WORKLOAD,
-                   "bodies": base["bodies"],
+        "config": {"workload": WORKLOAD if direct else ("astro2 " + WORKLOAD if bh else
+                                                        "512-member uneven ensemble"),
+                   "bodies": base.get("bodies", base.get("bodies_total")),
                    "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU",
                    "l2": "flushed between timed steps (256 MiB write, outside the events)",
                    "compensated_sums": True},
