@@ -324,6 +324,21 @@ void *physim_gpu_ensemble_stream(PhysimEnsemble *ens);
 int physim_gpu_ensemble_launches_per_step(PhysimEnsemble *ens);
 void physim_gpu_ensemble_destroy(PhysimEnsemble *ens);
 
+/* simple_astro accelerations for callers that cannot allocate device memory.
+ * This entry point has no counterpart in the reference.  It serves code that
+ * must not call cudaMalloc (a framework's memory pool or arena, a real-time
+ * loop, a process whose device memory is handed out up front): the caller
+ * passes device-accessible arrays, state[n] (read) and acc[n] (acc[i] += a_i
+ * for every non-fixed body, as simple_astro_transform does), and the work is
+ * enqueued on `stream` (a cudaStream_t; NULL: the legacy default stream).
+ * Scratch lives in one static device array of about 7.9 MiB that every GPU
+ * loading the library holds until exit; at most 65,536 bodies (larger n is
+ * rejected with PHYSIM_ERR_ARGUMENT).  The first call on a device looks up
+ * that array's device address, so make it before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race. */
+int physim_gpu_simple_astro_accumulate_static(const Entity *state, size_t n, double e,
+                                              Acceleration *acc, void *stream);
+
 /* Verlet integrator over host arrays (integrators/src/verlet.rs:19-121).
  * A Rust IntegratorElement shim evaluates acc_fn itself and hands the
  * accelerations over; the step runs on the GPU in f64 in the reference's

@@ -170,6 +170,11 @@ int direct_candidates(int n, int device, bool compensated, DirectPlan *out, int 
     return k;
 }
 
+DirectPlan make_direct_plan(int n, int block, int ipt, int splits, bool compensated)
+{
+    return make_plan(n, block, ipt, splits, compensated);
+}
+
 int launch_direct(const DirectPlan &plan, const float4 *body4, float e, double *partial,
                   cudaStream_t stream)
 {

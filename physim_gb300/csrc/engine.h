@@ -40,6 +40,8 @@ struct DirectPlan {
 // Heuristic plan that fills the GPU: picks the i-tile shape and the number of
 // j splits whose block count wastes least in the last wave.
 DirectPlan plan_direct(int n, int device, bool compensated);
+// A plan with a given shape and number of j splits (clamped to 1..j tiles).
+DirectPlan make_direct_plan(int n, int block, int ipt, int splits, bool compensated);
 // Enumerates the candidate plans the autotuner times for n bodies.
 int direct_candidates(int n, int device, bool compensated, DirectPlan *out, int cap);
 
