@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--skip-e2e", action="store_true", help="profiling runs: device path only")
     p.add_argument("--only", default="", help="comma list of parts: direct, bh, ensemble")
+    p.add_argument("--serve-seconds", type=float, default=20.0)
+    p.add_argument("--serve-drain", type=float, default=40.0)
     p.add_argument("--ens-steps", type=int, default=200)
     p.add_argument("--ens-members", type=int, default=512)
     p.add_argument("--bh-steps", type=int, default=1000)
@@ -547,14 +549,56 @@ def measure_ensemble(args, dist: Dist, device: int) -> dict:
             "speedup_vs_plain": ens_rate / plain_rate}
 
 
+def measure_served(args, dist: Dist, device: int) -> dict:
+    """The served mix: Poisson arrivals (50 jobs/s) of direct-sum and
+    Barnes-Hut jobs with log-uniform N in [1,024, 2,097,152] and 100-5,000
+    steps, admitted by a 150 GB HBM budget and run with continuous batching.
+    Arrivals for --serve-seconds, then up to --serve-drain seconds to finish;
+    jobs still queued or running at the cut-off are reported as unfinished."""
+    from physim_gb300.server import GpuExecutor, Server, latency_summary, served_mix
+
+    jobs = served_mix(rate=50.0, seconds=args.serve_seconds, seed=5)
+    srv = Server(GpuExecutor(device=device, tick_ms=25.0, download=True),
+                 hbm_budget=150 << 30)
+    srv.submit(jobs)
+    t0 = time.perf_counter()
+    res = srv.run(until=args.serve_seconds + args.serve_drain)
+    wall = time.perf_counter() - t0
+    unfinished = srv.unfinished()
+    srv.close()
+    offered_direct = sum(j.n * j.n * j.steps for j in jobs if j.gravity == "simple_astro")
+    lat = latency_summary(res)
+    depth = srv.queue_depth
+    return {"metric": "served-mix job latency (arrival to final state on the host)",
+            "p50_s": lat.get("p50_s"), "p99_s": lat.get("p99_s"), "latency": lat,
+            "jobs_arrived": len(jobs), "completed": len(res), "unfinished_at_cutoff": unfinished,
+            "failed": len(srv.failed), "rejected": len(srv.rejected),
+            "steps_completed": srv.steps_done,
+            "aggregate_steps_per_s": srv.steps_done / wall, "wall_s": wall,
+            "arrival_seconds": args.serve_seconds, "drain_seconds": args.serve_drain,
+            "max_waiting": max((d[1] for d in depth), default=0),
+            "max_running_units": max((d[2] for d in depth), default=0),
+            "max_hbm_in_use_gb": max((d[3] for d in depth), default=0) / 2**30,
+            "queue_depth_samples": [(round(t, 2), w, r) for t, w, r, _ in depth[::8]],
+            "offered_direct_pairs": offered_direct,
+            "note": "offered load far exceeds one GPU (the direct-sum jobs alone are "
+                    f"{offered_direct / 2.3e12:.0f} GPU-seconds at 2.3e12 pairs/s); latency "
+                    "is dominated by backlog"}
+
+
 def run_ours(args, dist: Dist):
     device, sms = _device_context(dist)
     peaks = measured_peaks()
-    parts = args.only.split(",") if args.only else ["direct", "bh", "ensemble"]
+    parts = args.only.split(",") if args.only else ["direct", "bh", "ensemble", "served"]
     direct = measure_direct(args, dist, device, sms, peaks) if "direct" in parts else None
     bh = measure_bh(args, dist, device, sms, peaks) if "bh" in parts else None
     ens = measure_ensemble(args, dist, device) if "ensemble" in parts else None
+    served = measure_served(args, dist, device) if "served" in parts else None
     if dist.rank != 0:
+        return
+    if served and not (direct or bh or ens):
+        print(json.dumps({"metric": served["metric"], "value": served["p50_s"], "unit": "s",
+                          "higher_is_better": False, "served": served}), flush=True)
         return
     base = direct if direct else (bh if bh else ens)
     line = {
@@ -576,6 +620,8 @@ def run_ours(args, dist: Dist):
         for k in ("roofline", "e2e", "gpu_launches", "cpu_baseline", "clocks"):
             if k in direct:
                 line[k] = direct[k]
+    if served:
+        line["served"] = served
     if ens:
         line["ensemble"] = ens
         if not direct and not bh:

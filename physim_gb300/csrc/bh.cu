@@ -31,6 +31,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 #include "engine.h"
 #include "plugin_state.h"
@@ -1150,6 +1152,7 @@ struct BhWorkspace {
     int launches = 0;
     // which key/val buffer holds the sorted result
     int sorted = 0;
+    int leaf_min = 1;  // smallest leaf size the node capacity was sized for
     // optional events around the traversal kernel (recorded into graphs too)
     bool profiling = false;
     cudaEvent_t trav_ev[2] = {nullptr, nullptr};
@@ -1175,9 +1178,10 @@ static int wsalloc(T *&p, size_t count)
     return PHYSIM_OK;
 }
 
-int bh_reserve(BhWorkspace *&ws, size_t n, int device)
+int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf)
 {
-    if (ws && n <= ws->cap_n) return PHYSIM_OK;
+    leaf = leaf < 1 ? 1 : leaf;
+    if (ws && n <= ws->cap_n && leaf >= ws->leaf_min) return PHYSIM_OK;
     if (ws) {
         ws_release(ws);
         delete ws;
@@ -1192,10 +1196,11 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device)
     w->grid_build = sms * 2;
     w->grid_mom = sms * 2;
     const int tiles = cdiv((long long)cap, kSortTile);
-    // Node capacity: about 4N nodes holds every non-degenerate distribution
-    // even with leaf size 1; deeper chains only truncate the tree (exact,
-    // slower) and raise a flag.
-    const size_t ncap = 4 * cap + 64 * kMaxLevels;
+    // Node capacity: leaves hold about leaf/4 bodies on average, so 8N/leaf
+    // (at most 4N) nodes hold every non-degenerate distribution; deeper
+    // chains only leave levels unsplit (exact, slower) and raise a flag.
+    const size_t ncap = std::min<size_t>(4 * cap, 8 * cap / (size_t)leaf) + 4096 + 64 * kMaxLevels;
+    w->leaf_min = leaf;
     int rc = PHYSIM_OK;
 #define PG_WA(ptr, cnt)                                                                     \
     if (rc == PHYSIM_OK) rc = wsalloc(ptr, cnt)

@@ -56,7 +56,7 @@ static int accumulate_locked(ElementState *el, const Entity *state, size_t n, Ac
         PG_TRY(launch_direct(el->plan, el->bodies.body4, (float)el->e, el->partial, st));
     } else {
         PG_TRY(ensure_doubles(el->partial, el->partial_cap, 3 * n));
-        PG_TRY(bh_reserve(el->bh, n, el->device));
+        PG_TRY(bh_reserve(el->bh, n, el->device, el->leaf_size));
         BhParams p;
         p.nchild = el->kind == 1 ? 8 : 4;
         p.theta = el->theta;

@@ -49,7 +49,7 @@ struct BhParams {
     bool compensated = true;
 };
 
-int bh_reserve(BhWorkspace *&ws, size_t n, int device);
+int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf);
 void bh_free(BhWorkspace *ws);
 // Accelerations of the bodies in b (f64 positions and f32 copies must be
 // current) into partial[c*n + i] (one split).

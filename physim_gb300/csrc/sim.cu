@@ -164,7 +164,7 @@ int physim_gpu_sim_create(const PhysimSimConfig *cfg, size_t n, PhysimSim **out)
         partial_elems *= (size_t)s->plan.splits;
     }
     if (rc == PHYSIM_OK && cfg->gravity != PHYSIM_GRAVITY_SIMPLE_ASTRO)
-        rc = bh_reserve(s->bh, n, cfg->device);
+        rc = bh_reserve(s->bh, n, cfg->device, (int)cfg->leaf_size);
     if (rc == PHYSIM_OK && cudaMalloc((void **)&s->partial, partial_elems * sizeof(double)) !=
                                cudaSuccess) {
         set_error("cudaMalloc of partial sums failed");

@@ -1,0 +1,389 @@
+"""A continuous-batching request loop for gravity simulations.
+
+Jobs (a physim pipeline: one gravity element + verlet, a body count, a step
+count) arrive over time.  The server admits them while their device memory
+fits an HBM budget, keeps every job's state on the device until it
+finishes, and overlaps the work of all admitted jobs on the GPU:
+
+  * direct-sum jobs admitted in the same admission round become the members
+    of one batched ensemble (one persistent pair kernel per step for all of
+    them, each member stopping at its own step count on the device);
+  * Barnes-Hut jobs (astro2) run as device-resident simulations;
+  * every running unit has its own CUDA stream and at most one "tick" of
+    steps in flight; when a tick completes the unit gets the next one, jobs
+    that finished are downloaded and their memory returns to the budget,
+    and waiting jobs are admitted into the freed room.
+
+Latency is measured per job from its arrival to the download of its final
+state.  The device work goes through the `Executor` interface so the
+scheduling logic can be exercised without a GPU (tests use a fake executor).
+"""
+from __future__ import annotations
+
+import collections
+import heapq
+import math
+import threading
+import time
+from dataclasses import dataclass, field
+from typing import Callable, Iterable
+
+import numpy as np
+
+# Device bytes per body, by how a job runs (state, f32 copy, partial sums and,
+# for Barnes-Hut, the key/sort/tree workspace); used for admission.
+BYTES_PER_BODY_DIRECT = 200
+BYTES_PER_BODY_TREE = 700
+BYTES_FIXED = 4 << 20
+
+
+@dataclass(order=True)
+class JobSpec:
+    arrival: float
+    id: int = field(compare=False)
+    n: int = field(compare=False)
+    steps: int = field(compare=False)
+    gravity: str = field(default="simple_astro", compare=False)  # or "astro2"
+    theta: float = field(default=0.5, compare=False)
+    e: float = field(default=0.01, compare=False)
+    dt: float = field(default=1e-5, compare=False)
+    ic: str = field(default="cube", compare=False)  # "cube" or "plummer"
+    seed: int = field(default=0, compare=False)
+    leaf_size: int = field(default=16, compare=False)
+
+    def device_bytes(self) -> int:
+        per = BYTES_PER_BODY_DIRECT if self.gravity == "simple_astro" else BYTES_PER_BODY_TREE
+        return BYTES_FIXED + per * self.n
+
+
+@dataclass
+class JobResult:
+    spec: JobSpec
+    admitted: float
+    finished: float
+    state: np.ndarray | None = None
+    error: str | None = None
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.spec.arrival
+
+
+def initial_state(spec: JobSpec) -> np.ndarray:
+    from . import ics
+    if spec.ic == "plummer":
+        return ics.plummer(spec.n, seed=spec.seed, a=0.1)
+    return ics.cube_with_stars(spec.n, seed=spec.seed)
+
+
+def served_mix(rate: float = 50.0, seconds: float = 120.0, seed: int = 5,
+               n_lo: int = 1024, n_hi: int = 2_097_152, steps_lo: int = 100,
+               steps_hi: int = 5000, direct_below: int = 32768) -> list[JobSpec]:
+    """Poisson arrivals at `rate` jobs/s for `seconds`; N log-uniform in
+    [n_lo, n_hi], steps uniform in [steps_lo, steps_hi]; N < direct_below runs
+    the direct sum, larger N Barnes-Hut with theta drawn from {0.5, 1.0};
+    cube or Plummer initial conditions with equal odds; e = 0.01, dt = 1e-5."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t, jobs, k = 0.0, [], 0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            break
+        n = int(math.floor(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi)))))
+        steps = int(rng.integers(steps_lo, steps_hi + 1))
+        direct = n < direct_below
+        theta = float(rng.choice([0.5, 1.0]))
+        ic = "cube" if rng.random() < 0.5 else "plummer"
+        jobs.append(JobSpec(arrival=t, id=k, n=n, steps=steps,
+                            gravity="simple_astro" if direct else "astro2", theta=theta,
+                            ic=ic, seed=1000 + k))
+        k += 1
+    return jobs
+
+
+# ---------------------------------------------------------------------------
+# device execution
+# ---------------------------------------------------------------------------
+class Unit:
+    """A group of jobs that advances together on one stream."""
+
+    jobs: list[JobSpec]
+
+    def launch_tick(self) -> None: ...
+
+    def tick_done(self) -> bool: ...
+
+    def finished_jobs(self) -> list[tuple[JobSpec, np.ndarray | None]]:
+        """Jobs that reached their step count since the last call (with states)."""
+        ...
+
+    def alive(self) -> bool: ...
+
+    def close(self) -> None: ...
+
+
+class Executor:
+    def make_units(self, jobs: list[JobSpec]) -> list[Unit]: ...
+
+
+class GpuExecutor(Executor):
+    """Runs direct-sum jobs of one admission round as one ensemble and each
+    Barnes-Hut job as one device-resident simulation, each on its own stream;
+    a tick is about `tick_ms` of device work."""
+
+    def __init__(self, device: int = 0, tick_ms: float = 20.0, download: bool = True):
+        self.device = device
+        self.tick_ms = tick_ms
+        self.download = download
+
+    def make_units(self, jobs: list[JobSpec]) -> list[Unit]:
+        direct = [j for j in jobs if j.gravity == "simple_astro"]
+        tree = [j for j in jobs if j.gravity != "simple_astro"]
+        units: list[Unit] = []
+        if direct:
+            units.append(_EnsembleUnit(direct, self))
+        for j in tree:
+            units.append(_SimUnit(j, self))
+        return units
+
+
+class _CudaTick:
+    def __init__(self, stream_ptr: int, device: int):
+        import torch
+        self.torch = torch
+        self.stream = torch.cuda.ExternalStream(stream_ptr, device=torch.device("cuda", device))
+        self.event = None
+
+    def record(self):
+        self.event = self.torch.cuda.Event()
+        self.event.record(self.stream)
+
+    def done(self) -> bool:
+        return self.event is None or self.event.query()
+
+
+class _EnsembleUnit(Unit):
+    def __init__(self, jobs: list[JobSpec], ex: GpuExecutor):
+        from . import Ensemble, SimConfig
+        self.jobs = list(jobs)
+        self.ex = ex
+        states = [initial_state(j) for j in jobs]
+        cfg = SimConfig(gravity="simple_astro", e=0.01, dt=1e-5, device=ex.device)
+        self.ens = Ensemble(states, cfg, steps=[j.steps for j in jobs],
+                            params=[(j.e, j.dt) for j in jobs])
+        self.tick = _CudaTick(self.ens.stream, ex.device)
+        pairs = sum(j.n * j.n for j in jobs)
+        est_ms = max(pairs / 2.0e12 * 1e3, 0.02)
+        self.k = int(max(1, min(max(j.steps for j in jobs), ex.tick_ms / est_ms)))
+        self.reported: set[int] = set()
+        self.left = len(jobs)
+
+    def launch_tick(self) -> None:
+        self.ens.step(self.k)
+        self.tick.record()
+
+    def tick_done(self) -> bool:
+        return self.tick.done()
+
+    def finished_jobs(self):
+        done, rem = self.ens.progress()
+        out = []
+        for i, j in enumerate(self.jobs):
+            if i not in self.reported and rem[i] == 0:
+                self.reported.add(i)
+                self.left -= 1
+                out.append((j, self.ens.download(i) if self.ex.download else None))
+        return out
+
+    def alive(self) -> bool:
+        return self.left > 0
+
+    def close(self) -> None:
+        self.ens.close()
+
+
+class _SimUnit(Unit):
+    def __init__(self, job: JobSpec, ex: GpuExecutor):
+        from . import SimConfig, Simulation
+        self.jobs = [job]
+        self.ex = ex
+        self.sim = Simulation(initial_state(job),
+                              SimConfig(gravity=job.gravity, theta=job.theta, e=job.e, dt=job.dt,
+                                        leaf_size=job.leaf_size, traversal="warp",
+                                        device=ex.device))
+        self.tick = _CudaTick(self.sim.stream, ex.device)
+        est_ms = max(job.n * 1.6e-6, 0.05)
+        self.k_full = int(max(1, ex.tick_ms / est_ms))
+        self.left = job.steps
+        self.reported = False
+
+    def launch_tick(self) -> None:
+        k = min(self.k_full, self.left)
+        if k > 0:
+            self.sim.step(k)
+            self.left -= k
+        self.tick.record()
+
+    def tick_done(self) -> bool:
+        return self.tick.done()
+
+    def finished_jobs(self):
+        if self.left == 0 and not self.reported:
+            self.reported = True
+            return [(self.jobs[0], self.sim.download() if self.ex.download else None)]
+        return []
+
+    def alive(self) -> bool:
+        return not self.reported
+
+    def close(self) -> None:
+        self.sim.close()
+
+
+# ---------------------------------------------------------------------------
+# the request loop
+# ---------------------------------------------------------------------------
+class Server:
+    """Continuous batching: admission by memory budget, overlapping units."""
+
+    def __init__(self, executor: Executor, hbm_budget: int = 150 << 30,
+                 clock: Callable[[], float] = time.perf_counter,
+                 max_units: int = 256, keep_states: bool = False):
+        self.executor = executor
+        self.keep_states = keep_states
+        self.budget = hbm_budget
+        self.clock = clock
+        self.max_units = max_units
+        self.pending: collections.deque[JobSpec] = collections.deque()
+        self.arrivals: list[JobSpec] = []  # heap by arrival time (not yet arrived)
+        self.units: list[Unit] = []
+        self.in_use = 0
+        self.results: list[JobResult] = []
+        self.admitted_at: dict[int, float] = {}
+        self.queue_depth: list[tuple[float, int, int, int]] = []  # (t, waiting, running, in_use)
+        self.rejected: list[JobSpec] = []
+        self.failed: list[JobResult] = []
+        self.steps_done = 0
+        self._lock = threading.Lock()
+        self.t0 = 0.0
+
+    def submit(self, jobs: Iterable[JobSpec]) -> None:
+        with self._lock:
+            for j in jobs:
+                heapq.heappush(self.arrivals, j)
+
+    def _admit(self, now: float) -> None:
+        while self.arrivals and self.arrivals[0].arrival <= now:
+            j = heapq.heappop(self.arrivals)
+            if j.device_bytes() > self.budget:
+                self.rejected.append(j)  # can never fit
+            else:
+                self.pending.append(j)
+        batch = []
+        # first fit in arrival order; a job that does not fit now keeps its
+        # place and later (smaller) jobs may go ahead of it
+        keep = collections.deque()
+        room = self.budget - self.in_use
+        while self.pending:
+            j = self.pending.popleft()
+            need = j.device_bytes()
+            if need <= room and len(self.units) + len(batch) < self.max_units:
+                batch.append(j)
+                room -= need
+            else:
+                keep.append(j)
+        self.pending = keep
+        if batch:
+            for j in batch:
+                self.admitted_at[j.id] = now
+                self.in_use += j.device_bytes()
+            try:
+                units = self.executor.make_units(batch)
+            except Exception as err:  # noqa: BLE001 -- e.g. device out of memory
+                t = self.clock() - self.t0
+                for j in batch:
+                    self.failed.append(JobResult(j, now, t, None, repr(err)))
+                    self.in_use -= j.device_bytes()
+                return
+            for u in units:
+                try:
+                    u.launch_tick()
+                    self.units.append(u)
+                except Exception as err:  # noqa: BLE001
+                    self._fail_unit(u, err)
+
+    def _fail_unit(self, u: Unit, err: BaseException) -> None:
+        """A unit whose device work raised: its unfinished jobs fail, their
+        memory returns to the budget, the other units keep running."""
+        done_ids = {r.spec.id for r in self.results}
+        t = self.clock() - self.t0
+        for j in u.jobs:
+            if j.id not in done_ids:
+                self.failed.append(JobResult(j, self.admitted_at.get(j.id, t), t, None, repr(err)))
+                self.in_use -= j.device_bytes()
+        try:
+            u.close()
+        except Exception:
+            pass
+
+    def _service(self, now: float) -> None:
+        still = []
+        for u in self.units:
+            try:
+                if not u.tick_done():
+                    still.append(u)
+                    continue
+                for j, state in u.finished_jobs():
+                    t = self.clock() - self.t0
+                    self.results.append(JobResult(j, self.admitted_at[j.id], t,
+                                                  state if self.keep_states else None))
+                    self.in_use -= j.device_bytes()
+                    self.steps_done += j.steps
+                if u.alive():
+                    u.launch_tick()
+                    still.append(u)
+                else:
+                    u.close()
+            except Exception as err:  # noqa: BLE001 -- isolate the failing unit
+                self._fail_unit(u, err)
+        self.units = still
+
+    def run(self, until: float | None = None, poll: float = 0.001,
+            sample_every: float = 0.25) -> list[JobResult]:
+        """Serves until every submitted job finished, or until `until` seconds
+        after the start (jobs still running then are left unfinished)."""
+        self.t0 = self.clock()
+        next_sample = 0.0
+        while True:
+            now = self.clock() - self.t0
+            if until is not None and now >= until:
+                break
+            with self._lock:
+                self._admit(now)
+            self._service(now)
+            if now >= next_sample:
+                self.queue_depth.append((now, len(self.pending), len(self.units), self.in_use))
+                next_sample = now + sample_every
+            if not self.units and not self.pending and not self.arrivals:
+                break
+            time.sleep(poll)
+        return self.results
+
+    def unfinished(self) -> int:
+        done_ids = {r.spec.id for r in self.results} | {f.spec.id for f in self.failed}
+        running = sum(1 for u in self.units for j in u.jobs if j.id not in done_ids)
+        return running + len(self.pending) + len(self.arrivals)
+
+    def close(self) -> None:
+        for u in self.units:
+            u.close()
+        self.units = []
+
+
+def latency_summary(results: list[JobResult]) -> dict:
+    if not results:
+        return {"completed": 0}
+    lat = np.array([r.latency for r in results])
+    return {"completed": len(results), "p50_s": float(np.percentile(lat, 50)),
+            "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()),
+            "max_s": float(lat.max())}

@@ -1,0 +1,144 @@
+"""The continuous-batching request loop (physim_gb300/server.py) with a fake
+executor: admission within the memory budget, first-fit ordering, arrival
+times, cutoff accounting and isolation of a failing unit.  CPU only; the
+failure is made on the host (an exception from a fake unit)."""
+from __future__ import annotations
+
+import pytest
+
+from physim_gb300.server import (BYTES_FIXED, BYTES_PER_BODY_DIRECT, Executor, JobSpec, Server,
+                                 Unit, latency_summary, served_mix)
+
+
+class FakeUnit(Unit):
+    def __init__(self, jobs, ex):
+        self.jobs = list(jobs)
+        self.ex = ex
+        self.left = {j.id: j.steps for j in jobs}
+        self.reported = set()
+
+    def launch_tick(self):
+        if any(j.id in self.ex.fail_ids for j in self.jobs):
+            raise RuntimeError("injected device failure")
+        for j in self.jobs:
+            self.left[j.id] = max(0, self.left[j.id] - self.ex.k)
+
+    def tick_done(self):
+        return True
+
+    def finished_jobs(self):
+        out = []
+        for j in self.jobs:
+            if self.left[j.id] == 0 and j.id not in self.reported:
+                self.reported.add(j.id)
+                out.append((j, None))
+        return out
+
+    def alive(self):
+        return len(self.reported) < len(self.jobs)
+
+    def close(self):
+        self.ex.closed += 1
+
+
+class FakeExecutor(Executor):
+    def __init__(self, k=10, fail_ids=()):
+        self.k = k
+        self.fail_ids = set(fail_ids)
+        self.batches = []
+        self.closed = 0
+        self.max_in_use = 0
+        self.server = None
+
+    def make_units(self, jobs):
+        self.batches.append([j.id for j in jobs])
+        if self.server is not None:
+            self.max_in_use = max(self.max_in_use, self.server.in_use)
+        return [FakeUnit([j], self) for j in jobs]
+
+
+def job(i, n, steps, t=0.0, gravity="simple_astro"):
+    return JobSpec(arrival=t, id=i, n=n, steps=steps, gravity=gravity)
+
+
+def test_all_jobs_complete_once():
+    ex = FakeExecutor()
+    srv = Server(ex, hbm_budget=1 << 40)
+    ex.server = srv
+    jobs = [job(i, 1000 + i, 5 + 3 * i, t=0.001 * i) for i in range(30)]
+    srv.submit(jobs)
+    res = srv.run(until=30.0)
+    assert sorted(r.spec.id for r in res) == list(range(30))
+    assert srv.unfinished() == 0 and srv.in_use == 0
+    assert srv.steps_done == sum(j.steps for j in jobs)
+    for r in res:
+        assert r.admitted >= r.spec.arrival and r.finished >= r.admitted
+    s = latency_summary(res)
+    assert s["completed"] == 30 and s["p99_s"] >= s["p50_s"]
+
+
+def test_budget_is_respected_and_first_fit():
+    ex = FakeExecutor(k=1)
+    per = BYTES_PER_BODY_DIRECT
+    budget = 2 * BYTES_FIXED + 2 * per * 10_000
+    srv = Server(ex, hbm_budget=budget)
+    ex.server = srv
+    big = job(0, 10_000, 50)
+    blocked = job(1, 15_000, 5, t=0.0001)   # does not fit beside `big`
+    small = job(2, 5_000, 5, t=0.0002)      # fits: overtakes the waiting job
+    srv.submit([big, blocked, small])
+    srv.run(until=30.0)
+    assert ex.max_in_use <= budget
+    order = [i for b in ex.batches for i in b]
+    assert order.index(2) < order.index(1)
+    assert srv.unfinished() == 0
+
+
+def test_oversized_job_is_rejected():
+    ex = FakeExecutor()
+    srv = Server(ex, hbm_budget=BYTES_FIXED + 10)
+    srv.submit([job(0, 1_000_000, 10)])
+    srv.run(until=5.0)
+    assert [j.id for j in srv.rejected] == [0]
+    assert not srv.results
+
+
+def test_arrivals_wait_for_their_time():
+    ex = FakeExecutor()
+    srv = Server(ex, hbm_budget=1 << 40)
+    srv.submit([job(0, 100, 1, t=0.0), job(1, 100, 1, t=0.15)])
+    res = srv.run(until=10.0)
+    by_id = {r.spec.id: r for r in res}
+    assert by_id[1].admitted >= 0.15
+
+
+def test_cutoff_leaves_jobs_unfinished():
+    ex = FakeExecutor(k=1)
+    srv = Server(ex, hbm_budget=1 << 40)
+    srv.submit([job(i, 100, 10**9, t=0.0) for i in range(3)] + [job(9, 100, 1, t=100.0)])
+    srv.run(until=0.05)
+    assert srv.unfinished() == 4
+    srv.close()
+
+
+def test_failing_unit_is_isolated():
+    ex = FakeExecutor(fail_ids={3})
+    srv = Server(ex, hbm_budget=1 << 40)
+    srv.submit([job(i, 100 * (i + 1), 20) for i in range(6)])
+    res = srv.run(until=30.0)
+    assert sorted(r.spec.id for r in res) == [0, 1, 2, 4, 5]
+    assert [f.spec.id for f in srv.failed] == [3]
+    assert "injected" in srv.failed[0].error
+    assert srv.in_use == 0
+
+
+def test_served_mix_distribution():
+    jobs = served_mix(rate=50.0, seconds=20.0, seed=5)
+    assert 800 < len(jobs) < 1200
+    ns = [j.n for j in jobs]
+    assert min(ns) >= 1024 and max(ns) <= 2_097_152
+    assert all((j.gravity == "simple_astro") == (j.n < 32768) for j in jobs)
+    assert {j.theta for j in jobs if j.gravity == "astro2"} <= {0.5, 1.0}
+    assert all(100 <= j.steps <= 5000 for j in jobs)
+    arr = [j.arrival for j in jobs]
+    assert arr == sorted(arr) and arr[-1] < 20.0
