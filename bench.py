@@ -577,7 +577,7 @@ def measure_served(args, dist: Dist, device: int) -> dict:
             "aggregate_steps_per_s": srv.steps_done / wall, "wall_s": wall,
             "arrival_seconds": args.serve_seconds, "drain_seconds": args.serve_drain,
             "max_waiting": max((d[1] for d in depth), default=0),
-            "max_running_units": max((d[2] for d in depth), default=0),
+            "max_running_units": srv.max_running,
             "max_hbm_in_use_gb": max((d[3] for d in depth), default=0) / 2**30,
             "queue_depth_samples": [(round(t, 2), w, r) for t, w, r, _ in depth[::8]],
             "offered_direct_pairs": offered_direct,

@@ -264,6 +264,7 @@ class Server:
         self.rejected: list[JobSpec] = []
         self.failed: list[JobResult] = []
         self.steps_done = 0
+        self.max_running = 0  # most units with work on the device at one time
         self._lock = threading.Lock()
         self.t0 = 0.0
 
@@ -311,6 +312,7 @@ class Server:
                     self.units.append(u)
                 except Exception as err:  # noqa: BLE001
                     self._fail_unit(u, err)
+            self.max_running = max(self.max_running, len(self.units))
 
     def _fail_unit(self, u: Unit, err: BaseException) -> None:
         """A unit whose device work raised: its unfinished jobs fail, their
