@@ -573,8 +573,8 @@ def measure_served(args, dist: Dist, device: int) -> dict:
             "p50_s": lat.get("p50_s"), "p99_s": lat.get("p99_s"), "latency": lat,
             "jobs_arrived": len(jobs), "completed": len(res), "unfinished_at_cutoff": unfinished,
             "failed": len(srv.failed), "rejected": len(srv.rejected),
-            "steps_completed": srv.steps_done,
-            "aggregate_steps_per_s": srv.steps_done / wall, "wall_s": wall,
+            "steps_of_completed_jobs": srv.steps_done, "steps_executed": srv.steps_executed,
+            "aggregate_steps_per_s": srv.steps_executed / wall, "wall_s": wall,
             "arrival_seconds": args.serve_seconds, "drain_seconds": args.serve_drain,
             "max_waiting": max((d[1] for d in depth), default=0),
             "max_running_units": srv.max_running,

@@ -108,6 +108,7 @@ class Unit:
     """A group of jobs that advances together on one stream."""
 
     jobs: list[JobSpec]
+    tick_steps: int = 0  # job-steps enqueued by the last launch_tick
 
     def launch_tick(self) -> None: ...
 
@@ -177,9 +178,16 @@ class _EnsembleUnit(Unit):
         self.k = int(max(1, min(max(j.steps for j in jobs), ex.tick_ms / est_ms)))
         self.reported: set[int] = set()
         self.left = len(jobs)
+        self.host_left = [j.steps for j in jobs]  # host-side count for step accounting
+        self.tick_steps = 0
 
     def launch_tick(self) -> None:
         self.ens.step(self.k)
+        self.tick_steps = 0
+        for i, r in enumerate(self.host_left):
+            t = min(self.k, r)
+            self.host_left[i] = r - t
+            self.tick_steps += t
         self.tick.record()
 
     def tick_done(self) -> bool:
@@ -216,12 +224,14 @@ class _SimUnit(Unit):
         self.k_full = int(max(1, ex.tick_ms / est_ms))
         self.left = job.steps
         self.reported = False
+        self.tick_steps = 0
 
     def launch_tick(self) -> None:
         k = min(self.k_full, self.left)
         if k > 0:
             self.sim.step(k)
             self.left -= k
+        self.tick_steps = k
         self.tick.record()
 
     def tick_done(self) -> bool:
@@ -248,8 +258,9 @@ class Server:
 
     def __init__(self, executor: Executor, hbm_budget: int = 150 << 30,
                  clock: Callable[[], float] = time.perf_counter,
-                 max_units: int = 256, keep_states: bool = False):
+                 max_units: int = 64, max_batch: int = 16, keep_states: bool = False):
         self.executor = executor
+        self.max_batch = max_batch
         self.keep_states = keep_states
         self.budget = hbm_budget
         self.clock = clock
@@ -263,7 +274,8 @@ class Server:
         self.queue_depth: list[tuple[float, int, int, int]] = []  # (t, waiting, running, in_use)
         self.rejected: list[JobSpec] = []
         self.failed: list[JobResult] = []
-        self.steps_done = 0
+        self.steps_done = 0      # steps of completed jobs
+        self.steps_executed = 0  # all job-steps the device finished
         self.max_running = 0  # most units with work on the device at one time
         self._lock = threading.Lock()
         self.t0 = 0.0
@@ -288,7 +300,8 @@ class Server:
         while self.pending:
             j = self.pending.popleft()
             need = j.device_bytes()
-            if need <= room and len(self.units) + len(batch) < self.max_units:
+            if (need <= room and len(self.units) + len(batch) < self.max_units
+                    and len(batch) < self.max_batch):
                 batch.append(j)
                 room -= need
             else:
@@ -335,6 +348,8 @@ class Server:
                 if not u.tick_done():
                     still.append(u)
                     continue
+                self.steps_executed += u.tick_steps
+                u.tick_steps = 0
                 for j, state in u.finished_jobs():
                     t = self.clock() - self.t0
                     self.results.append(JobResult(j, self.admitted_at[j.id], t,

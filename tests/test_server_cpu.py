@@ -20,8 +20,11 @@ class FakeUnit(Unit):
     def launch_tick(self):
         if any(j.id in self.ex.fail_ids for j in self.jobs):
             raise RuntimeError("injected device failure")
+        self.tick_steps = 0
         for j in self.jobs:
-            self.left[j.id] = max(0, self.left[j.id] - self.ex.k)
+            t = min(self.ex.k, self.left[j.id])
+            self.left[j.id] -= t
+            self.tick_steps += t
 
     def tick_done(self):
         return True
@@ -71,6 +74,7 @@ def test_all_jobs_complete_once():
     assert sorted(r.spec.id for r in res) == list(range(30))
     assert srv.unfinished() == 0 and srv.in_use == 0
     assert srv.steps_done == sum(j.steps for j in jobs)
+    assert srv.steps_executed == sum(j.steps for j in jobs)
     for r in res:
         assert r.admitted >= r.spec.arrival and r.finished >= r.admitted
     s = latency_summary(res)
@@ -92,6 +96,17 @@ def test_budget_is_respected_and_first_fit():
     order = [i for b in ex.batches for i in b]
     assert order.index(2) < order.index(1)
     assert srv.unfinished() == 0
+
+
+def test_unit_and_batch_caps():
+    ex = FakeExecutor(k=1)
+    srv = Server(ex, hbm_budget=1 << 40, max_units=5, max_batch=2)
+    ex.server = srv
+    srv.submit([job(i, 100, 30) for i in range(12)])
+    srv.run(until=30.0)
+    assert max(len(b) for b in ex.batches) <= 2
+    assert srv.max_running <= 5
+    assert len(srv.results) == 12
 
 
 def test_oversized_job_is_rejected():
