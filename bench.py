@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--skip-e2e", action="store_true", help="profiling runs: device path only")
     p.add_argument("--only", default="", help="comma list of parts: direct, bh, ensemble")
+    p.add_argument("--precision-steps", type=int, default=200)
+    p.add_argument("--precision-bodies", type=int, default=262_144)
     p.add_argument("--serve-seconds", type=float, default=20.0)
     p.add_argument("--serve-drain", type=float, default=40.0)
     p.add_argument("--ens-steps", type=int, default=200)
@@ -549,6 +551,74 @@ def measure_ensemble(args, dist: Dist, device: int) -> dict:
             "speedup_vs_plain": ens_rate / plain_rate}
 
 
+def _acc_errors(sim, state, idx, e) -> dict:
+    """RMS / max relative acceleration error of the GPU forces of `state`
+    against the f64 direct sum (the oracle) on the bodies idx."""
+    import oracle
+    exact = oracle.simple_astro_sample(state, e, idx)
+    ex = np.stack([exact["x"], exact["y"], exact["z"]], 1)
+    a = sim.accelerations()[idx]
+    got = np.stack([a["x"], a["y"], a["z"]], 1)
+    rel = np.linalg.norm(got - ex, axis=1) / np.linalg.norm(ex, axis=1)
+    return {"rms": float(np.sqrt(np.mean(rel ** 2))), "max": float(rel.max())}
+
+
+def measure_precision(args, dist: Dist, device: int) -> dict:
+    """Precision study: 262,144-body Plummer sphere (a = 0.1, M = 1, seed 7,
+    isotropic distribution-function velocities), e = 1e-3, dt = 1e-4.  Per
+    variant (plain FP32 sums, compensated FP32 sums): RMS/max relative
+    acceleration error against the f64 direct sum (the oracle) on a
+    1,024-body sample of the initial and of the final state, and the relative
+    energy and momentum drift (f64 on the device) every steps/10 steps over
+    --precision-steps steps."""
+    import physim_gb300 as pg
+    from physim_gb300 import ics
+
+    n = args.precision_bodies
+    steps = args.precision_steps
+    state = ics.plummer(n, seed=7, a=0.1, total_mass=1.0)
+    e, dt = 1e-3, 1e-4
+    idx = np.sort(np.random.default_rng(7).choice(n, min(n, 1024), replace=False))
+    every = max(1, steps // 10)
+    # momentum scale: sum of |m v| of the initial state
+    pscale = float(np.sum(state["mass"] * np.sqrt(state["vx"] ** 2 + state["vy"] ** 2 +
+                                                  state["vz"] ** 2)))
+    out = {"bodies": n, "e": e, "dt": dt, "steps": steps, "sample_bodies": len(idx),
+           "potential": "V = -m_a m_b atan(sqrt(e)/r)/sqrt(e) (gradient = the reference force)",
+           "variants": {}}
+    for name, comp in (("fp32_plain", False), ("fp32_compensated", True)):
+        sim = pg.Simulation(state, pg.SimConfig(gravity="simple_astro", e=e, dt=dt,
+                                                compensated=comp, device=device))
+        err0 = _acc_errors(sim, state, idx, e)
+        d0 = sim.diagnostics(potential=True)
+        p0 = np.array(d0["momentum"])
+        series = []
+        t0 = time.perf_counter()
+        done = 0
+        while done < steps:
+            k = min(every, steps - done)
+            sim.step(k)
+            done += k
+            d = sim.diagnostics(potential=True)
+            series.append({"step": done,
+                           "energy_drift": (d["energy"] - d0["energy"]) / abs(d0["energy"]),
+                           "momentum_drift": float(np.linalg.norm(np.array(d["momentum"]) - p0))
+                           / pscale})
+        run_s = time.perf_counter() - t0
+        final = sim.download()
+        err1 = _acc_errors(sim, final, idx, e)
+        sim.close()
+        out["variants"][name] = {
+            "acc_rms_rel_error": err0["rms"], "acc_max_rel_error": err0["max"],
+            "acc_rms_rel_error_final": err1["rms"], "acc_max_rel_error_final": err1["max"],
+            "energy_start": d0["energy"], "kinetic_start": d0["kinetic"],
+            "potential_start": d0["potential"],
+            "max_abs_relative_energy_drift": max(abs(r["energy_drift"]) for r in series),
+            "max_momentum_drift_over_sum_mv": max(r["momentum_drift"] for r in series),
+            "series": series, "run_s": run_s}
+    return out
+
+
 def measure_served(args, dist: Dist, device: int) -> dict:
     """The served mix: Poisson arrivals (50 jobs/s) of direct-sum and
     Barnes-Hut jobs with log-uniform N in [1,024, 2,097,152] and 100-5,000
@@ -589,12 +659,20 @@ def measure_served(args, dist: Dist, device: int) -> dict:
 def run_ours(args, dist: Dist):
     device, sms = _device_context(dist)
     peaks = measured_peaks()
-    parts = args.only.split(",") if args.only else ["direct", "bh", "ensemble", "served"]
+    parts = (args.only.split(",") if args.only
+             else ["direct", "bh", "ensemble", "served", "precision"])
     direct = measure_direct(args, dist, device, sms, peaks) if "direct" in parts else None
     bh = measure_bh(args, dist, device, sms, peaks) if "bh" in parts else None
     ens = measure_ensemble(args, dist, device) if "ensemble" in parts else None
     served = measure_served(args, dist, device) if "served" in parts else None
+    precision = measure_precision(args, dist, device) if "precision" in parts else None
     if dist.rank != 0:
+        return
+    if precision and not (direct or bh or ens or served):
+        print(json.dumps({"metric": "precision study (RMS relative acceleration error)",
+                          "value": precision["variants"]["fp32_compensated"]["acc_rms_rel_error"],
+                          "unit": "relative", "higher_is_better": False,
+                          "precision": precision}), flush=True)
         return
     if served and not (direct or bh or ens):
         print(json.dumps({"metric": served["metric"], "value": served["p50_s"], "unit": "s",
@@ -622,6 +700,8 @@ def run_ours(args, dist: Dist):
                 line[k] = direct[k]
     if served:
         line["served"] = served
+    if precision:
+        line["precision"] = precision
     if ens:
         line["ensemble"] = ens
         if not direct and not bh:

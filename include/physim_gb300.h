@@ -278,6 +278,24 @@ typedef struct PhysimTreeSnapshot {
 /* Builds the tree of the current state of an astro/astro2 simulation and
  * copies it out. */
 int physim_gpu_sim_tree_snapshot(PhysimSim *sim, PhysimTreeSnapshot *out);
+/* Whole-system diagnostics, summed in f64 on the device.  The potential is the
+ * one whose gradient is the reference's pair force G m_a m_b / (r^2 + e)
+ * (astro/src/lib.rs:84-113): V = -G m_a m_b atan(sqrt(e)/r)/sqrt(e), or
+ * -G m_a m_b / r for e = 0, over pairs at distinct positions (physim's debug
+ * energysink, debug/src/energysink.rs:35-99, reports K, V and dE with a
+ * 1/r potential). */
+typedef struct PhysimDiagnostics {
+    double mass;
+    double centre_of_mass[3];
+    double momentum[3];
+    double kinetic;
+    double potential; /* 0 unless requested (it is an O(N^2) pass) */
+    double energy;    /* kinetic + potential */
+} PhysimDiagnostics;
+
+/* Waits for the stream; with_potential != 0 also evaluates the potential. */
+int physim_gpu_sim_diagnostics(PhysimSim *sim, PhysimDiagnostics *out, int with_potential);
+
 /* Waits for the stream, then reports the most recent Barnes-Hut traversal:
  * node visits (one per warp and node), pair interactions (per body) and,
  * with profiling on, the traversal kernel's device time (else -1). */

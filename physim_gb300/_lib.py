@@ -68,6 +68,12 @@ class PhysimTreeSnapshot(C.Structure):
                 ("extent", C.c_double), ("flags", C.c_uint32)]
 
 
+class PhysimDiagnostics(C.Structure):
+    _fields_ = [("mass", C.c_double), ("centre_of_mass", C.c_double * 3),
+                ("momentum", C.c_double * 3), ("kinetic", C.c_double), ("potential", C.c_double),
+                ("energy", C.c_double)]
+
+
 class PhysimEnsembleTuning(C.Structure):
     _fields_ = [("block", C.c_uint32), ("ipt", C.c_uint32), ("chunk_bodies", C.c_uint32),
                 ("candidates", C.c_uint32), ("force_ms", C.c_double)]
@@ -102,6 +108,7 @@ def _load() -> C.CDLL:
         "physim_gpu_sim_set_profiling": (C.c_int, [vp, C.c_int]),
         "physim_gpu_sim_last_step_ms": (C.c_int, [vp, C.POINTER(dbl), C.POINTER(dbl)]),
         "physim_gpu_sim_destroy": (None, [vp]),
+        "physim_gpu_sim_diagnostics": (C.c_int, [vp, C.POINTER(PhysimDiagnostics), C.c_int]),
         "physim_gpu_sim_tree_snapshot": (C.c_int, [vp, C.POINTER(PhysimTreeSnapshot)]),
         "physim_gpu_sim_bh_stats": (C.c_int, [vp, C.POINTER(C.c_uint64),
                                               C.POINTER(C.c_uint64), C.POINTER(dbl)]),

@@ -92,6 +92,11 @@ int launch_verlet_aos(const Entity *d_in, const Entity *d_prev, Entity *d_out,
                       const Acceleration *d_acc, size_t n, double dt, bool initial,
                       cudaStream_t stream);
 
+// Whole-system f64 diagnostics into d_out[0..8]: mass, m*x, m*y, m*z,
+// m*vx, m*vy, m*vz, kinetic energy, potential energy (if `potential`).
+int launch_diagnostics(const DeviceBodies &b, double e, double *d_out, bool potential,
+                       int device, cudaStream_t stream);
+
 // Device count / SM count helpers (cached).
 int device_sm_count(int device);
 

@@ -38,6 +38,7 @@ struct PhysimSim {
     bool use_graph = true;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
+    double *diag = nullptr;  // 9 f64 diagnostics sums
 };
 
 struct PhysimVerlet {
@@ -321,6 +322,28 @@ int physim_gpu_sim_bh_stats(PhysimSim *s, uint64_t *node_visits, uint64_t *inter
     return PHYSIM_OK;
 }
 
+int physim_gpu_sim_diagnostics(PhysimSim *s, PhysimDiagnostics *out, int with_potential)
+{
+    PG_CHECK(s && out, PHYSIM_ERR_ARGUMENT, "null argument");
+    PG_CHECK(s->uploaded, PHYSIM_ERR_ARGUMENT, "diagnostics before upload");
+    PG_CUDA(cudaSetDevice(s->cfg.device));
+    if (!s->diag) PG_CUDA(cudaMalloc((void **)&s->diag, 9 * sizeof(double)));
+    PG_TRY(launch_diagnostics(s->b, s->cfg.e, s->diag, with_potential != 0, s->cfg.device,
+                              s->stream));
+    double h[9];
+    PG_CUDA(cudaMemcpyAsync(h, s->diag, sizeof h, cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    out->mass = h[0];
+    for (int c = 0; c < 3; ++c) {
+        out->centre_of_mass[c] = h[0] != 0.0 ? h[1 + c] / h[0] : 0.0;
+        out->momentum[c] = h[4 + c];
+    }
+    out->kinetic = h[7];
+    out->potential = with_potential ? h[8] : 0.0;
+    out->energy = out->kinetic + out->potential;
+    return PHYSIM_OK;
+}
+
 int physim_gpu_sim_synchronize(PhysimSim *s)
 {
     PG_CHECK(s, PHYSIM_ERR_ARGUMENT, "null simulation");
@@ -346,6 +369,7 @@ void physim_gpu_sim_destroy(PhysimSim *s)
     bodies_free(s->b);
     if (s->partial) cudaFree(s->partial);
     if (s->acc_soa) cudaFree(s->acc_soa);
+    if (s->diag) cudaFree(s->diag);
     bh_free(s->bh);
     if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
     if (s->graph) cudaGraphDestroy(s->graph);

@@ -102,6 +102,18 @@ class Simulation:
                 "com": com[:4 * m].reshape(m, 4), "n_nodes": int(s.n_nodes),
                 "extent": s.extent, "flags": int(s.flags)}
 
+    def diagnostics(self, potential: bool = False) -> dict:
+        """f64 mass, centre of mass, momentum, kinetic and (optionally) potential
+        energy of the current state."""
+        from ._lib import PhysimDiagnostics
+        d = PhysimDiagnostics()
+        check(lib.physim_gpu_sim_diagnostics(self.handle, C.byref(d), 1 if potential else 0),
+              "physim_gpu_sim_diagnostics")
+        return {"mass": d.mass, "centre_of_mass": list(d.centre_of_mass),
+                "momentum": list(d.momentum), "kinetic": d.kinetic,
+                "potential": d.potential if potential else None,
+                "energy": d.energy if potential else None}
+
     def bh_stats(self) -> dict:
         """Node visits and pair interactions of the most recent traversal."""
         v, i, t = C.c_uint64(), C.c_uint64(), C.c_double()
