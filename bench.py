@@ -411,11 +411,29 @@ def measure_bh(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict:
     stream = torch.cuda.Stream(device=device)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
     results = {}
-    for theta, steps in ((0.5, args.bh_steps), (1.0, max(args.bh_steps // 4, 10)),
-                         (1.5, max(args.bh_steps // 4, 10))):
+    # accuracy sample: RMS relative error of the initial accelerations against
+    # the f64 direct sum (the oracle) on 256 bodies
+    sample = np.sort(np.random.default_rng(5).choice(n, 256, replace=False))
+    exact = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        import oracle
+        ex = oracle.simple_astro_sample(state, E, sample)
+        exact = np.stack([ex["x"], ex["y"], ex["z"]], 1)
+    runs = [("0.5", 0.5, args.bh_steps, {}), ("1.0", 1.0, max(args.bh_steps // 4, 10), {}),
+            ("1.5", 1.5, max(args.bh_steps // 4, 10), {}),
+            ("0.5 quadrupole com_theta 0.6", 0.5, max(args.bh_steps // 4, 10),
+             {"quadrupole": True, "com_theta": 0.6})]
+    for name, theta, steps, extra in runs:
         sim = pg.Simulation(state, pg.SimConfig(gravity="astro2", theta=theta, e=E, dt=DT,
                                                 leaf_size=16, traversal="warp", device=device,
-                                                stream=stream.cuda_stream))
+                                                stream=stream.cuda_stream, **extra))
+        err = None
+        if exact is not None:
+            a = sim.accelerations()[sample]
+            got = np.stack([a["x"], a["y"], a["z"]], 1)
+            rel = np.linalg.norm(got - exact, axis=1) / np.linalg.norm(exact, axis=1)
+            err = {"rms_rel": float(np.sqrt(np.mean(rel ** 2))), "max_rel": float(rel.max()),
+                   "sample_bodies": len(sample)}
         sim.set_profiling(True)
         with torch.cuda.stream(stream):
             sim.step(max(args.warmup, 3))
@@ -424,15 +442,16 @@ def measure_bh(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict:
         step_ms, grav_ms = _timed_steps(sim, stream, steps, flush)
         total = dist.max(sum(step_ms))
         st = sim.bh_stats()
-        results[theta] = {"steps_per_s": dist.sum(float(steps)) / (total / 1e3),
-                          "ms_per_step": total / steps, "steps": steps,
-                          "gravity_ms": statistics.mean(grav_ms),
-                          "traversal_ms_last_step": st["traversal_ms"],
-                          "interactions_per_step": st["interactions"],
-                          "node_visits_per_step": st["node_visits"],
-                          "gpu_launches": sim.launches_per_step * steps}
+        results[name] = {"steps_per_s": dist.sum(float(steps)) / (total / 1e3),
+                         "ms_per_step": total / steps, "steps": steps,
+                         "gravity_ms": statistics.mean(grav_ms),
+                         "traversal_ms_last_step": st["traversal_ms"],
+                         "interactions_per_step": st["interactions"],
+                         "node_visits_per_step": st["node_visits"],
+                         "gpu_launches": sim.launches_per_step * steps,
+                         "acc_error_vs_f64": err}
         sim.close()
-    main = results[0.5]
+    main = results["0.5"]
     bytes_step = sum(BH_BYTES_PER_BODY.values()) * n
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     achieved = bytes_step / (main["ms_per_step"] / 1e3) / 1e9
@@ -443,7 +462,7 @@ def measure_bh(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict:
                    if trav_ms and trav_ms > 0 else None)
     out = {"metric": "BH steps/s at N=1M (astro2, theta 0.5, leaf 16, warp traversal)",
            "value": main["steps_per_s"], "unit": "steps/s", "ms_per_step": main["ms_per_step"],
-           "bodies": n, "theta": {str(k): v for k, v in results.items()},
+           "bodies": n, "theta": results,
            "roofline": {"bound": "hbm", "kernel": "whole step", "achieved": achieved,
                         "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
                         "algorithmic_bytes_per_body": BH_BYTES_PER_BODY,
@@ -625,7 +644,8 @@ def measure_served(args, dist: Dist, device: int) -> dict:
     steps, admitted by a 150 GB HBM budget and run with continuous batching.
     Arrivals for --serve-seconds, then up to --serve-drain seconds to finish;
     jobs still queued or running at the cut-off are reported as unfinished."""
-    from physim_gb300.server import GpuExecutor, Server, latency_summary, served_mix
+    from physim_gb300.server import (GpuExecutor, PlainExecutor, Server, latency_summary,
+                                     served_mix)
 
     jobs = served_mix(rate=50.0, seconds=args.serve_seconds, seed=5)
     srv = Server(GpuExecutor(device=device, tick_ms=25.0, download=True),
@@ -636,6 +656,16 @@ def measure_served(args, dist: Dist, device: int) -> dict:
     wall = time.perf_counter() - t0
     unfinished = srv.unfinished()
     srv.close()
+    # the same arrivals, one job at a time through the plain per-simulation
+    # kernels (100 ms ticks), over the same window
+    plain = Server(PlainExecutor(device=device, download=True), hbm_budget=150 << 30,
+                   max_units=1, max_batch=1)
+    plain.submit(served_mix(rate=50.0, seconds=args.serve_seconds, seed=5))
+    t1 = time.perf_counter()
+    plain_res = plain.run(until=args.serve_seconds + args.serve_drain)
+    plain_wall = time.perf_counter() - t1
+    plain.close()
+    plain_lat = latency_summary(plain_res)
     offered_direct = sum(j.n * j.n * j.steps for j in jobs if j.gravity == "simple_astro")
     lat = latency_summary(res)
     depth = srv.queue_depth
@@ -651,6 +681,14 @@ def measure_served(args, dist: Dist, device: int) -> dict:
             "max_hbm_in_use_gb": max((d[3] for d in depth), default=0) / 2**30,
             "queue_depth_samples": [(round(t, 2), w, r) for t, w, r, _ in depth[::8]],
             "offered_direct_pairs": offered_direct,
+            "plain_one_at_a_time": {
+                "aggregate_steps_per_s": plain.steps_executed / plain_wall,
+                "completed": len(plain_res), "p50_s": plain_lat.get("p50_s"),
+                "p99_s": plain_lat.get("p99_s"), "wall_s": plain_wall,
+                "path": "each job alone as a device-resident simulation (direct or "
+                        "Barnes-Hut), in arrival order, 100 ms ticks"},
+            "speedup_vs_plain": (srv.steps_executed / wall) /
+                                max(plain.steps_executed / plain_wall, 1e-9),
             "note": "offered load far exceeds one GPU (the direct-sum jobs alone are "
                     f"{offered_direct / 2.3e12:.0f} GPU-seconds at 2.3e12 pairs/s); latency "
                     "is dominated by backlog"}

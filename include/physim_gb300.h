@@ -13,8 +13,8 @@
  *     names, properties (`theta`, `e`) and the Entity layout are unchanged, so
  *     pipeline TOML files and CLI strings load it unchanged.
  *
- *  2. A device-resident C API (physim_gpu_*): the verlet integrator
- *     (integrators/src/verlet.rs) over host arrays, and simulations whose
+ *  2. A device-resident C API (physim_gpu_*): the verlet, euler and rk4
+ *     integrators (integrators/src/) over host arrays, and simulations whose
  *     state stays in HBM between steps.
  *
  * Types below have the layout of c_plugin/physim.h:6-94 (same type names;
@@ -142,6 +142,10 @@ void set_callback_target(void *target);
  *    traversal  ("exact": each body uses its own reference interaction list,
  *                the default; "warp": a cell is accepted only when every body
  *                of a 32-body warp accepts it)
+ *    quadrupole (astro, astro2; true adds the cells' quadrupole moments;
+ *                default false = the reference's monopole pseudo-particles)
+ *    com_theta  (astro, astro2; > 0 also requires b_max < com_theta |x - c|
+ *                to accept a cell, see PhysimSimConfig; default 0 = off)
  *    device     (CUDA device ordinal, default 0)
  *  Returns NULL for text that is not a JSON object (transform.rs:72-76).  It
  *  does not touch the GPU; the CUDA context is created by the first transform.
@@ -210,6 +214,19 @@ typedef enum PhysimTraversal {
     PHYSIM_TRAVERSAL_WARP = 1   /* a cell is accepted only if the whole warp accepts it */
 } PhysimTraversal;
 
+/* Cell expansion order of the Barnes-Hut force. */
+typedef enum PhysimMultipole {
+    PHYSIM_MULTIPOLE_MONOPOLE = 0,  /* the reference's pseudo-particle (astro/src/lib.rs:64-76) */
+    PHYSIM_MULTIPOLE_QUADRUPOLE = 1 /* + second moments about the centre of mass */
+} PhysimMultipole;
+
+/* Integrator elements, by the reference's element names. */
+typedef enum PhysimIntegratorKind {
+    PHYSIM_INTEGRATOR_VERLET = 0, /* integrators/src/verlet.rs:19-121 (position Verlet) */
+    PHYSIM_INTEGRATOR_EULER = 1,  /* integrators/src/euler.rs:11-49 (Taylor step) */
+    PHYSIM_INTEGRATOR_RK4 = 2     /* integrators/src/rk4.rs:11-178 (4 force evaluations) */
+} PhysimIntegratorKind;
+
 /* Settings of one device-resident simulation. */
 typedef struct PhysimSimConfig {
     uint32_t gravity;     /* PhysimGravity */
@@ -218,14 +235,21 @@ typedef struct PhysimSimConfig {
     uint32_t compensated; /* 1: FP32 pairs, compensated per-body sums; 0: plain FP32 sums */
     double theta;         /* opening parameter: extent/r < theta accepts a cell */
     double e;             /* easing factor added to r^2 (astro/src/lib.rs:95-98) */
-    double dt;            /* verlet time step */
+    double dt;            /* integrator time step */
     void *stream;         /* cudaStream_t to run on; NULL: the simulation makes its own */
     int32_t device;       /* CUDA device ordinal */
-    uint32_t reserved[3]; /* must be zero */
+    uint32_t integrator;  /* PhysimIntegratorKind */
+    /* Accuracy options of astro/astro2 beyond the reference (0 = off, the
+     * reference's monopole cells and opening rule): */
+    uint32_t multipole;   /* PhysimMultipole */
+    float com_theta;      /* also require b_max < com_theta * |x - c| to accept a
+                           * cell (c its centre of mass, b_max = sqrt(3) extent +
+                           * |c - centre| bounds its bodies' distance from c) */
 } PhysimSimConfig;
 
 /* Fills *cfg with the reference's defaults: simple_astro, theta 1.0, e 1.0,
- * dt 1e-6 (pipeline.rs:334), leaf 1, exact traversal, compensated sums. */
+ * dt 1e-6 (pipeline.rs:334), leaf 1, exact traversal, compensated sums,
+ * verlet, monopole cells, no centre-of-mass guard. */
 void physim_gpu_sim_config_default(PhysimSimConfig *cfg);
 
 typedef struct PhysimSim PhysimSim;
@@ -235,10 +259,16 @@ int physim_gpu_sim_create(const PhysimSimConfig *cfg, size_t n, PhysimSim **out)
 /* Copies the host state in and clears the verlet history, so the next step
  * is the reference's Taylor first step (verlet.rs:24-50). */
 int physim_gpu_sim_upload(PhysimSim *sim, const Entity *state, size_t n);
-/* Enqueues `steps` pipeline steps (gravity, then verlet), asynchronously on
- * the simulation's stream. */
+/* Enqueues `steps` pipeline steps, asynchronously on the simulation's stream:
+ * gravity then the integrator's update; rk4 evaluates gravity four times per
+ * step, at the stage states (rk4.rs:33-112).  Updates are f64 in the
+ * reference's operation order, so given the same accelerations the new state
+ * is bit-identical to the reference integrator's. */
 int physim_gpu_sim_step(PhysimSim *sim, uint32_t steps);
-/* Waits for the stream, then copies the current state out. */
+/* Waits for the stream, then copies the current state out.  This call, sim_accelerations
+ * and sim_synchronize report a Barnes-Hut traversal stack overflow
+ * (PHYSIM_ERR_TREE) or a radix-sort wait that gave up (PHYSIM_ERR_TIMEOUT) raised by
+ * the kernels since the last check. */
 int physim_gpu_sim_download(PhysimSim *sim, Entity *state, size_t n);
 /* Waits, then writes the accelerations of the current state (not +=). */
 int physim_gpu_sim_accelerations(PhysimSim *sim, Acceleration *acc, size_t n);
@@ -269,10 +299,13 @@ typedef struct PhysimTreeSnapshot {
     uint8_t *node_level;   /* [cap] depth below the root */
     double *node_centre;   /* [4*m] planes cx, cy, cz, half-width; m = min(n_nodes, cap) */
     float *node_com;       /* [4*cap] centre of mass x, y, z and mass, per node */
+    float *node_quad;      /* [8*m] second moments about the centre of mass (quadrupole
+                            * builds): m x (Sxx, Syy, Szz, trace), then m x (Sxy, Sxz, Syz, 0) */
     size_t n_bodies;       /* out */
     size_t n_nodes;        /* out: nodes in the tree */
     double extent;         /* out: root half-width X (transformers.rs:126-132) */
-    uint32_t flags;        /* out: bit 0 node arrays full (tree truncated), bit 1 stack overflow */
+    uint32_t flags;        /* out: bit 0 node arrays full (tree truncated), bit 1 stack
+                            * overflow, bit 2 radix-sort look-back wait gave up */
 } PhysimTreeSnapshot;
 
 /* Builds the tree of the current state of an astro/astro2 simulation and
@@ -366,6 +399,24 @@ int physim_gpu_verlet_create(int32_t device, PhysimVerlet **out);
 int physim_gpu_verlet_integrate(PhysimVerlet *v, const Entity *entities, Entity *new_state,
                                 size_t n, const Acceleration *acc, double dt);
 void physim_gpu_verlet_destroy(PhysimVerlet *v);
+
+/* Any of the three integrators over host arrays, in the shape of physim's
+ * IntegratorElement::integrate(entities, new_state, acc_fn, dt)
+ * (physim-core/src/plugin/integrator.rs:5-13): the library calls acc_fn once
+ * (verlet, euler) or four times (rk4) with a host state and zeroed host
+ * accelerations that acc_fn adds into (physim's transform_fn,
+ * pipeline.rs:137-141), and computes the stage states and the update on the
+ * GPU in f64 in the reference's operation order.  This is what a Rust
+ * IntegratorElement shim for `verlet`, `euler` or `rk4` binds
+ * (verlet_create_element etc., physim-attribute/src/lib.rs:384-427).
+ * verlet keeps previous_state on the device between calls (verlet.rs:102). */
+typedef void (*PhysimAccFn)(void *user, const Entity *state, size_t n, Acceleration *acc);
+typedef struct PhysimIntegrator PhysimIntegrator;
+int physim_gpu_integrator_create(uint32_t kind, int32_t device, PhysimIntegrator **out);
+int physim_gpu_integrator_integrate(PhysimIntegrator *it, const Entity *entities,
+                                    Entity *new_state, size_t n, PhysimAccFn acc_fn, void *user,
+                                    double dt);
+void physim_gpu_integrator_destroy(PhysimIntegrator *it);
 
 #ifdef __cplusplus
 }

@@ -72,11 +72,15 @@ def load() -> C.CDLL:
         "oracle_verlet_free": (None, [vp]),
         "oracle_verlet_step": (i32, [vp, vp, vp, sz, vp, dbl]),
         "oracle_run_pipeline": (i32, [vp, sz, i32, dbl, dbl, dbl, i32, i32]),
+        "oracle_run_pipeline_with": (i32, [vp, sz, i32, i32, dbl, dbl, dbl, i32, i32]),
+        "oracle_euler_step": (None, [vp, vp, sz, vp, dbl]),
+        "oracle_rk4_step": (i32, [vp, vp, sz, vp, vp, dbl]),
         "oracle_max_threads": (i32, []),
         "oracle_tree_dump": (sz, [vp, vp, vp, sz]),
         "bh_model_extent": (dbl, [vp, sz]),
         "bh_model_keys": (None, [vp, sz, i32, vp]),
         "bh_model_build": (C.c_long, [vp, sz, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, sz]),
+        "bh_model_accel": (i32, [vp, sz, i32, i32, dbl, dbl, i32, dbl, vp, sz, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -160,16 +164,53 @@ def barnes_hut(state: np.ndarray, theta: float, e: float, nchild: int = 8,
     return out
 
 
+INTEGRATORS = {"verlet": 0, "euler": 1, "rk4": 2}
+
+
 def run_pipeline(state: np.ndarray, element: str, steps: int, dt: float, e: float,
-                 theta: float = 1.0, threads: int = 0) -> np.ndarray:
-    """pipeline.rs loop with one gravity element + verlet; returns the final state."""
+                 theta: float = 1.0, threads: int = 0, integrator: str = "verlet") -> np.ndarray:
+    """pipeline.rs loop with one gravity element + one integrator (verlet,
+    euler or rk4); returns the final state."""
     lib = load()
     s = np.array(_ent(state), copy=True)
     code = {"simple_astro": 0, "astro2": 1, "astro": 2}[element]
-    st = lib.oracle_run_pipeline(s.ctypes.data, len(s), code, theta, e, dt, steps, threads)
+    st = lib.oracle_run_pipeline_with(s.ctypes.data, len(s), code, INTEGRATORS[integrator],
+                                      theta, e, dt, steps, threads)
     if st != 0:
         raise RuntimeError(f"reference tree panics (status {st})")
     return s
+
+
+def euler_step(entities: np.ndarray, acc: np.ndarray, dt: float) -> np.ndarray:
+    """euler.rs:17-49 given the accelerations acc_fn produced."""
+    lib = load()
+    entities, acc = _ent(entities), _acc(acc)
+    out = np.empty_like(entities)
+    lib.oracle_euler_step(entities.ctypes.data, out.ctypes.data, len(entities), acc.ctypes.data,
+                          dt)
+    return out
+
+
+ACC_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p)
+
+
+def rk4_step(entities: np.ndarray, acc_fn, dt: float) -> np.ndarray:
+    """rk4.rs:24-178 with a Python acc_fn(state, acc) that adds into acc."""
+    from physim_gb300.entity import ACCELERATION, ENTITY
+    lib = load()
+    entities = _ent(entities)
+    out = np.empty_like(entities)
+
+    def cb(_user, sp, n, ap):
+        st = np.ctypeslib.as_array(C.cast(sp, C.POINTER(C.c_uint8)), (n * ENTITY.itemsize,))
+        ac = np.ctypeslib.as_array(C.cast(ap, C.POINTER(C.c_uint8)), (n * 24,))
+        acc_fn(st.view(ENTITY), ac.view(ACCELERATION))
+
+    fn = ACC_FN(cb)
+    if lib.oracle_rk4_step(entities.ctypes.data, out.ctypes.data, len(entities),
+                           C.cast(fn, C.c_void_p), None, dt) != 0:
+        raise MemoryError("rk4 oracle: out of memory")
+    return out
 
 
 class Verlet:
@@ -253,3 +294,19 @@ def bh_model(state: np.ndarray, nchild: int = 8, leaf: int = 16) -> dict:
     return {"keys": keys, "order": order, "begin": nb[:m], "count": nc[:m], "child": ch[:m],
             "nchild": nn[:m], "level": lvl[:m], "centre": cen,
             "extent": lib.bh_model_extent(state.ctypes.data, n)}
+
+
+def bh_model_accel(state: np.ndarray, theta: float, e: float, idx: np.ndarray, nchild: int = 8,
+                   leaf: int = 16, quad: bool = False, com_theta: float = 0.0) -> np.ndarray:
+    """f64 model of the GPU traversal's accuracy options (per-body rule): the
+    reference's opening rule, optionally the centre-of-mass guard and the
+    quadrupole term, over the model tree.  Returns (len(idx), 3)."""
+    lib = load()
+    state = _ent(state)
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    out = np.zeros((len(idx), 3))
+    if lib.bh_model_accel(state.ctypes.data, len(state), nchild, leaf, theta, e,
+                          1 if quad else 0, com_theta, idx.ctypes.data, len(idx),
+                          out.ctypes.data) != 0:
+        raise MemoryError("bh_model_accel: out of memory")
+    return out

@@ -170,3 +170,138 @@ long bh_model_build(const BhEntity *s, size_t n, int nchild, int leaf, uint64_t 
     }
     return (long)total;
 }
+
+/* ------------------------------------------------------------------------ */
+/* The accuracy options of the GPU traversal (not reference behaviour), in   */
+/* f64, per body: a cell is accepted when the reference's rule               */
+/* extent / |x - centre| < theta holds (astro/src/octree.rs:137-144) and,    */
+/* with com_theta > 0, b_max < com_theta |x - c| with c the cell's centre of */
+/* mass and b_max = sqrt(3) extent + |c - centre|.  Accepted cells add their */
+/* monopole and, with quad != 0, the quadrupole term of the reference law    */
+/* a = sum m d / (|d| (|d|^2 + e)) expanded about c (second moments S about  */
+/* c):  a_2 = h S D + (h tr S + (h'/r) D.S.D) D / 2, D = c - x,              */
+/* h = g'/r, g(r) = 1/(r (r^2 + e)).  Opened leaves add their bodies         */
+/* exactly, skipping bodies at the same position.  out[k] = acceleration of  */
+/* body idx[k].  Returns 0, or -1 when out of memory.                         */
+/* ------------------------------------------------------------------------ */
+static void model_pair(const double x[3], const double p[3], double m, double e, double a[3])
+{
+    const double d0 = p[0] - x[0], d1 = p[1] - x[1], d2 = p[2] - x[2];
+    const double r2 = d0 * d0 + d1 * d1 + d2 * d2;
+    if (r2 == 0.0) return;
+    const double f = m / (sqrt(r2) * (r2 + e));
+    a[0] += d0 * f;
+    a[1] += d1 * f;
+    a[2] += d2 * f;
+}
+
+int bh_model_accel(const BhEntity *s, size_t n, int nchild, int leaf, double theta, double e,
+                   int quad, double com_theta, const int64_t *idx, size_t n_idx, double *out)
+{
+    const size_t cap = 4 * (n > 64 ? n : 64) + 64 * 31;
+    uint64_t *keys = malloc((n ? n : 1) * sizeof *keys);
+    uint32_t *order = malloc((n ? n : 1) * sizeof *order);
+    int32_t *nb = malloc(cap * sizeof *nb), *nc = malloc(cap * sizeof *nc);
+    int32_t *ch = malloc(cap * sizeof *ch);
+    uint8_t *nn = malloc(cap), *lvl = malloc(cap);
+    double *cen = malloc(4 * cap * sizeof *cen);
+    double *mom = malloc(10 * cap * sizeof *mom); /* M, cx, cy, cz, Sxx Syy Szz Sxy Sxz Syz */
+    int64_t *rank = malloc((n ? n : 1) * sizeof *rank);
+    int32_t *stack = malloc(cap * sizeof *stack);
+    int rc = -1;
+    if (!keys || !order || !nb || !nc || !ch || !nn || !lvl || !cen || !mom || !rank || !stack)
+        goto done;
+    long total = bh_model_build(s, n, nchild, leaf, keys, order, nb, nc, ch, nn, lvl, cen, cap);
+    if (total < 0) goto done;
+    for (size_t k = 0; k < n; ++k) rank[order[k]] = (int64_t)k;
+    /* moments by direct summation over each node's sorted bodies */
+    for (long i = 0; i < total; ++i) {
+        double M = 0, c[3] = {0, 0, 0};
+        for (int32_t j = nb[i]; j < nb[i] + nc[i]; ++j) {
+            const BhEntity *b = &s[order[j]];
+            M += b->mass;
+            c[0] += b->mass * b->x;
+            c[1] += b->mass * b->y;
+            c[2] += b->mass * b->z;
+        }
+        if (M != 0.0)
+            for (int a = 0; a < 3; ++a) c[a] /= M;
+        else
+            for (int a = 0; a < 3; ++a) c[a] = cen[a * cap + i];
+        double S[6] = {0, 0, 0, 0, 0, 0};
+        for (int32_t j = nb[i]; j < nb[i] + nc[i]; ++j) {
+            const BhEntity *b = &s[order[j]];
+            const double dx = b->x - c[0], dy = b->y - c[1], dz = b->z - c[2];
+            S[0] += b->mass * dx * dx;
+            S[1] += b->mass * dy * dy;
+            S[2] += b->mass * dz * dz;
+            S[3] += b->mass * dx * dy;
+            S[4] += b->mass * dx * dz;
+            S[5] += b->mass * dy * dz;
+        }
+        double *o = &mom[10 * i];
+        o[0] = M;
+        o[1] = c[0];
+        o[2] = c[1];
+        o[3] = c[2];
+        for (int a = 0; a < 6; ++a) o[4 + a] = S[a];
+    }
+    for (size_t k = 0; k < n_idx; ++k) {
+        const BhEntity *bi = &s[idx[k]];
+        const double x[3] = {bi->x, bi->y, bi->z};
+        double a[3] = {0, 0, 0};
+        size_t sp = 0;
+        if (n) stack[sp++] = 0;
+        while (sp) {
+            const int32_t i = stack[--sp];
+            const double *o = &mom[10 * i];
+            const double g0 = x[0] - cen[i], g1 = x[1] - cen[cap + i], g2 = x[2] - cen[2 * cap + i];
+            const double r = sqrt(g0 * g0 + g1 * g1 + g2 * g2);
+            const double ext = cen[3 * cap + i];
+            int accept = ext / r < theta;
+            if (accept && com_theta > 0.0) {
+                const double o0 = o[1] - cen[i], o1 = o[2] - cen[cap + i], o2 = o[3] - cen[2 * cap + i];
+                const double bmax = sqrt(3.0) * ext + sqrt(o0 * o0 + o1 * o1 + o2 * o2);
+                const double D0 = o[1] - x[0], D1 = o[2] - x[1], D2 = o[3] - x[2];
+                accept = bmax < com_theta * sqrt(D0 * D0 + D1 * D1 + D2 * D2);
+            }
+            if (accept) {
+                model_pair(x, &o[1], o[0], e, a);
+                if (quad) {
+                    const double D0 = o[1] - x[0], D1 = o[2] - x[1], D2 = o[3] - x[2];
+                    const double r2 = D0 * D0 + D1 * D1 + D2 * D2;
+                    if (r2 > 0.0) {
+                        const double rr = sqrt(r2), u = rr * (r2 + e), A = 3.0 * r2 + e;
+                        const double h = -A / (rr * u * u);
+                        const double hp = (-6.0 / (u * u) + A * (u + 2.0 * rr * A) / (r2 * u * u * u)) / rr;
+                        const double *S = &o[4];
+                        const double sd0 = S[0] * D0 + S[3] * D1 + S[4] * D2;
+                        const double sd1 = S[3] * D0 + S[1] * D1 + S[5] * D2;
+                        const double sd2 = S[4] * D0 + S[5] * D1 + S[2] * D2;
+                        const double dsd = D0 * sd0 + D1 * sd1 + D2 * sd2;
+                        const double kk = 0.5 * (h * (S[0] + S[1] + S[2]) + hp * dsd);
+                        a[0] += h * sd0 + kk * D0;
+                        a[1] += h * sd1 + kk * D1;
+                        a[2] += h * sd2 + kk * D2;
+                    }
+                }
+            } else if (ch[i] < 0) {
+                for (int32_t j = nb[i]; j < nb[i] + nc[i]; ++j) {
+                    const BhEntity *b = &s[order[j]];
+                    const double p[3] = {b->x, b->y, b->z};
+                    model_pair(x, p, b->mass, e, a);
+                }
+            } else {
+                for (int c = 0; c < nn[i]; ++c) stack[sp++] = ch[i] + c;
+            }
+        }
+        out[3 * k] = a[0];
+        out[3 * k + 1] = a[1];
+        out[3 * k + 2] = a[2];
+    }
+    rc = 0;
+done:
+    free(keys); free(order); free(nb); free(nc); free(ch); free(nn); free(lvl);
+    free(cen); free(mom); free(rank); free(stack);
+    return rc;
+}

@@ -19,6 +19,8 @@
  *   astro           astro/src/transformers.rs:31-69
  *   simple_astro    astro/src/transformers.rs:219-244
  *   verlet          integrators/src/verlet.rs:24-107
+ *   euler           integrators/src/euler.rs:17-49
+ *   rk4             integrators/src/rk4.rs:24-178
  *   pipeline step   physim-core/src/pipeline.rs:137-141,166-173
  *
  * Parity status: the reference is Rust and cannot be built here, and its own
@@ -503,35 +505,192 @@ int oracle_verlet_step(Verlet *v, const Entity *entities, Entity *new_state, siz
 }
 
 /* ------------------------------------------------------------------------ */
-/* Pipeline loop (pipeline.rs:137-141,166-173) with one gravity transform    */
-/* and the verlet integrator.  element: 0 simple_astro, 1 astro2, 2 astro.   */
-/* state is advanced in place by `steps` steps.  Returns 0 or a panic status. */
+/* Euler (integrators/src/euler.rs:17-49): one acc_fn call, the Taylor step  */
+/* x + v dt + 0.5 a dt^2, v + a dt for every body (fixed ones included).     */
 /* ------------------------------------------------------------------------ */
-int oracle_run_pipeline(Entity *state, size_t n, int element, double theta, double e, double dt,
-                        int steps, int threads)
+void oracle_euler_step(const Entity *entities, Entity *new_state, size_t n, const Acceleration *a,
+                       double dt)
+{
+    double dt2 = dt * dt; /* dt.powi(2) */
+    for (size_t i = 0; i < n; ++i) {
+        const Entity *en = &entities[i];
+        Entity ne = *en;
+        ne.x = en->x + en->vx * dt + 0.5 * a[i].x * dt2;
+        ne.y = en->y + en->vy * dt + 0.5 * a[i].y * dt2;
+        ne.z = en->z + en->vz * dt + 0.5 * a[i].z * dt2;
+        ne.vx = en->vx + a[i].x * dt;
+        ne.vy = en->vy + a[i].y * dt;
+        ne.vz = en->vz + a[i].z * dt;
+        new_state[i] = ne;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* RK4 (integrators/src/rk4.rs:24-178): four acc_fn calls per step, at the   */
+/* state, at state + k1/2, at state + k2/2 and at state + k3, where          */
+/* k = (dt v, dt a) of the stage state.  The combination is evaluated left   */
+/* to right, (k1 + 2 k2 + 2 k3 + k4) / 6, as the reference writes it; fixed  */
+/* bodies keep their position and get zero velocity (rk4.rs:165-171).       */
+/* acc_fn receives zeroed accelerations (rk4.rs:33,57,82,108).               */
+/* ------------------------------------------------------------------------ */
+typedef void (*oracle_acc_fn)(void *user, const Entity *state, size_t n, Acceleration *acc);
+
+typedef struct Stage6 {
+    double x, y, z, vx, vy, vz;
+} Stage6;
+
+/* k of a stage state and its accelerations (rk4.rs:36-47 and the later copies) */
+static void rk4_k(const Entity *t, const Acceleration *f, size_t n, double dt, Stage6 *k)
+{
+    for (size_t i = 0; i < n; ++i) {
+        k[i].x = dt * t[i].vx;
+        k[i].y = dt * t[i].vy;
+        k[i].z = dt * t[i].vz;
+        k[i].vx = dt * f[i].x;
+        k[i].vy = dt * f[i].y;
+        k[i].vz = dt * f[i].z;
+    }
+}
+
+/* the next stage state: entities + c k (rk4.rs:50-62, c = 0.5 or 1) */
+static void rk4_shift(const Entity *e, const Stage6 *k, size_t n, int half, Entity *t)
+{
+    for (size_t i = 0; i < n; ++i) {
+        t[i] = e[i];
+        if (half) {
+            t[i].x = e[i].x + 0.5 * k[i].x;
+            t[i].y = e[i].y + 0.5 * k[i].y;
+            t[i].z = e[i].z + 0.5 * k[i].z;
+            t[i].vx = e[i].vx + 0.5 * k[i].vx;
+            t[i].vy = e[i].vy + 0.5 * k[i].vy;
+            t[i].vz = e[i].vz + 0.5 * k[i].vz;
+        } else {
+            t[i].x = e[i].x + k[i].x;
+            t[i].y = e[i].y + k[i].y;
+            t[i].z = e[i].z + k[i].z;
+            t[i].vx = e[i].vx + k[i].vx;
+            t[i].vy = e[i].vy + k[i].vy;
+            t[i].vz = e[i].vz + k[i].vz;
+        }
+    }
+}
+
+int oracle_rk4_step(const Entity *entities, Entity *new_state, size_t n, oracle_acc_fn acc_fn,
+                    void *user, double dt)
+{
+    size_t m = n ? n : 1;
+    Acceleration *f = (Acceleration *)calloc(m, sizeof(Acceleration));
+    Entity *t = (Entity *)malloc(m * sizeof(Entity));
+    Stage6 *k1 = (Stage6 *)malloc(m * sizeof(Stage6));
+    Stage6 *k2 = (Stage6 *)malloc(m * sizeof(Stage6));
+    Stage6 *k3 = (Stage6 *)malloc(m * sizeof(Stage6));
+    Stage6 *k4 = (Stage6 *)malloc(m * sizeof(Stage6));
+    if (!f || !t || !k1 || !k2 || !k3 || !k4) {
+        free(f); free(t); free(k1); free(k2); free(k3); free(k4);
+        return 1;
+    }
+    acc_fn(user, entities, n, f);
+    rk4_k(entities, f, n, dt, k1);
+    rk4_shift(entities, k1, n, 1, t);
+    memset(f, 0, m * sizeof(Acceleration));
+    acc_fn(user, t, n, f);
+    rk4_k(t, f, n, dt, k2);
+    rk4_shift(entities, k2, n, 1, t);
+    memset(f, 0, m * sizeof(Acceleration));
+    acc_fn(user, t, n, f);
+    rk4_k(t, f, n, dt, k3);
+    rk4_shift(entities, k3, n, 0, t);
+    memset(f, 0, m * sizeof(Acceleration));
+    acc_fn(user, t, n, f);
+    rk4_k(t, f, n, dt, k4);
+    for (size_t i = 0; i < n; ++i) {
+        const Entity *e = &entities[i];
+        Entity *ns = &new_state[i];
+        if (!e->fixed) {
+            ns->x = e->x + (k1[i].x + 2.0 * k2[i].x + 2.0 * k3[i].x + k4[i].x) / 6.0;
+            ns->y = e->y + (k1[i].y + 2.0 * k2[i].y + 2.0 * k3[i].y + k4[i].y) / 6.0;
+            ns->z = e->z + (k1[i].z + 2.0 * k2[i].z + 2.0 * k3[i].z + k4[i].z) / 6.0;
+            ns->vx = e->vx + (k1[i].vx + 2.0 * k2[i].vx + 2.0 * k3[i].vx + k4[i].vx) / 6.0;
+            ns->vy = e->vy + (k1[i].vy + 2.0 * k2[i].vy + 2.0 * k3[i].vy + k4[i].vy) / 6.0;
+            ns->vz = e->vz + (k1[i].vz + 2.0 * k2[i].vz + 2.0 * k3[i].vz + k4[i].vz) / 6.0;
+        } else {
+            ns->x = e->x;
+            ns->y = e->y;
+            ns->z = e->z;
+            ns->vx = 0.0;
+            ns->vy = 0.0;
+            ns->vz = 0.0;
+        }
+        ns->mass = e->mass;
+        ns->radius = e->radius;
+        ns->id = e->id;
+        ns->fixed = e->fixed;
+    }
+    free(f); free(t); free(k1); free(k2); free(k3); free(k4);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Pipeline loop (pipeline.rs:137-141,166-173) with one gravity transform    */
+/* and one integrator.  element: 0 simple_astro, 1 astro2, 2 astro;          */
+/* integrator: 0 verlet, 1 euler, 2 rk4.  state is advanced in place by      */
+/* `steps` steps.  Returns 0 or a panic status.                              */
+/* ------------------------------------------------------------------------ */
+typedef struct GravityFn {
+    int element;
+    double theta, e;
+    int threads;
+    const int64_t *all;
+    int status;
+} GravityFn;
+
+/* transform_fn (pipeline.rs:137-141) with the single gravity element */
+static void gravity_acc(void *user, const Entity *state, size_t n, Acceleration *acc)
+{
+    GravityFn *g = (GravityFn *)user;
+    if (g->status) return;
+    if (g->element == 0)
+        oracle_simple_astro_sample(state, n, g->e, g->all, n, acc, g->threads);
+    else
+        g->status = oracle_barnes_hut(g->element == 1 ? 8 : 4, state, n, g->theta, g->e, NULL, 0,
+                                      acc, g->threads);
+}
+
+int oracle_run_pipeline_with(Entity *state, size_t n, int element, int integrator, double theta,
+                             double e, double dt, int steps, int threads)
 {
     Verlet *v = oracle_verlet_new();
     Entity *new_state = (Entity *)malloc((n ? n : 1) * sizeof(Entity));
     Acceleration *acc = (Acceleration *)malloc((n ? n : 1) * sizeof(Acceleration));
     int64_t *all = (int64_t *)malloc((n ? n : 1) * sizeof(int64_t));
     for (size_t i = 0; i < n; ++i) all[i] = (int64_t)i;
-    int st = 0;
-    for (int s = 0; s < steps && st == 0; ++s) {
-        memset(acc, 0, n * sizeof(Acceleration));
-        if (element == 0) {
-            oracle_simple_astro_sample(state, n, e, all, n, acc, threads);
+    GravityFn g = {element, theta, e, threads, all, 0};
+    for (int s = 0; s < steps && g.status == 0; ++s) {
+        if (integrator == 2) {
+            if (oracle_rk4_step(state, new_state, n, gravity_acc, &g, dt)) g.status = 1;
         } else {
-            st = oracle_barnes_hut(element == 1 ? 8 : 4, state, n, theta, e, NULL, 0, acc, threads);
+            memset(acc, 0, n * sizeof(Acceleration));
+            gravity_acc(&g, state, n, acc);
+            if (g.status) break;
+            if (integrator == 1)
+                oracle_euler_step(state, new_state, n, acc, dt);
+            else
+                oracle_verlet_step(v, state, new_state, n, acc, dt);
         }
-        if (st) break;
-        oracle_verlet_step(v, state, new_state, n, acc, dt);
+        if (g.status) break;
         memcpy(state, new_state, n * sizeof(Entity));
     }
     free(all);
     free(acc);
     free(new_state);
     oracle_verlet_free(v);
-    return st;
+    return g.status;
+}
+
+int oracle_run_pipeline(Entity *state, size_t n, int element, double theta, double e, double dt,
+                        int steps, int threads)
+{
+    return oracle_run_pipeline_with(state, n, element, 0, theta, e, dt, steps, threads);
 }
 
 /* Number of OpenMP threads this build would use (1 without OpenMP). */

@@ -9,12 +9,13 @@ loudly if the library is missing; there is no CPU fallback.
 """
 from ._lib import LIB_PATH, PhysimError, last_error, lib
 from .entity import ACCELERATION, ENTITY, accelerations, entities, entity_new
-from .plugin import GpuVerlet, NullElement, Pipeline, TransformElementHandler, register
+from .plugin import (GpuIntegrator, GpuVerlet, NullElement, Pipeline, TransformElementHandler,
+                     register)
 from .sim import SimConfig, Simulation
 from .ensemble import Ensemble
 
 __all__ = [
     "LIB_PATH", "PhysimError", "last_error", "lib", "ACCELERATION", "ENTITY", "accelerations",
-    "entities", "entity_new", "GpuVerlet", "NullElement", "Pipeline", "TransformElementHandler",
-    "register", "SimConfig", "Simulation", "Ensemble",
+    "entities", "entity_new", "GpuIntegrator", "GpuVerlet", "NullElement", "Pipeline",
+    "TransformElementHandler", "register", "SimConfig", "Simulation", "Ensemble",
 ]

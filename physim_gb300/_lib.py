@@ -24,6 +24,11 @@ GRAVITY_ASTRO2 = 1
 GRAVITY_ASTRO = 2
 TRAVERSAL_EXACT = 0
 TRAVERSAL_WARP = 1
+INTEGRATOR_VERLET = 0
+INTEGRATOR_EULER = 1
+INTEGRATOR_RK4 = 2
+MULTIPOLE_MONOPOLE = 0
+MULTIPOLE_QUADRUPOLE = 1
 
 
 class CMessage(C.Structure):
@@ -56,7 +61,12 @@ class PhysimSimConfig(C.Structure):
     _fields_ = [("gravity", C.c_uint32), ("leaf_size", C.c_uint32), ("traversal", C.c_uint32),
                 ("compensated", C.c_uint32), ("theta", C.c_double), ("e", C.c_double),
                 ("dt", C.c_double), ("stream", C.c_void_p), ("device", C.c_int32),
-                ("reserved", C.c_uint32 * 3)]
+                ("integrator", C.c_uint32), ("multipole", C.c_uint32),
+                ("com_theta", C.c_float)]
+
+
+# void (*PhysimAccFn)(void *user, const Entity *state, size_t n, Acceleration *acc)
+AccFn = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p)
 
 
 class PhysimTreeSnapshot(C.Structure):
@@ -64,7 +74,8 @@ class PhysimTreeSnapshot(C.Structure):
                 ("node_begin", C.c_void_p), ("node_count", C.c_void_p),
                 ("node_child", C.c_void_p), ("node_nchild", C.c_void_p),
                 ("node_level", C.c_void_p), ("node_centre", C.c_void_p),
-                ("node_com", C.c_void_p), ("n_bodies", C.c_size_t), ("n_nodes", C.c_size_t),
+                ("node_com", C.c_void_p), ("node_quad", C.c_void_p), ("n_bodies", C.c_size_t),
+                ("n_nodes", C.c_size_t),
                 ("extent", C.c_double), ("flags", C.c_uint32)]
 
 
@@ -127,6 +138,9 @@ def _load() -> C.CDLL:
         "physim_gpu_verlet_create": (C.c_int, [i32, C.POINTER(vp)]),
         "physim_gpu_verlet_integrate": (C.c_int, [vp, vp, vp, sz, vp, dbl]),
         "physim_gpu_verlet_destroy": (None, [vp]),
+        "physim_gpu_integrator_create": (C.c_int, [u32, i32, C.POINTER(vp)]),
+        "physim_gpu_integrator_integrate": (C.c_int, [vp, vp, vp, sz, AccFn, vp, dbl]),
+        "physim_gpu_integrator_destroy": (None, [vp]),
     }
     for el in ELEMENTS:
         sig[f"{el}_get_api"] = (C.POINTER(TransformElementAPI), [])

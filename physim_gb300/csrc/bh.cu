@@ -19,8 +19,8 @@
 //                order is deterministic (per-level scans, no atomics).
 //                Geometric centres are computed exactly as the reference does
 //                (child = parent +- extent/2, octree.rs:167-215).
-//   5. moments   mass and centre of mass of every cell from f64 prefix sums
-//                over the sorted bodies.
+//   5. moments   mass, centre of mass (f64 sums) and optionally second
+//                moments (f32) of every cell, bottom up in one launch.
 //   6. traversal one warp per 32 consecutive sorted bodies, DFS with a shared
 //                stack, the reference's opening rule extent/|x - centre| < theta
 //                (octree.rs:137-144).  EXACT: every body keeps its own
@@ -57,13 +57,23 @@ constexpr int kBuf = 128;
 
 // flags[0]: node capacity exceeded (tree truncated; results stay exact)
 // flags[1]: traversal stack overflow (results of the affected warp invalid)
+// flags[2]: a radix-sort look-back wait gave up (sort order invalid)
 constexpr int kFlagNodes = 0;
 constexpr int kFlagStack = 1;
+constexpr int kFlagSort = 2;
+
+// Radix sort of the 63-bit (62-bit) keys: 8 passes of 8-bit digits.
+constexpr int kSortPasses = 8;
+// Look-back spin limit per digit (each spin is one L2 load, ~0.5 us worst
+// case), far above any wait of a running predecessor tile.
+constexpr int kLookbackSpins = 1 << 20;
 
 struct LevelInfo {
     int32_t begin[kMaxLevels + 2];
     int32_t count[kMaxLevels + 2];
-    int32_t total;  // nodes in the tree
+    int32_t total;                      // nodes in the tree
+    uint32_t tile_ctr[kMaxLevels + 1];  // node tiles claimed per level (reset per build)
+    uint32_t epoch;                     // builds so far (tags the look-back words)
 };
 
 __host__ __device__ inline int tree_levels(int nchild) { return nchild == 8 ? 21 : 31; }
@@ -72,25 +82,34 @@ __host__ __device__ inline int level_bits(int nchild) { return nchild == 8 ? 3 :
 // ---------------------------------------------------------------------------
 // 1. extent
 // ---------------------------------------------------------------------------
+// |coordinate| maxima on the f64 bit patterns: non-negative doubles order like
+// their bit patterns, so integer maxima replace f64 ones (GB300 issues f64
+// instructions at a small fraction of its integer rate).  NaN coordinates are
+// skipped, as f64::max skips a NaN operand.
+__device__ __forceinline__ unsigned long long abs_bits(double v)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    return b > 0x7ff0000000000000ull ? 0ull : b;
+}
+
 __global__ void extent_kernel(const double *__restrict__ x, const double *__restrict__ y,
                               const double *__restrict__ z, int n,
                               unsigned long long *__restrict__ out_bits)
 {
-    double m = 0.0;
+    unsigned long long m = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        m = fmax(m, fabs(x[i]));
-        m = fmax(m, fabs(y[i]));
-        m = fmax(m, fabs(z[i]));
+        m = max(m, abs_bits(x[i]));
+        m = max(m, abs_bits(y[i]));
+        m = max(m, abs_bits(z[i]));
     }
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    __shared__ double wm[32];
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ unsigned long long wm[32];
     if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
     __syncthreads();
     if (threadIdx.x < 32) {
-        m = threadIdx.x < (blockDim.x >> 5) ? wm[threadIdx.x] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-        // non-negative doubles order like their bit patterns
-        if (threadIdx.x == 0) atomicMax(out_bits, (unsigned long long)__double_as_longlong(m));
+        m = threadIdx.x < (blockDim.x >> 5) ? wm[threadIdx.x] : 0ull;
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) atomicMax(out_bits, m);
     }
 }
 
@@ -99,24 +118,31 @@ __global__ void extent_kernel(const double *__restrict__ x, const double *__rest
 // ---------------------------------------------------------------------------
 // Cell index of coordinate p at the finest level D: the reference descends
 // from centre 0 / half-width X deciding `p > centre` at every level.
-__device__ __forceinline__ uint32_t axis_cell(double p, double X, double scale, int D,
-                                              double margin)
+// u = (p + X) * 2^(D-1) / X is the position in finest-cell units; unless u is
+// within 2^-mbits (mbits = 40 - D) of a cell boundary, the cell is floor(u),
+// read off u's bits with integer instructions (two f64 operations per axis).
+// Close to a boundary, or for u < 1, the reference's centre arithmetic is
+// replayed in f64.
+__device__ __forceinline__ uint32_t axis_cell(double p, double X, double scale, int D, int mbits)
 {
-    const int lim = (int)((1u << D) - 1u);
-    const double u = __dmul_rn(__dadd_rn(p, X), scale);  // (p + X) / (2X) * 2^D
-    const double fl = trunc(u);
-    const double frac = u - fl;  // exact
-    if (!(u == u)) return 0;
-    if (frac >= margin && frac <= 1.0 - margin) {
-        // u is not within `margin` of a cell boundary: ceil(u) - 1 = floor(u)
-        return (uint32_t)min(max((int)fl, 0), lim);
+    const uint32_t lim = (1u << D) - 1u;
+    const double u = __dmul_rn(__dadd_rn(p, X), scale);
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(u);
+    const int ex = (int)((bits >> 52) & 0x7ff) - 1023;
+    if (ex == 1024) return 0;  // NaN (or infinite) coordinate
+    if (ex >= 0 && ex <= 52 - mbits) {
+        const unsigned long long mant = (bits & 0xfffffffffffffull) | (1ull << 52);
+        const int fb = 52 - ex;  // fraction bits of u
+        const unsigned long long ip = mant >> fb;
+        const unsigned long long top = (mant >> (fb - mbits)) & ((1ull << mbits) - 1ull);
+        if (top != 0ull && top != (1ull << mbits) - 1ull)
+            return ip > lim ? lim : (uint32_t)ip;
     }
-    // Close to a boundary: replay the reference's centre arithmetic.
     double c = 0.0, ext = X;
     uint32_t q = 0;
     for (int d = 0; d < D; ++d) {
         const bool hi = p > c;
-        const double h = __ddiv_rn(ext, 2.0);
+        const double h = __dmul_rn(ext, 0.5);  // ext / 2, exact
         c = hi ? __dadd_rn(c, h) : __dsub_rn(c, h);
         ext = h;
         q = (q << 1) | (hi ? 1u : 0u);
@@ -146,33 +172,53 @@ __device__ __forceinline__ uint64_t spread2(uint32_t v)
     return x;
 }
 
-__global__ void keys_kernel(const double *__restrict__ x, const double *__restrict__ y,
-                            const double *__restrict__ z, int n, int nchild,
-                            const unsigned long long *__restrict__ extent_bits,
-                            uint64_t *__restrict__ keys, uint32_t *__restrict__ vals)
+// Keys, plus the histograms of all 8 radix digits of all keys (block-local in
+// shared memory, then one global atomic per non-empty bucket), for the
+// one-sweep sort.  ghist [8][256] must be zero on entry.  Block 0 also resets
+// the sort's tile counters and advances its epoch (see radix_pass_kernel).
+__global__ void __launch_bounds__(256)
+keys_kernel(const double *__restrict__ x, const double *__restrict__ y,
+            const double *__restrict__ z, int n, int nchild,
+            const unsigned long long *__restrict__ extent_bits, uint64_t *__restrict__ keys,
+            uint32_t *__restrict__ vals, uint32_t *__restrict__ ghist,
+            uint32_t *__restrict__ tile_ctr, uint32_t *__restrict__ epoch)
 {
     __shared__ double s_scale;
+    __shared__ uint32_t h[kSortPasses][kRadixBuckets];
     const double X = __longlong_as_double((long long)*extent_bits);
     const int D = tree_levels(nchild);
+    for (int k = threadIdx.x; k < kSortPasses * kRadixBuckets; k += blockDim.x) (&h[0][0])[k] = 0;
     if (threadIdx.x == 0) s_scale = X > 0.0 ? __ddiv_rn(ldexp(1.0, D - 1), X) : 0.0;
-    __syncthreads();
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double scale = s_scale;
-    const double margin = ldexp(1.0, D - 40);
-    uint64_t key = 0;
-    if (X > 0.0) {
-        const uint32_t qx = axis_cell(x[i], X, scale, D, margin);
-        const uint32_t qy = axis_cell(y[i], X, scale, D, margin);
-        if (nchild == 8) {
-            const uint32_t qz = axis_cell(z[i], X, scale, D, margin);
-            key = spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2);
-        } else {
-            key = spread2(qx) | (spread2(qy) << 1);
-        }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        for (int p = 0; p < kSortPasses; ++p) tile_ctr[p] = 0;
+        *epoch += 1u;
     }
-    keys[i] = key;
-    vals[i] = (uint32_t)i;
+    __syncthreads();
+    const double scale = s_scale;
+    const int mbits = 40 - D;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint64_t key = 0;
+        if (X > 0.0) {
+            const uint32_t qx = axis_cell(x[i], X, scale, D, mbits);
+            const uint32_t qy = axis_cell(y[i], X, scale, D, mbits);
+            if (nchild == 8) {
+                const uint32_t qz = axis_cell(z[i], X, scale, D, mbits);
+                key = spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2);
+            } else {
+                key = spread2(qx) | (spread2(qy) << 1);
+            }
+        }
+        keys[i] = key;
+        vals[i] = (uint32_t)i;
+#pragma unroll
+        for (int p = 0; p < kSortPasses; ++p)
+            atomicAdd(&h[p][(uint32_t)(key >> (kRadixBits * p)) & (kRadixBuckets - 1)], 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kSortPasses * kRadixBuckets; k += blockDim.x) {
+        const uint32_t c = (&h[0][0])[k];
+        if (c) atomicAdd(&ghist[k], c);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -183,31 +229,6 @@ __device__ __forceinline__ uint32_t lanemask_lt()
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
     return m;
-}
-
-__global__ void __launch_bounds__(kSortThreads)
-radix_hist_kernel(const uint64_t *__restrict__ keys, int n, int shift, uint32_t *__restrict__ hist,
-                  int n_tiles)
-{
-    __shared__ uint32_t h[kSortWarps][kRadixBuckets];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int k = threadIdx.x; k < kSortWarps * kRadixBuckets; k += kSortThreads)
-        (&h[0][0])[k] = 0;
-    __syncthreads();
-    const int base = blockIdx.x * kSortTile + warp * (kSortItems * 32);
-    for (int r = 0; r < kSortItems; ++r) {
-        const int idx = base + r * 32 + lane;
-        const bool valid = idx < n;
-        const uint32_t d = valid ? (uint32_t)(keys[idx] >> shift) & (kRadixBuckets - 1) : 0xffffffffu;
-        const uint32_t peers = __match_any_sync(0xffffffffu, d);
-        if (valid && (peers & lanemask_lt()) == 0) h[warp][d] += __popc(peers);
-    }
-    __syncthreads();
-    for (int d = threadIdx.x; d < kRadixBuckets; d += kSortThreads) {
-        uint32_t s = 0;
-        for (int w = 0; w < kSortWarps; ++w) s += h[w][d];
-        hist[(size_t)d * n_tiles + blockIdx.x] = s;
-    }
 }
 
 // Block-wide exclusive scan of one value per thread (blockDim.x <= 1024).
@@ -239,52 +260,58 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *w
     return r;
 }
 
-// Per digit (one block each), the exclusive prefix over tiles of that
-// digit's counts, in place; the digit's total goes to totals[digit].
+// One stable counting pass of the one-sweep LSD radix sort (single-pass
+// chained scan with decoupled look-back, after Merrill & Garland 2016 and
+// Adinets & Merrill 2022).  Tiles of kSortTile keys are claimed in launch
+// order from an atomic counter, so every tile a block looks back at is held
+// by a block that is already running.  Each block ranks its keys by digit
+// (warp by warp, stable), publishes its per-digit counts, then walks back over
+// the preceding tiles' published words until it meets an inclusive prefix,
+// publishes its own inclusive prefix, and scatters.  A status word is
+// (epoch * 4 + flag) << 32 | count, flag 1 = tile count, 2 = inclusive
+// prefix, and epoch counts (sort, pass) pairs; words of earlier passes and
+// sorts carry older epochs and read as not ready, so the status array needs
+// no clearing.  A wait that exceeds
+// kLookbackSpins sets flags[kFlagSort] and gives up (the order is then
+// invalid and the host reports an error).
 __global__ void __launch_bounds__(kSortThreads)
-radix_digit_scan_kernel(uint32_t *__restrict__ hist, int n_tiles, uint32_t *__restrict__ totals)
-{
-    __shared__ uint32_t ws[33];
-    uint32_t *row = hist + (size_t)blockIdx.x * n_tiles;
-    uint32_t carry = 0;
-    for (int t0 = 0; t0 < n_tiles; t0 += blockDim.x) {
-        const int t = t0 + threadIdx.x;
-        const uint32_t v = t < n_tiles ? row[t] : 0;
-        uint32_t total;
-        const uint32_t ex = block_exclusive_scan(v, ws, total);
-        if (t < n_tiles) row[t] = carry + ex;
-        carry += total;
-    }
-    if (threadIdx.x == 0) totals[blockIdx.x] = carry;
-}
-
-__global__ void __launch_bounds__(kSortThreads)
-radix_scatter_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
-                     uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int n,
-                     int shift, const uint32_t *__restrict__ offsets, int n_tiles,
-                     const uint32_t *__restrict__ totals)
+radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
+                  uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int n,
+                  int pass, const uint32_t *__restrict__ ghist, uint32_t *__restrict__ tile_ctr,
+                  unsigned long long *__restrict__ status, const uint32_t *__restrict__ epoch_ptr,
+                  uint32_t *__restrict__ flags)
 {
     static_assert(kSortThreads == kRadixBuckets, "one thread per digit");
     __shared__ uint32_t h[kSortWarps][kRadixBuckets];
-    __shared__ uint32_t digit_base[kRadixBuckets];
+    __shared__ uint32_t digit_off[kRadixBuckets];
     __shared__ uint32_t ws[33];
+    __shared__ int s_tile;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int shift = kRadixBits * pass;
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(&tile_ctr[pass], 1u);
     for (int k = threadIdx.x; k < kSortWarps * kRadixBuckets; k += kSortThreads)
         (&h[0][0])[k] = 0;
+    uint32_t digit_base;
     {
         uint32_t total;
-        digit_base[threadIdx.x] = block_exclusive_scan(totals[threadIdx.x], ws, total);
+        digit_base = block_exclusive_scan(ghist[pass * kRadixBuckets + threadIdx.x], ws, total);
     }
-    __syncthreads();
-    const int base = blockIdx.x * kSortTile + warp * (kSortItems * 32);
+    const int tile = s_tile;
+    const int base = tile * kSortTile + warp * (kSortItems * 32);
     uint64_t kk[kSortItems];
     uint32_t vv[kSortItems];
     uint32_t rank[kSortItems];
+#pragma unroll
     for (int r = 0; r < kSortItems; ++r) {
         const int idx = base + r * 32 + lane;
         const bool valid = idx < n;
         kk[r] = valid ? keys_in[idx] : 0;
         vv[r] = valid ? (vals_in ? vals_in[idx] : (uint32_t)idx) : 0;
+    }
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int idx = base + r * 32 + lane;
+        const bool valid = idx < n;
         const uint32_t d = valid ? (uint32_t)(kk[r] >> shift) & (kRadixBuckets - 1) : 0xffffffffu;
         const uint32_t peers = __match_any_sync(0xffffffffu, d);
         const uint32_t before = __popc(peers & lanemask_lt());
@@ -296,21 +323,52 @@ radix_scatter_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__res
         rank[r] = cur + before;
     }
     __syncthreads();
-    // exclusive prefix over warps, per digit, plus the global offset
-    for (int d = threadIdx.x; d < kRadixBuckets; d += kSortThreads) {
-        uint32_t run = digit_base[d] + offsets[(size_t)d * n_tiles + blockIdx.x];
-        for (int w = 0; w < kSortWarps; ++w) {
-            uint32_t c = h[w][d];
-            h[w][d] = run;
-            run += c;
-        }
+    // this tile's count of digit d, and the warps' exclusive offsets within it
+    const int d = threadIdx.x;
+    uint32_t count = 0;
+    for (int w = 0; w < kSortWarps; ++w) {
+        const uint32_t c = h[w][d];
+        h[w][d] = count;
+        count += c;
     }
+    // tag base of this sort and pass: the passes share the status array
+    const unsigned long long ep =
+        ((unsigned long long)(*epoch_ptr & 0x03ffffffu) * kSortPasses + (unsigned)pass) * 4ull;
+    volatile unsigned long long *st = status;
+    uint32_t excl = 0;
+    if (tile == 0) {
+        st[d] = ((ep + 2ull) << 32) | count;
+    } else {
+        st[(size_t)tile * kRadixBuckets + d] = ((ep + 1ull) << 32) | count;
+        int t = tile - 1;
+        int spins = 0;
+        for (;;) {
+            const unsigned long long w = st[(size_t)t * kRadixBuckets + d];
+            const unsigned long long tag = w >> 32;
+            if (tag == ep + 2ull) {
+                excl += (uint32_t)w;
+                break;
+            }
+            if (tag == ep + 1ull) {
+                excl += (uint32_t)w;
+                --t;  // t > 0 here: tile 0 publishes its inclusive prefix at once
+                continue;
+            }
+            if (++spins > kLookbackSpins) {
+                atomicOr(&flags[kFlagSort], 1u);
+                break;
+            }
+        }
+        st[(size_t)tile * kRadixBuckets + d] = ((ep + 2ull) << 32) | (excl + count);
+    }
+    digit_off[d] = digit_base + excl;
     __syncthreads();
+#pragma unroll
     for (int r = 0; r < kSortItems; ++r) {
         const int idx = base + r * 32 + lane;
         if (idx >= n) continue;
-        const uint32_t d = (uint32_t)(kk[r] >> shift) & (kRadixBuckets - 1);
-        const uint32_t pos = h[warp][d] + rank[r];
+        const uint32_t dg = (uint32_t)(kk[r] >> shift) & (kRadixBuckets - 1);
+        const uint32_t pos = digit_off[dg] + h[warp][dg] + rank[r];
         keys_out[pos] = kk[r];
         vals_out[pos] = vv[r];
     }
@@ -345,6 +403,11 @@ struct NodeArrays {
     float4 *geo;   // cx, cy, cz, extent (f32)
     float4 *com;   // x, y, z, mass (f32)
     int4 *meta;    // (id | nchild << 28, first child, first body, body count)
+    int32_t *parent;   // parent node, -1 for the root
+    double4 *msum;     // f64 mass and mass-weighted position sums (M, Mx, My, Mz)
+    float4 *quad_a;    // second moments about the centre of mass: Sxx, Syy, Szz, trace
+    float4 *quad_b;    // Sxy, Sxz, Syz, 0
+    uint32_t *arrivals;  // children finished, for the bottom-up moment pass (kept at 0)
     int cap;
 };
 
@@ -357,11 +420,14 @@ __global__ void root_kernel(NodeArrays nd, LevelInfo *lv, int n,
         lv->begin[d] = 0;
         lv->count[d] = 0;
     }
+    for (int d = 0; d < kMaxLevels + 1; ++d) lv->tile_ctr[d] = 0;
+    lv->epoch += 1u;
     lv->total = n > 0 ? 1 : 0;
     lv->count[0] = n > 0 ? 1 : 0;
     lv->begin[1] = 1;
     nd.begin[0] = 0;
     nd.count[0] = n;
+    nd.parent[0] = -1;
     nd.child[0] = -1;
     nd.nchild[0] = 0;
     nd.level[0] = 0;
@@ -486,87 +552,48 @@ __device__ int node_child_count(const uint64_t *__restrict__ keys, const NodeArr
     return k;
 }
 
-// Per-block sums of child counts over the level's nodes (block b takes a
-// contiguous chunk).  The last block to finish (atomic ticket after a
-// memory fence; nothing waits) turns the block sums into exclusive offsets
-// and sizes the next level, leaving it empty (the level's nodes stay
-// leaves: exact, slower) if the node arrays would overflow.
+// One level of the build in one launch: the level's nodes are cut into tiles
+// of kBuildThreads, claimed in launch order from an atomic counter; each
+// block counts its tile's children, publishes the tile's total, walks back
+// over the preceding tiles' words to its exclusive prefix (decoupled
+// look-back, as in the radix passes; the tile holding an earlier word is
+// held by a block that is already running), then writes its nodes' children
+// at that offset.  Children therefore follow their parents' order, so the
+// next level is laid out exactly as a serial build would lay it out.  A tile
+// whose children would overflow the node arrays leaves its nodes unsplit
+// (results stay exact, flags[kFlagNodes]); the tiles before it keep theirs.
+// Status words are (tag << 32 | tile total), tag = (epoch * 32 + level) * 4 +
+// flag, flag 1 = tile total, 2 = inclusive prefix; words of other levels and
+// builds read as not ready.
 __global__ void __launch_bounds__(kBuildThreads)
-level_count_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, LevelInfo *lv, int level,
-                   int leaf, int nchild, const int32_t *__restrict__ top, int32_t *__restrict__ bsum,
-                   unsigned int *__restrict__ ticket, uint32_t *__restrict__ flags)
+level_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, LevelInfo *lv, int level, int leaf,
+             int nchild, const int32_t *__restrict__ top, unsigned long long *__restrict__ status,
+             uint32_t *__restrict__ flags)
 {
     const int D = tree_levels(nchild), bits = level_bits(nchild);
-    const int cnt = lv->count[level], first = lv->begin[level];
-    if (cnt == 0) {  // empty level: the tree is complete
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            lv->begin[level + 1] = first;
-            lv->count[level + 1] = 0;
-        }
-        return;
-    }
-    const int chunk = (cnt + gridDim.x - 1) / gridDim.x;
-    const int cb = blockIdx.x * chunk, ce = min(cb + chunk, cnt);
-    int s = 0;
-    for (int k = cb + threadIdx.x; k < ce; k += blockDim.x)
-        s += node_child_count(keys, nd, first + k, leaf, level, D, bits, nchild, top);
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    __shared__ int ws[kBuildThreads / 32];
-    __shared__ bool last;
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int t = 0;
-        for (int w = 0; w < kBuildThreads / 32; ++w) t += ws[w];
-        bsum[blockIdx.x] = t;
-        __threadfence();
-        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    if (threadIdx.x == 0) {
-        int32_t run = 0;
-        for (int b = 0; b < (int)gridDim.x; ++b) {
-            const int32_t v = ((volatile int32_t *)bsum)[b];
-            bsum[b] = run;
-            run += v;
-        }
-        const int32_t next_begin = first + cnt;
-        const bool fits = (long long)next_begin + run <= (long long)nd.cap;
-        lv->begin[level + 1] = next_begin;
-        lv->count[level + 1] = fits ? run : 0;
-        lv->total = next_begin + (fits ? run : 0);
-        if (!fits) atomicOr(&flags[kFlagNodes], 1u);
-        *ticket = 0;
-    }
-}
-
-// Writes the children of the level's nodes at the offsets level_count_kernel
-// produced.
-__global__ void __launch_bounds__(kBuildThreads)
-level_write_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, const LevelInfo *__restrict__ lv,
-                   int level, int leaf, int nchild, const int32_t *__restrict__ top,
-                   const int32_t *__restrict__ boff)
-{
-    const int D = tree_levels(nchild), bits = level_bits(nchild);
-    const int cnt = lv->count[level], first = lv->begin[level];
-    if (cnt == 0 || lv->count[level + 1] == 0) return;
-    __shared__ int32_t ws[kBuildThreads / 32];
-    __shared__ int32_t carry;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (threadIdx.x == 0) carry = boff[blockIdx.x];
-    __syncthreads();
-    const int child_base = lv->begin[level + 1];
-    const int chunk = (cnt + gridDim.x - 1) / gridDim.x;
-    const int cb = blockIdx.x * chunk, ce = min(cb + chunk, cnt);
-    for (int k0 = cb; k0 < ce; k0 += blockDim.x) {
-        const int k = k0 + threadIdx.x;
+    const int cnt = lv->count[level];
+    if (cnt == 0) return;  // the tree is complete
+    const int first = lv->begin[level];
+    const int child_base = first + cnt;
+    const int ntiles = (cnt + kBuildThreads - 1) / kBuildThreads;
+    const unsigned long long tag =
+        ((unsigned long long)(lv->epoch & 0x03ffffffu) * 32ull + (unsigned)level) * 4ull;
+    volatile unsigned long long *st = status;
+    __shared__ uint32_t ws[33];
+    __shared__ int s_tile;
+    __shared__ int32_t s_excl;
+    if (blockIdx.x == 0 && threadIdx.x == 0) lv->begin[level + 1] = child_base;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(&lv->tile_ctr[level], 1u);
+        __syncthreads();
+        const int tile = s_tile;
+        if (tile >= ntiles) break;
+        const int k = tile * kBuildThreads + threadIdx.x;
         const int node = first + k;
         int bounds[9];
-        int nc = 0;
+        uint32_t nc = 0;
         bool split = false;
-        if (k < ce) {
+        if (k < cnt) {
             const int b = nd.begin[node], c = nd.count[node];
             split = node_splits(keys, b, c, leaf, level, D);
             if (split) {
@@ -575,32 +602,53 @@ level_write_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, const Level
                 for (int q = 0; q < nchild; ++q) nc += bounds[q + 1] > bounds[q];
             }
         }
-        // block-wide exclusive scan of nc
-        int incl = nc;
-        for (int o = 1; o < 32; o <<= 1) {
-            int t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
+        uint32_t T;
+        const uint32_t local = block_exclusive_scan(nc, ws, T);
+        if (threadIdx.x == 0) {
+            uint32_t excl = 0;
+            if (tile == 0) {
+                st[0] = ((tag + 2ull) << 32) | T;
+            } else {
+                st[tile] = ((tag + 1ull) << 32) | T;
+                int t = tile - 1, spins = 0;
+                for (;;) {
+                    const unsigned long long w = st[t];
+                    const unsigned long long wt = w >> 32;
+                    if (wt == tag + 2ull) {
+                        excl += (uint32_t)w;
+                        break;
+                    }
+                    if (wt == tag + 1ull) {
+                        excl += (uint32_t)w;
+                        --t;
+                        continue;
+                    }
+                    if (++spins > kLookbackSpins) {
+                        atomicOr(&flags[kFlagSort], 1u);
+                        break;
+                    }
+                }
+                st[tile] = ((tag + 2ull) << 32) | (excl + T);
+            }
+            s_excl = (int32_t)excl;
         }
-        if (lane == 31) ws[warp] = incl;
         __syncthreads();
-        int wbase = 0;
-        for (int w = 0; w < warp; ++w) wbase += ws[w];
-        const int excl = carry + wbase + incl - nc;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry = excl + nc;
-        if (k < ce) {
-            if (split) {
-                const int fc = child_base + excl;
+        const int32_t P = s_excl;
+        const bool fits = (long long)child_base + P + T <= (long long)nd.cap;
+        if (k < cnt) {
+            if (split && fits) {
+                const int fc = child_base + P + (int)local;
                 nd.child[node] = fc;
                 nd.nchild[node] = (uint8_t)nc;
                 const size_t cap = nd.cap;
                 const double pcx = nd.c64[node], pcy = nd.c64[cap + node];
                 const double pcz = nd.c64[2 * cap + node], pext = nd.c64[3 * cap + node];
-                const double h = __ddiv_rn(pext, 2.0);
+                const double h = __dmul_rn(pext, 0.5);  // pext / 2, exact
                 int w = 0;
                 for (int q = 0; q < nchild; ++q) {
                     if (bounds[q + 1] <= bounds[q]) continue;
                     const int ci = fc + w++;
+                    nd.parent[ci] = node;
                     nd.begin[ci] = bounds[q];
                     nd.count[ci] = bounds[q + 1] - bounds[q];
                     nd.child[ci] = -1;
@@ -617,170 +665,143 @@ level_write_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, const Level
                 nd.nchild[node] = 0;
             }
         }
+        if (threadIdx.x == 0 && T > 0) {
+            if (fits) {
+                atomicMax(&lv->count[level + 1], P + (int32_t)T);
+                atomicMax(&lv->total, child_base + P + (int32_t)T);
+            } else {
+                atomicOr(&flags[kFlagNodes], 1u);
+            }
+        }
         __syncthreads();
     }
 }
 
 // ---------------------------------------------------------------------------
-// 5. moments: exclusive prefix sums of m, m x, m y, m z over sorted bodies
+// 5. moments: mass, centre of mass and (optionally) second moments of every
+//    cell, bottom up in one launch
 // ---------------------------------------------------------------------------
-constexpr int kMomThreads = 256;
-
-__global__ void __launch_bounds__(kMomThreads)
-moment_partial_kernel(const double *__restrict__ spos, const double *__restrict__ smass, int n,
-                      double *__restrict__ bsum)
+// Each leaf sums its own bodies: mass and mass-weighted positions in f64 (the
+// f32 centre of mass is then within one rounding of the exact one, as the
+// reference's f64 arithmetic needs where a cell's centre of mass lies very
+// close to a body that interacts with it, e.g. a quadtree cell holding a
+// heavy body that a body far above it in z accepts), second moments in f32.
+// A leaf whose bodies all sit at one position keeps that exact position, so a
+// body there cancels against it as the reference's equal-centre skip does.
+// A parent is finished by the thread of its last child to arrive (atomic
+// count of arrivals after a fence; nothing waits), which combines the
+// children in child order -- so results do not depend on the arrival order --
+// and continues upwards:
+//   M = sum M_c,  M c = sum (M c)_c   (f64 sums),
+//   S = sum_c [S_c + M_c (c_c - c)(c_c - c)^T]   (second moments about c).
+// A massless cell sits at its geometric centre.  Every node also gets its f32
+// geometry and packed traversal metadata here.
+__device__ __forceinline__ void store_quad(const NodeArrays &nd, int i, const float s[6])
 {
-    const int chunk = (n + gridDim.x - 1) / gridDim.x;
-    const int cb = blockIdx.x * chunk, ce = min(cb + chunk, n);
-    double s[4] = {0, 0, 0, 0};
-    for (int k = cb + threadIdx.x; k < ce; k += blockDim.x) {
-        const double m = smass[k];
-        s[0] += m;
-        s[1] += m * spos[k];
-        s[2] += m * spos[n + k];
-        s[3] += m * spos[2 * (size_t)n + k];
-    }
-    __shared__ double red[4][kMomThreads];
-    for (int c = 0; c < 4; ++c) red[c][threadIdx.x] = s[c];
-    __syncthreads();
-    for (int off = kMomThreads / 2; off > 0; off >>= 1) {
-        if (threadIdx.x < off)
-            for (int c = 0; c < 4; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + off];
-        __syncthreads();
-    }
-    if (threadIdx.x < 4) bsum[threadIdx.x * gridDim.x + blockIdx.x] = red[threadIdx.x][0];
+    nd.quad_a[i] = make_float4(s[0], s[1], s[2], s[0] + s[1] + s[2]);
+    nd.quad_b[i] = make_float4(s[3], s[4], s[5], 0.f);
 }
 
-// Exclusive scan of the per-block sums, one warp per component.
-__global__ void __launch_bounds__(128) moment_blockscan_kernel(double *__restrict__ bsum, int nblocks)
+__device__ __forceinline__ void node_geometry(const NodeArrays &nd, int i)
 {
-    const int c = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double *v = bsum + (size_t)c * nblocks;
-    const int per = (nblocks + 31) / 32;
-    const int b = lane * per, e = min(b + per, nblocks);
-    double s = 0.0;
-    for (int k = b; k < e; ++k) s += v[k];
-    double incl = s;
-    for (int o = 1; o < 32; o <<= 1) {
-        const double t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
-    }
-    double run = incl - s;
-    for (int k = b; k < e; ++k) {
-        const double t = v[k];
-        v[k] = run;
-        run += t;
-    }
+    const size_t cap = nd.cap;
+    nd.geo[i] = make_float4((float)nd.c64[i], (float)nd.c64[cap + i], (float)nd.c64[2 * cap + i],
+                            (float)nd.c64[3 * cap + i]);
+    nd.meta[i] = make_int4(i | ((int)nd.nchild[i] << 28), nd.child[i], nd.begin[i], nd.count[i]);
 }
 
-constexpr int kMomItems = 4;
-
-// Exclusive prefix sums pref[c][k] of (m, m x, m y, m z) over the sorted
-// bodies.  Block b covers a contiguous chunk starting from its block offset;
-// each thread takes kMomItems consecutive bodies per tile.
-__global__ void __launch_bounds__(kMomThreads)
-moment_scan_kernel(const double *__restrict__ spos, const double *__restrict__ smass, int n,
-                   const double *__restrict__ boff, double *__restrict__ pref)
+// f32 centre of mass from the f64 sums (one f64 reciprocal, three products).
+__device__ __forceinline__ float4 com_from_sums(const NodeArrays &nd, int i, double4 m)
 {
-    const int chunk = (n + gridDim.x - 1) / gridDim.x;
-    const int cb = blockIdx.x * chunk, ce = min(cb + chunk, n);
-    const size_t stride = (size_t)n + 1;
-    __shared__ double carry[4];
-    __shared__ double ws[4][kMomThreads / 32];
-    if (threadIdx.x < 4) carry[threadIdx.x] = boff[threadIdx.x * gridDim.x + blockIdx.x];
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr int kTile = kMomThreads * kMomItems;
-    for (int t0 = cb; t0 < ce; t0 += kTile) {
-        const int k0 = t0 + threadIdx.x * kMomItems;
-        double v[kMomItems][4];
-        double tot[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll
-        for (int j = 0; j < kMomItems; ++j) {
-            const int k = k0 + j;
-            double m = 0.0, px = 0.0, py = 0.0, pz = 0.0;
-            if (k < ce) {
-                m = smass[k];
-                px = spos[k];
-                py = spos[n + k];
-                pz = spos[2 * (size_t)n + k];
-            }
-            v[j][0] = m;
-            v[j][1] = m * px;
-            v[j][2] = m * py;
-            v[j][3] = m * pz;
-#pragma unroll
-            for (int c = 0; c < 4; ++c) tot[c] += v[j][c];
-        }
-        double incl[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            incl[c] = tot[c];
-            for (int o = 1; o < 32; o <<= 1) {
-                const double t = __shfl_up_sync(0xffffffffu, incl[c], o);
-                if (lane >= o) incl[c] += t;
-            }
-            if (lane == 31) ws[c][warp] = incl[c];
-        }
-        __syncthreads();
-        double run[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            double wb = 0.0;
-            for (int w = 0; w < warp; ++w) wb += ws[c][w];
-            run[c] = carry[c] + wb + incl[c] - tot[c];
-        }
-        __syncthreads();
-#pragma unroll
-        for (int j = 0; j < kMomItems; ++j) {
-            const int k = k0 + j;
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                if (k < ce) pref[c * stride + k] = run[c];
-                run[c] += v[j][c];
-            }
-        }
-        if (threadIdx.x == kMomThreads - 1)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) carry[c] = run[c];
-        __syncthreads();
+    if (m.x != 0.0) {
+        const double r = __drcp_rn(m.x);
+        return make_float4((float)(m.y * r), (float)(m.z * r), (float)(m.w * r), (float)m.x);
     }
-    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
-        for (int c = 0; c < 4; ++c) pref[c * stride + n] = carry[c];
+    return make_float4((float)nd.c64[i], (float)nd.c64[nd.cap + i],
+                       (float)nd.c64[2 * (size_t)nd.cap + i], 0.f);
 }
 
-__global__ void node_finish_kernel(NodeArrays nd, const LevelInfo *__restrict__ lv,
-                                   const double *__restrict__ pref, int n,
-                                   const float4 *__restrict__ sbody, const double *__restrict__ spos)
+__global__ void moments_kernel(NodeArrays nd, const LevelInfo *__restrict__ lv,
+                               const float4 *__restrict__ sbody, const double *__restrict__ spos,
+                               const double *__restrict__ smass, int n, int quad)
 {
     const int total = lv->total;
-    const size_t stride = (size_t)n + 1;
-    const size_t cap = nd.cap;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        if (nd.child[i] >= 0) continue;
+        node_geometry(nd, i);
         const int b = nd.begin[i], e = b + nd.count[i];
-        nd.geo[i] = make_float4((float)nd.c64[i], (float)nd.c64[cap + i], (float)nd.c64[2 * cap + i],
-                                (float)nd.c64[3 * cap + i]);
-        float4 com;
-        const bool same_pos = spos[b] == spos[e - 1] && spos[n + b] == spos[n + e - 1] &&
-                              spos[2 * (size_t)n + b] == spos[2 * (size_t)n + e - 1];
-        const double M = pref[e] - pref[b];
-        if (e - b == 1) {
-            // a single body: the body itself, so it cancels against itself in
-            // the pair law as the reference's equal-centre skip does
-            com = sbody[b];
-        } else if (same_pos) {
-            com = sbody[b];
-            com.w = (float)M;
-        } else if (M != 0.0) {
-            com = make_float4((float)((pref[stride + e] - pref[stride + b]) / M),
-                              (float)((pref[2 * stride + e] - pref[2 * stride + b]) / M),
-                              (float)((pref[3 * stride + e] - pref[3 * stride + b]) / M), (float)M);
-        } else {
-            com = make_float4((float)nd.c64[i], (float)nd.c64[cap + i], (float)nd.c64[2 * cap + i],
-                              0.f);
+        const float4 p0 = sbody[b];
+        double4 ms = make_double4(0.0, 0.0, 0.0, 0.0);
+        bool same = true;
+        for (int j = b; j < e; ++j) {
+            const double m = smass[j];
+            ms.x += m;
+            ms.y = fma(m, spos[j], ms.y);
+            ms.z = fma(m, spos[n + j], ms.z);
+            ms.w = fma(m, spos[2 * (size_t)n + j], ms.w);
+            const float4 p = sbody[j];
+            same = same && p.x == p0.x && p.y == p0.y && p.z == p0.z;
         }
+        nd.msum[i] = ms;
+        const float4 com = same ? make_float4(p0.x, p0.y, p0.z, (float)ms.x)
+                                : com_from_sums(nd, i, ms);
         nd.com[i] = com;
-        nd.meta[i] = make_int4(i | ((int)nd.nchild[i] << 28), nd.child[i], b, e - b);
+        if (quad) {
+            float q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (!same)
+                for (int j = b; j < e; ++j) {
+                    const float4 p = sbody[j];
+                    const float dx = p.x - com.x, dy = p.y - com.y, dz = p.z - com.z;
+                    q[0] = fmaf(p.w * dx, dx, q[0]);
+                    q[1] = fmaf(p.w * dy, dy, q[1]);
+                    q[2] = fmaf(p.w * dz, dz, q[2]);
+                    q[3] = fmaf(p.w * dx, dy, q[3]);
+                    q[4] = fmaf(p.w * dx, dz, q[4]);
+                    q[5] = fmaf(p.w * dy, dz, q[5]);
+                }
+            store_quad(nd, i, q);
+        }
+        int node = i;
+        for (;;) {
+            const int par = nd.parent[node];
+            if (par < 0) break;
+            __threadfence();
+            const uint32_t arrived = atomicAdd(&nd.arrivals[par], 1u);
+            if (arrived + 1u != (uint32_t)nd.nchild[par]) break;
+            __threadfence();
+            nd.arrivals[par] = 0u;  // ready for the next build
+            node_geometry(nd, par);
+            const int fc = nd.child[par], nc = nd.nchild[par];
+            double4 pm = make_double4(0.0, 0.0, 0.0, 0.0);
+            for (int k = fc; k < fc + nc; ++k) {
+                const double2 *q2 = reinterpret_cast<const double2 *>(&nd.msum[k]);
+                const double2 lo = __ldcg(q2), hi = __ldcg(q2 + 1);
+                pm.x += lo.x;
+                pm.y += lo.y;
+                pm.z += hi.x;
+                pm.w += hi.y;
+            }
+            nd.msum[par] = pm;
+            const float4 cp = com_from_sums(nd, par, pm);
+            nd.com[par] = cp;
+            if (quad) {
+                float t[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                for (int k = fc; k < fc + nc; ++k) {
+                    const float4 cc = __ldcg(&nd.com[k]);
+                    const float4 qa = __ldcg(&nd.quad_a[k]);
+                    const float4 qb = __ldcg(&nd.quad_b[k]);
+                    const float dx = cc.x - cp.x, dy = cc.y - cp.y, dz = cc.z - cp.z;
+                    t[0] += fmaf(cc.w * dx, dx, qa.x);
+                    t[1] += fmaf(cc.w * dy, dy, qa.y);
+                    t[2] += fmaf(cc.w * dz, dz, qa.z);
+                    t[3] += fmaf(cc.w * dx, dy, qb.x);
+                    t[4] += fmaf(cc.w * dx, dz, qb.y);
+                    t[5] += fmaf(cc.w * dy, dz, qb.z);
+                }
+                store_quad(nd, par, t);
+            }
+            node = par;
+        }
     }
 }
 
@@ -801,6 +822,12 @@ struct TravArgs {
     double *partial;
     const unsigned long long *extent_bits;
     unsigned long long *stats;  // [0] node visits, [1] pair interactions (lanes)
+    // accuracy options (not reference behaviour): quadrupole correction of
+    // accepted cells, and a centre-of-mass guard that also requires
+    // b_max < com_theta * |x - c| (b_max = sqrt(3) extent + |c - centre|
+    // bounds the distance of the cell's bodies from c); 0 disables it.
+    int quad;
+    float com_theta;
 };
 
 __device__ __forceinline__ float load_extent(const TravArgs &a)
@@ -846,6 +873,72 @@ __device__ __forceinline__ void pair_acc(float qx, float qy, float qz, float4 b,
     az = fmaf(dz, s, az);
 }
 
+// Quadrupole correction of a cell with centre of mass c and second moments S
+// (about c) for the reference's law a = sum m d / (|d| (|d|^2 + e)):
+// expanding d g(|d|), g(r) = 1/(r (r^2 + e)), to second order about c gives
+//   a_2 = h S D + (h tr S + h' / r  D.S.D) D / 2,  D = c - x,
+// h = g'(r)/r = -A / (r u^2), h'/r = (-6 + A (1/r^2 + 2 A / (u r))) / (r u^2),
+// u = r (r^2 + e), A = 3 r^2 + e (e = 0 gives the Newtonian -3/r^5, 15/r^7).
+__device__ __forceinline__ void quad_acc(float qx, float qy, float qz, float4 c, float4 qa,
+                                         float4 qb, float e, float &ax, float &ay, float &az)
+{
+    const float dx = c.x - qx, dy = c.y - qy, dz = c.z - qz;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (!(r2 > 1e-30f)) return;
+    const float ir = rsqrt_approx(r2);
+    const float iu = ir * __fdividef(1.f, r2 + e);
+    const float A = fmaf(3.f, r2, e);
+    const float base = ir * iu * iu;
+    const float h = -A * base;
+    const float hp = base * fmaf(A, fmaf(2.f * A, iu * ir, ir * ir), -6.f);
+    const float sdx = fmaf(qa.x, dx, fmaf(qb.x, dy, qb.y * dz));
+    const float sdy = fmaf(qb.x, dx, fmaf(qa.y, dy, qb.z * dz));
+    const float sdz = fmaf(qb.y, dx, fmaf(qb.z, dy, qa.z * dz));
+    const float dsd = fmaf(dx, sdx, fmaf(dy, sdy, dz * sdz));
+    const float k = 0.5f * fmaf(h, qa.w, hp * dsd);
+    ax = fmaf(h, sdx, fmaf(k, dx, ax));
+    ay = fmaf(h, sdy, fmaf(k, dy, ay));
+    az = fmaf(h, sdz, fmaf(k, dz, az));
+}
+
+// Monopole + quadrupole of one accepted cell, sharing the one reciprocal
+// square root: 1/sqrt(r^2 (r^2 + e)^2) = 1/u, and 1/r = (r^2 + e)/u.
+__device__ __forceinline__ void cell_quad_acc(float qx, float qy, float qz, float4 c, float4 qa,
+                                              float4 qb, float e, float &ax, float &ay,
+                                              float &az)
+{
+    const float dx = c.x - qx, dy = c.y - qy, dz = c.z - qz;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float w = r2 + e;
+    const float iu = rsqrt_approx(fmaf(r2, w * w, kPairGuard));
+    const float s = c.w * iu;
+    const float ir = r2 > 1e-30f ? iu * w : 0.f;  // no quadrupole term at r = 0
+    const float A = fmaf(3.f, r2, e);
+    const float base = ir * iu * iu;
+    const float h = -A * base;
+    const float hp = base * fmaf(A, fmaf(2.f * A, iu * ir, ir * ir), -6.f);
+    const float sdx = fmaf(qa.x, dx, fmaf(qb.x, dy, qb.y * dz));
+    const float sdy = fmaf(qb.x, dx, fmaf(qa.y, dy, qb.z * dz));
+    const float sdz = fmaf(qb.y, dx, fmaf(qb.z, dy, qa.z * dz));
+    const float dsd = fmaf(dx, sdx, fmaf(dy, sdy, dz * sdz));
+    const float k = fmaf(0.5f, fmaf(h, qa.w, hp * dsd), s);
+    ax = fmaf(h, sdx, fmaf(k, dx, ax));
+    ay = fmaf(h, sdy, fmaf(k, dy, ay));
+    az = fmaf(h, sdz, fmaf(k, dz, az));
+}
+
+// The centre-of-mass guard for one body: b_max < com_theta |x - c|.
+__device__ __forceinline__ bool com_guard(const TravArgs &a, float4 geo, float4 c, float qx,
+                                          float qy, float qz)
+{
+    if (a.com_theta <= 0.f) return true;
+    const float ox = c.x - geo.x, oy = c.y - geo.y, oz = c.z - geo.z;
+    const float bmax = fmaf(1.7320509f, geo.w, sqrtf(fmaf(ox, ox, fmaf(oy, oy, oz * oz))));
+    const float dx = c.x - qx, dy = c.y - qy, dz = c.z - qz;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    return bmax * bmax < a.com_theta * a.com_theta * r2;
+}
+
 __device__ __forceinline__ void fold(float &hi, float &lo, float &t)
 {
     float s, err;
@@ -889,11 +982,17 @@ traverse_exact_kernel(TravArgs a_in)
         const float4 geo = a.nd.geo[node];
         const int child = a.nd.child[node];
         bool acc = false;
-        if (in) acc = accept_cell(a, node, geo, q.x, q.y, q.z, k);
+        if (in) {
+            acc = accept_cell(a, node, geo, q.x, q.y, q.z, k);
+            if (acc && a.com_theta > 0.f) acc = com_guard(a, geo, a.nd.com[node], q.x, q.y, q.z);
+        }
         const uint32_t open = top.mask & ~__ballot_sync(0xffffffffu, acc);
         ++visits;
         if (acc) {
-            pair_acc(q.x, q.y, q.z, a.nd.com[node], a.e, ax, ay, az);
+            const float4 cm = a.nd.com[node];
+            pair_acc(q.x, q.y, q.z, cm, a.e, ax, ay, az);
+            if (a.quad) quad_acc(q.x, q.y, q.z, cm, a.nd.quad_a[node], a.nd.quad_b[node], a.e, ax,
+                                 ay, az);
             ++pairs;
         }
         ++since_fold;
@@ -970,12 +1069,18 @@ __device__ __forceinline__ int warp_exclusive_scan(int v, int lane, int &total)
     return x - v;
 }
 
+// kQuad: quadrupole corrections of accepted cells (the quadrupole tiles are
+// only sized in that instantiation, so the monopole kernel keeps its
+// registers and occupancy).
+template <bool kQuad>
 __global__ void __launch_bounds__(kTravWarps * 32)
 traverse_warp_kernel(TravArgs a_in)
 {
     __shared__ int32_t gstack[kTravWarps][kGStack];
     __shared__ int32_t queue[kTravWarps][kGQueue];
     __shared__ float4 tile[kTravWarps][32];
+    __shared__ float4 tqa[kQuad ? kTravWarps : 1][32];
+    __shared__ float4 tqb[kQuad ? kTravWarps : 1][32];
     TravArgs a = a_in;
     a.extent = load_extent(a_in);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1006,22 +1111,44 @@ traverse_warp_kernel(TravArgs a_in)
     int sp = 1;
     if (lane == 0) gstack[warp][0] = 0;
     __syncwarp();
+    // Bodies are queued from the front of the queue, accepted cells from the
+    // back, so each is evaluated by its own loop: plain pairs for bodies,
+    // pair + quadrupole (kQuad) for cells.
+    int nc = 0;  // queued cells
     auto flush = [&]() {
         for (int j0 = 0; j0 < nq; j0 += 32) {
             const int m = min(32, nq - j0);
             __syncwarp();
-            if (lane < m) {
-                const int r = queue[warp][j0 + lane];
-                tile[warp][lane] = r >= 0 ? a.sbody[r] : a.nd.com[-r - 1];
-            }
+            if (lane < m) tile[warp][lane] = a.sbody[queue[warp][j0 + lane]];
             __syncwarp();
             for (int j = 0; j < m; ++j) pair_acc(q.x, q.y, q.z, tile[warp][j], a.e, ax, ay, az);
         }
-        pairs += nq;
+        for (int j0 = 0; j0 < nc; j0 += 32) {
+            const int m = min(32, nc - j0);
+            __syncwarp();
+            if (lane < m) {
+                const int c = -queue[warp][kGQueue - 1 - (j0 + lane)] - 1;
+                tile[warp][lane] = a.nd.com[c];
+                if (kQuad) {
+                    tqa[warp][lane] = a.nd.quad_a[c];
+                    tqb[warp][lane] = a.nd.quad_b[c];
+                }
+            }
+            __syncwarp();
+            for (int j = 0; j < m; ++j) {
+                if (kQuad)
+                    cell_quad_acc(q.x, q.y, q.z, tile[warp][j], tqa[warp][j], tqb[warp][j], a.e,
+                                  ax, ay, az);
+                else
+                    pair_acc(q.x, q.y, q.z, tile[warp][j], a.e, ax, ay, az);
+            }
+        }
+        pairs += nq + nc;
         fold(hx, lx, ax);
         fold(hy, ly, ay);
         fold(hz, lz, az);
         nq = 0;
+        nc = 0;
         __syncwarp();
     };
     bool overflow = false;
@@ -1047,6 +1174,19 @@ traverse_warp_kernel(TravArgs a_in)
             // 1.1e-7 (|p| + |c|) + 3.5e-7 r against the reference's f64 value
             const float rmin = r - (2e-7f * (bmax + cmax) + 5e-7f * r);
             acc = theta > 0.f && rmin > 0.f && geo.w * (1.f + 2e-6f) < theta * rmin;
+            if (acc && a.com_theta > 0.f) {
+                // centre-of-mass guard against the whole box (distance from c
+                // to the box is a lower bound of every body's |x - c|)
+                const float4 cm = a.nd.com[cell];
+                const float ox = cm.x - geo.x, oy = cm.y - geo.y, oz = cm.z - geo.z;
+                const float bmax =
+                    fmaf(1.7320509f, geo.w, sqrtf(fmaf(ox, ox, fmaf(oy, oy, oz * oz))));
+                const float ex = fmaxf(fmaxf(lo_x - cm.x, cm.x - hi_x), 0.f);
+                const float ey = fmaxf(fmaxf(lo_y - cm.y, cm.y - hi_y), 0.f);
+                const float ez = fmaxf(fmaxf(lo_z - cm.z, cm.z - hi_z), 0.f);
+                const float rc2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+                acc = bmax * bmax < a.com_theta * a.com_theta * rc2;
+            }
             if (acc) {
                 qref = -cell - 1;
                 qcnt = 1;
@@ -1074,7 +1214,12 @@ traverse_warp_kernel(TravArgs a_in)
             const float r = r2 * rsqrt_approx(r2);
             const float cm = fmaxf(fmaxf(fabsf(gx), fabsf(gy)), fabsf(gz));
             const float rl = r - (2e-7f * (pmax + cm) + 5e-7f * r);
-            const bool ok = !valid || (rl > 0.f && gw * (1.f + 2e-6f) < theta * rl);
+            bool ok = !valid || (rl > 0.f && gw * (1.f + 2e-6f) < theta * rl);
+            if (a.com_theta > 0.f) {
+                const int src_cell = __shfl_sync(0xffffffffu, cell, src);
+                const float4 c4 = a.nd.com[src_cell];
+                ok = ok && (!valid || com_guard(a, make_float4(gx, gy, gz, gw), c4, q.x, q.y, q.z));
+            }
             if (__all_sync(0xffffffffu, ok) && lane == src) {
                 qref = -cell - 1;
                 qcnt = 1;
@@ -1090,23 +1235,27 @@ traverse_warp_kernel(TravArgs a_in)
         }
         for (int c = 0; c < nchild; ++c) gstack[warp][sp + coff + c] = first_child + c;
         sp += ctotal;
-        // queue cells and leaf bodies, at most 16 entries per lane per round
+        // queue leaf bodies (front) and cells (back), at most 16 entries per
+        // lane per round
         while (__any_sync(0xffffffffu, qcnt > 0)) {
             const int take = min(qcnt, 16);
-            int qtotal;
-            const int qoff = warp_exclusive_scan(take, lane, qtotal);
-            if (nq + qtotal > kGQueue) flush();
-            if (qref < 0) {
-                if (take) queue[warp][nq + qoff] = qref;
+            const bool is_cell = qref < 0;
+            int btotal, ctotal;
+            const int boff = warp_exclusive_scan(is_cell ? 0 : take, lane, btotal);
+            const int coff = warp_exclusive_scan(is_cell ? take : 0, lane, ctotal);
+            if (nq + nc + btotal + ctotal > kGQueue) flush();
+            if (is_cell) {
+                if (take) queue[warp][kGQueue - 1 - (nc + coff)] = qref;
             } else {
-                for (int j = 0; j < take; ++j) queue[warp][nq + qoff + j] = qref + j;
+                for (int j = 0; j < take; ++j) queue[warp][nq + boff + j] = qref + j;
                 qref += take;
             }
             qcnt -= take;
-            nq += qtotal;
+            nq += btotal;
+            nc += ctotal;
         }
         __syncwarp();
-        if (nq >= 256) flush();
+        if (nq + nc >= 256) flush();
     }
     flush();
     if (lane == 0) {
@@ -1133,19 +1282,19 @@ struct BhWorkspace {
     int device = 0;
     size_t cap_n = 0;
     int grid_build = 0;  // blocks of the per-level build kernels
-    int grid_mom = 0;
     uint64_t *keys[2] = {nullptr, nullptr};
     uint32_t *vals[2] = {nullptr, nullptr};
-    uint32_t *hist = nullptr;
-    uint32_t *digit_totals = nullptr;
+    // sort_meta: [0, 2048) digit histograms of the 8 passes, [2048, 2056) tile
+    // counters, [2056] epoch; sort_status: look-back words, tiles x 256
+    uint32_t *sort_meta = nullptr;
+    unsigned long long *sort_status = nullptr;
     float4 *sbody = nullptr;
-    double *spos = nullptr, *smass = nullptr, *pref = nullptr, *mom_bsum = nullptr;
+    double *spos = nullptr, *smass = nullptr;
     NodeArrays nd = {};
     LevelInfo *lv = nullptr;
-    int32_t *bsum = nullptr;
+    unsigned long long *level_status = nullptr;  // look-back words of the level build
     unsigned long long *extent_bits = nullptr;
     unsigned long long *stats = nullptr;  // node visits, pair interactions of the last traversal
-    unsigned int *ticket = nullptr;       // last-block ticket of level_count_kernel (kept at 0)
     int32_t *top = nullptr;               // cell starts of the top tree level (see top_levels)
     int32_t *top_blockmin = nullptr;      // per-1024-cell minima while filling `top`
     uint32_t *flags = nullptr;
@@ -1160,13 +1309,14 @@ struct BhWorkspace {
 
 static void ws_release(BhWorkspace *ws)
 {
-    void *p[] = {ws->keys[0],  ws->keys[1],   ws->vals[0],       ws->vals[1],     ws->hist,
-                 ws->digit_totals,
-                 ws->sbody,    ws->spos,      ws->smass,         ws->pref,        ws->mom_bsum,
+    void *p[] = {ws->keys[0],  ws->keys[1],   ws->vals[0],       ws->vals[1],     ws->sort_meta,
+                 ws->sort_status,
+                 ws->sbody,    ws->spos,      ws->smass,      ws->nd.msum,
                  ws->nd.begin, ws->nd.count,  ws->nd.child,      ws->nd.nchild,   ws->nd.level,
-                 ws->nd.c64,   ws->nd.geo,    ws->nd.com,        ws->lv,          ws->bsum,
-                 ws->extent_bits, ws->flags, ws->nd.meta, ws->stats, ws->ticket,
-                 ws->top, ws->top_blockmin};
+                 ws->nd.c64,   ws->nd.geo,    ws->nd.com,        ws->lv,          ws->level_status,
+                 ws->extent_bits, ws->flags, ws->nd.meta, ws->stats,
+                 ws->top, ws->top_blockmin, ws->nd.parent, ws->nd.quad_a, ws->nd.quad_b,
+                 ws->nd.arrivals};
     for (void *q : p)
         if (q) cudaFree(q);
 }
@@ -1194,7 +1344,6 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf)
     w->cap_n = cap;
     const int sms = device_sm_count(device);
     w->grid_build = sms * 2;
-    w->grid_mom = sms * 2;
     const int tiles = cdiv((long long)cap, kSortTile);
     // Node capacity: leaves hold about leaf/4 bodies on average, so 8N/leaf
     // (at most 4N) nodes hold every non-degenerate distribution; deeper
@@ -1208,13 +1357,11 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf)
     PG_WA(w->keys[1], cap);
     PG_WA(w->vals[0], cap);
     PG_WA(w->vals[1], cap);
-    PG_WA(w->hist, (size_t)kRadixBuckets * tiles);
-    PG_WA(w->digit_totals, kRadixBuckets);
+    PG_WA(w->sort_meta, (size_t)kSortPasses * kRadixBuckets + kSortPasses + 1);
+    PG_WA(w->sort_status, (size_t)kRadixBuckets * tiles);
     PG_WA(w->sbody, cap);
     PG_WA(w->spos, 3 * cap);
     PG_WA(w->smass, cap);
-    PG_WA(w->pref, 4 * (cap + 1));
-    PG_WA(w->mom_bsum, 4 * (size_t)w->grid_mom);
     PG_WA(w->nd.begin, ncap);
     PG_WA(w->nd.count, ncap);
     PG_WA(w->nd.child, ncap);
@@ -1224,18 +1371,32 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf)
     PG_WA(w->nd.geo, ncap);
     PG_WA(w->nd.com, ncap);
     PG_WA(w->nd.meta, ncap);
+    PG_WA(w->nd.parent, ncap);
+    PG_WA(w->nd.msum, ncap);
+    PG_WA(w->nd.quad_a, ncap);
+    PG_WA(w->nd.quad_b, ncap);
+    PG_WA(w->nd.arrivals, ncap);
     PG_WA(w->stats, 4);
-    PG_WA(w->ticket, 1);
     PG_WA(w->top, (size_t)(1 << 15) + 1);
     PG_WA(w->top_blockmin, 32);
     PG_WA(w->lv, 1);
-    PG_WA(w->bsum, (size_t)w->grid_build);
+    PG_WA(w->level_status, ncap / kBuildThreads + 2);
     PG_WA(w->extent_bits, 1);
     PG_WA(w->flags, 4);
 #undef PG_WA
     w->nd.cap = (int)ncap;
     if (rc == PHYSIM_OK && (cudaMemset(w->flags, 0, 4 * sizeof(uint32_t)) != cudaSuccess ||
-                            cudaMemset(w->ticket, 0, sizeof(unsigned int)) != cudaSuccess))
+                            cudaMemset(w->nd.arrivals, 0, ncap * sizeof(uint32_t)) != cudaSuccess ||
+                            cudaMemset(w->lv, 0, sizeof(LevelInfo)) != cudaSuccess ||
+                            cudaMemset(w->level_status, 0,
+                                       (ncap / kBuildThreads + 2) * sizeof(unsigned long long)) !=
+                                cudaSuccess ||
+                            cudaMemset(w->sort_meta, 0,
+                                       ((size_t)kSortPasses * kRadixBuckets + kSortPasses + 1) *
+                                           sizeof(uint32_t)) != cudaSuccess ||
+                            cudaMemset(w->sort_status, 0,
+                                       (size_t)kRadixBuckets * tiles *
+                                           sizeof(unsigned long long)) != cudaSuccess))
         rc = PHYSIM_ERR_CUDA;
     if (rc != PHYSIM_OK) {
         ws_release(w);
@@ -1276,6 +1437,24 @@ int bh_traversal_ms(BhWorkspace *ws, double *ms)
 
 int bh_launches(const BhWorkspace *ws) { return ws ? ws->launches : 0; }
 
+int bh_check(BhWorkspace *ws, cudaStream_t st)
+{
+    if (!ws) return PHYSIM_OK;
+    uint32_t f[4];
+    PG_CUDA(cudaMemcpyAsync(f, ws->flags, sizeof f, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    if (f[kFlagStack] == 0 && f[kFlagSort] == 0) return PHYSIM_OK;
+    PG_CUDA(cudaMemsetAsync(ws->flags + kFlagStack, 0, 2 * sizeof(uint32_t), st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    if (f[kFlagSort]) {
+        set_error("Barnes-Hut build: a look-back wait (radix sort or tree level) gave up; "
+                  "results are invalid");
+        return PHYSIM_ERR_TIMEOUT;
+    }
+    set_error("Barnes-Hut traversal stack overflow; results are invalid");
+    return PHYSIM_ERR_TREE;
+}
+
 int bh_stats(BhWorkspace *ws, cudaStream_t st, uint64_t out[2])
 {
     PG_CHECK(ws && out, PHYSIM_ERR_ARGUMENT, "null argument");
@@ -1294,22 +1473,23 @@ static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, c
     PG_CUDA(cudaMemsetAsync(ws->extent_bits, 0, sizeof(unsigned long long), st));
     const int sms = device_sm_count(ws->device);
     extent_kernel<<<sms * 2, 256, 0, st>>>(b.x, b.y, b.z, n, ws->extent_bits);
-    keys_kernel<<<cdiv(n, 256), 256, 0, st>>>(b.x, b.y, b.z, n, p.nchild, ws->extent_bits,
-                                              ws->keys[0], ws->vals[0]);
+    uint32_t *ghist = ws->sort_meta;
+    uint32_t *tile_ctr = ws->sort_meta + kSortPasses * kRadixBuckets;
+    uint32_t *epoch = tile_ctr + kSortPasses;
+    PG_CUDA(cudaMemsetAsync(ghist, 0, kSortPasses * kRadixBuckets * sizeof(uint32_t), st));
+    keys_kernel<<<std::min(cdiv(n, 256), sms * 8), 256, 0, st>>>(
+        b.x, b.y, b.z, n, p.nchild, ws->extent_bits, ws->keys[0], ws->vals[0], ghist, tile_ctr,
+        epoch);
     launches += 2;
-    // radix sort
+    // one-sweep radix sort: one launch per 8-bit digit
     const int tiles = cdiv(n, kSortTile);
-    const int key_bits = tree_levels(p.nchild) * level_bits(p.nchild);
     int cur = 0;
-    for (int shift = 0; shift < key_bits; shift += kRadixBits) {
-        radix_hist_kernel<<<tiles, kSortThreads, 0, st>>>(ws->keys[cur], n, shift, ws->hist, tiles);
-        radix_digit_scan_kernel<<<kRadixBuckets, kSortThreads, 0, st>>>(ws->hist, tiles,
-                                                                        ws->digit_totals);
-        radix_scatter_kernel<<<tiles, kSortThreads, 0, st>>>(
-            ws->keys[cur], shift == 0 ? nullptr : ws->vals[cur], ws->keys[cur ^ 1],
-            ws->vals[cur ^ 1], n, shift, ws->hist, tiles, ws->digit_totals);
+    for (int pass = 0; pass < kSortPasses; ++pass) {
+        radix_pass_kernel<<<tiles, kSortThreads, 0, st>>>(
+            ws->keys[cur], pass == 0 ? nullptr : ws->vals[cur], ws->keys[cur ^ 1],
+            ws->vals[cur ^ 1], n, pass, ghist, tile_ctr, ws->sort_status, epoch, ws->flags);
         cur ^= 1;
-        launches += 3;
+        launches += 1;
     }
     ws->sorted = cur;
     gather_kernel<<<cdiv(n, 256), 256, 0, st>>>(ws->vals[cur], n, b.body4, b.x, b.y, b.z, b.m,
@@ -1326,20 +1506,14 @@ static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, c
     top_fill_kernel<<<top_cells / 1024, 1024, 0, st>>>(ws->top, top_cells, n, ws->top_blockmin);
     launches += 3;
     for (int level = 0; level < D; ++level) {
-        level_count_kernel<<<ws->grid_build, kBuildThreads, 0, st>>>(
-            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->top, ws->bsum,
-            ws->ticket, ws->flags);
-        level_write_kernel<<<ws->grid_build, kBuildThreads, 0, st>>>(
-            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->top, ws->bsum);
-        launches += 2;
+        level_kernel<<<ws->grid_build, kBuildThreads, 0, st>>>(
+            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->top,
+            ws->level_status, ws->flags);
+        launches += 1;
     }
-    moment_partial_kernel<<<ws->grid_mom, kMomThreads, 0, st>>>(ws->spos, ws->smass, n,
-                                                                ws->mom_bsum);
-    moment_blockscan_kernel<<<1, 128, 0, st>>>(ws->mom_bsum, ws->grid_mom);
-    moment_scan_kernel<<<ws->grid_mom, kMomThreads, 0, st>>>(ws->spos, ws->smass, n, ws->mom_bsum,
-                                                             ws->pref);
-    node_finish_kernel<<<sms * 4, 256, 0, st>>>(ws->nd, ws->lv, ws->pref, n, ws->sbody, ws->spos);
-    launches += 4;
+    moments_kernel<<<sms * 4, 256, 0, st>>>(ws->nd, ws->lv, ws->sbody, ws->spos, ws->smass, n,
+                                            p.multipole == kMultipoleQuadrupole ? 1 : 0);
+    launches += 1;
     PG_CUDA(cudaGetLastError());
     ws->launches = launches;
     return PHYSIM_OK;
@@ -1369,13 +1543,17 @@ int bh_accelerations(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, 
     a.extent = 0.f;  // read on the device from extent_bits
     a.extent_bits = ws->extent_bits;
     a.stats = ws->stats;
+    a.quad = p.multipole == kMultipoleQuadrupole ? 1 : 0;
+    a.com_theta = (float)p.com_theta;
     PG_CUDA(cudaMemsetAsync(ws->stats, 0, 2 * sizeof(unsigned long long), st));
     const int blocks = cdiv(cdiv(n, 32), kTravWarps);
     // external records, so they also time the kernel when replayed from a graph
     if (ws->profiling)
         PG_CUDA(cudaEventRecordWithFlags(ws->trav_ev[0], st, cudaEventRecordExternal));
-    if (p.traversal == PHYSIM_TRAVERSAL_WARP)
-        traverse_warp_kernel<<<blocks, kTravWarps * 32, 0, st>>>(a);
+    if (p.traversal == PHYSIM_TRAVERSAL_WARP && a.quad)
+        traverse_warp_kernel<true><<<blocks, kTravWarps * 32, 0, st>>>(a);
+    else if (p.traversal == PHYSIM_TRAVERSAL_WARP)
+        traverse_warp_kernel<false><<<blocks, kTravWarps * 32, 0, st>>>(a);
     else
         traverse_exact_kernel<<<blocks, kTravWarps * 32, 0, st>>>(a);
     PG_CUDA(cudaGetLastError());
@@ -1401,7 +1579,7 @@ int bh_snapshot(BhWorkspace *ws, size_t n, cudaStream_t st, PhysimTreeSnapshot *
     out->extent = X;
     out->n_bodies = n;
     out->n_nodes = (size_t)lv.total;
-    out->flags = flags[kFlagNodes] | (flags[kFlagStack] << 1);
+    out->flags = flags[kFlagNodes] | (flags[kFlagStack] << 1) | (flags[kFlagSort] << 2);
     const size_t nn = out->n_nodes < out->cap_nodes ? out->n_nodes : out->cap_nodes;
     auto cp = [&](void *dst, const void *src, size_t bytes) -> int {
         if (dst && bytes) PG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
@@ -1419,6 +1597,10 @@ int bh_snapshot(BhWorkspace *ws, size_t n, cudaStream_t st, PhysimTreeSnapshot *
             PG_TRY(cp(out->node_centre + c * nn, ws->nd.c64 + (size_t)c * ws->nd.cap,
                       nn * sizeof(double)));
     PG_TRY(cp(out->node_com, ws->nd.com, nn * sizeof(float4)));
+    if (out->node_quad) {
+        PG_TRY(cp(out->node_quad, ws->nd.quad_a, nn * sizeof(float4)));
+        PG_TRY(cp(out->node_quad + 4 * nn, ws->nd.quad_b, nn * sizeof(float4)));
+    }
     PG_CUDA(cudaStreamSynchronize(st));
     return PHYSIM_OK;
 }

@@ -63,11 +63,14 @@ static int accumulate_locked(ElementState *el, const Entity *state, size_t n, Ac
         p.e = el->e;
         p.leaf_size = el->leaf_size;
         p.traversal = el->traversal;
+        p.multipole = el->multipole;
+        p.com_theta = el->com_theta;
         PG_TRY(bh_accelerations(el->bh, el->bodies, p, el->partial, st));
     }
     PG_TRY(launch_accumulate_aos(el->bodies, el->partial, splits, el->d_acc, st));
     PG_CUDA(cudaMemcpyAsync(acc, el->d_acc, n * sizeof(Acceleration), cudaMemcpyDeviceToHost, st));
     PG_CUDA(cudaStreamSynchronize(st));
+    if (tree) PG_TRY(bh_check(el->bh, st));
     return PHYSIM_OK;
 }
 

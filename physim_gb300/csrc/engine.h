@@ -87,6 +87,22 @@ int launch_combine_soa(const DeviceBodies &b, const double *partial, int splits,
 int launch_verlet(DeviceBodies &b, const double *partial, int splits, double dt, bool initial,
                   cudaStream_t stream);
 
+// Euler step (euler.rs:17-49) fused with the combine of the partial sums.
+int launch_euler(DeviceBodies &b, const double *partial, int splits, double dt,
+                 cudaStream_t stream);
+// RK4 stage 1..4 (rk4.rs:24-178) after the forces of the stage state: saves
+// the entity state (stage 1, `save`: 6 x n f64), accumulates the k's (`ksum`:
+// 6 x n f64) and writes the next stage state, or the new state at stage 4,
+// to the f64 state and the f32 body copy.
+int launch_rk4_stage(DeviceBodies &b, const double *partial, int splits, double dt, int stage,
+                     double *save, double *ksum, cudaStream_t stream);
+// Euler and RK4 stages over explicit Entity arrays (host-array integrators).
+int launch_euler_aos(const Entity *d_in, Entity *d_out, const Acceleration *d_acc, size_t n,
+                     double dt, cudaStream_t stream);
+int launch_rk4_aos_stage(const Entity *d_ent, const Entity *d_q, const Acceleration *d_f,
+                         double *ksum, Entity *d_out, size_t n, double dt, int stage,
+                         cudaStream_t stream);
+
 // Verlet over explicit device arrays (the host-array integrator path).
 int launch_verlet_aos(const Entity *d_in, const Entity *d_prev, Entity *d_out,
                       const Acceleration *d_acc, size_t n, double dt, bool initial,

@@ -36,6 +36,7 @@ struct MemberInfo {
     int32_t splits;
     float e;
     double dt;
+    double rdt;  // RN(1/dt), for the velocity division (div_rn_by)
 };
 
 struct WorkUnit {
@@ -108,7 +109,7 @@ __global__ void ensemble_verlet_kernel(float4 *body4, const double *__restrict__
             vn = __dadd_rn(v[c], __dmul_rn(a[c], dt));
         } else {
             xn = __dadd_rn(__dsub_rn(__dmul_rn(2.0, q[c]), pr[c]), __dmul_rn(a[c], dt2));
-            vn = __ddiv_rn(__dsub_rn(xn, q[c]), dt);
+            vn = div_rn_by(__dsub_rn(xn, q[c]), dt, m.rdt);
         }
         pr[c] = q[c];
         q[c] = xn;
@@ -374,6 +375,7 @@ int physim_gpu_ensemble_create(const PhysimSimConfig *cfg, const size_t *sizes, 
         mi.n = (int32_t)sizes[k];
         mi.e = (float)E->cfg.e;
         mi.dt = E->cfg.dt;
+        mi.rdt = 1.0 / E->cfg.dt;
         E->members[k] = mi;
         slots += (long long)pad_bodies(sizes[k]);
         partial_elems += 3LL * (long long)sizes[k] * cdiv((long long)sizes[k], kMinChunk);
@@ -484,6 +486,7 @@ int physim_gpu_ensemble_set_member(PhysimEnsemble *E, size_t index, double e, do
     PG_CUDA(cudaSetDevice(E->device));
     E->members[index].e = (float)fabs(e);
     E->members[index].dt = dt;
+    E->members[index].rdt = 1.0 / dt;
     PG_CUDA(cudaMemcpyAsync(E->d_members + index, &E->members[index], sizeof(MemberInfo),
                             cudaMemcpyHostToDevice, E->stream));
     const unsigned long long r = steps_remaining;

@@ -1,5 +1,6 @@
-// integrate.cu -- body staging and the verlet integrator
-// (integrators/src/verlet.rs:24-107) on the device.
+// integrate.cu -- body staging and the integrators on the device: verlet
+// (integrators/src/verlet.rs:24-107), euler (integrators/src/euler.rs:17-49)
+// and rk4 (integrators/src/rk4.rs:24-178).
 //
 // The integrator runs in f64 with the reference's operation order, written
 // with explicit round-to-nearest intrinsics so the compiler cannot contract
@@ -113,8 +114,9 @@ __global__ void combine_soa_kernel(const double *__restrict__ mass, const uint8_
 }
 
 // verlet.rs:33-39 (initial, Taylor step) and verlet.rs:64-70 (regular).
+// rdt = RN(1/dt) for the division (x' - x) / dt (see div_rn_by).
 __device__ __forceinline__ void verlet_axis(double &x, double &v, double &p, double a, double dt,
-                                            double dt2, bool initial)
+                                            double dt2, bool initial, double rdt)
 {
     double xn, vn;
     if (initial) {
@@ -124,7 +126,7 @@ __device__ __forceinline__ void verlet_axis(double &x, double &v, double &p, dou
     } else {
         // 2*x - prev + a*dt^2 ; (x' - x)/dt
         xn = __dadd_rn(__dsub_rn(__dmul_rn(2.0, x), p), __dmul_rn(a, dt2));
-        vn = __ddiv_rn(__dsub_rn(xn, x), dt);
+        vn = div_rn_by(__dsub_rn(xn, x), dt, rdt);
     }
     p = x;
     x = xn;
@@ -135,7 +137,7 @@ __global__ void verlet_kernel(float4 *body4, const double *mass, const uint8_t *
                               const double *partial,
                               int splits, int n, double *x, double *y, double *z, double *vx,
                               double *vy, double *vz, double *px, double *py, double *pz,
-                              double dt, int initial)
+                              double dt, double rdt, int initial)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -146,9 +148,9 @@ __global__ void verlet_kernel(float4 *body4, const double *mass, const uint8_t *
     double xi = x[i], yi = y[i], zi = z[i];
     double vxi = vx[i], vyi = vy[i], vzi = vz[i];
     double pxi = px[i], pyi = py[i], pzi = pz[i];
-    verlet_axis(xi, vxi, pxi, ax, dt, dt2, initial);
-    verlet_axis(yi, vyi, pyi, ay, dt, dt2, initial);
-    verlet_axis(zi, vzi, pzi, az, dt, dt2, initial);
+    verlet_axis(xi, vxi, pxi, ax, dt, dt2, initial, rdt);
+    verlet_axis(yi, vyi, pyi, ay, dt, dt2, initial, rdt);
+    verlet_axis(zi, vzi, pzi, az, dt, dt2, initial, rdt);
     x[i] = xi; y[i] = yi; z[i] = zi;
     vx[i] = vxi; vy[i] = vyi; vz[i] = vzi;
     px[i] = pxi; py[i] = pyi; pz[i] = pzi;
@@ -159,7 +161,8 @@ __global__ void verlet_kernel(float4 *body4, const double *mass, const uint8_t *
 }
 
 __global__ void verlet_aos_kernel(const Entity *in, const Entity *prev, Entity *out,
-                                  const Acceleration *acc, int n, double dt, int initial)
+                                  const Acceleration *acc, int n, double dt, double rdt,
+                                  int initial)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -172,10 +175,156 @@ __global__ void verlet_aos_kernel(const Entity *in, const Entity *prev, Entity *
         py = prev[i].y;
         pz = prev[i].z;
     }
-    verlet_axis(en.x, en.vx, px, a.x, dt, dt2, initial);
-    verlet_axis(en.y, en.vy, py, a.y, dt, dt2, initial);
-    verlet_axis(en.z, en.vz, pz, a.z, dt, dt2, initial);
+    verlet_axis(en.x, en.vx, px, a.x, dt, dt2, initial, rdt);
+    verlet_axis(en.y, en.vy, py, a.y, dt, dt2, initial, rdt);
+    verlet_axis(en.z, en.vz, pz, a.z, dt, dt2, initial, rdt);
     out[i] = en;
+}
+
+// euler.rs:29-37: x + vx*dt + 0.5*a*dt^2 ; vx + a*dt for every body.  A fixed
+// body has a = 0 (transforms skip it) and still drifts with its velocity.
+__global__ void euler_kernel(float4 *body4, const double *mass, const uint8_t *fixed,
+                             const double *partial, int splits, int n, double *x, double *y,
+                             double *z, double *vx, double *vy, double *vz, double dt)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 b = body4[i];
+    double ax, ay, az;
+    body_acc(partial, splits, n, i, fixed[i] != 0, mass[i], ax, ay, az);
+    const double dt2 = __dmul_rn(dt, dt);
+    double xi = x[i], yi = y[i], zi = z[i];
+    double vxi = vx[i], vyi = vy[i], vzi = vz[i];
+    double unused = 0.0;
+    verlet_axis(xi, vxi, unused, ax, dt, dt2, true, 0.0);
+    verlet_axis(yi, vyi, unused, ay, dt, dt2, true, 0.0);
+    verlet_axis(zi, vzi, unused, az, dt, dt2, true, 0.0);
+    x[i] = xi; y[i] = yi; z[i] = zi;
+    vx[i] = vxi; vy[i] = vyi; vz[i] = vzi;
+    b.x = (float)xi;
+    b.y = (float)yi;
+    b.z = (float)zi;
+    body4[i] = b;
+}
+
+// One RK4 stage (rk4.rs:33-178) for body i, given the stage state q (x, y, z,
+// vx, vy, vz), its acceleration a, the entity's own state e and the running
+// sum S of the k's.  k = (dt v_q, dt a) (rk4.rs:40-46); S accumulates
+// k1 + 2 k2 + 2 k3 + k4 left to right, as rk4.rs:160-165 evaluates it.
+// Stages 1-3 return the next stage state e + k/2 (stages 1, 2) or e + k
+// (stage 3); stage 4 returns the new state e + S/6, or (e, v = 0) for a fixed
+// body (rk4.rs:165-171).
+__device__ __forceinline__ void rk4_stage(int stage, const double q[6], const double a[3],
+                                          const double e[6], double S[6], bool fixed, double dt,
+                                          double out[6])
+{
+    double k[6];
+    for (int c = 0; c < 3; ++c) {
+        k[c] = __dmul_rn(dt, q[3 + c]);
+        k[3 + c] = __dmul_rn(dt, a[c]);
+    }
+    for (int c = 0; c < 6; ++c) {
+        if (stage == 1)
+            S[c] = k[c];
+        else if (stage == 4)
+            S[c] = __dadd_rn(S[c], k[c]);
+        else
+            S[c] = __dadd_rn(S[c], __dmul_rn(2.0, k[c]));
+    }
+    if (stage < 3) {
+        for (int c = 0; c < 6; ++c) out[c] = __dadd_rn(e[c], __dmul_rn(0.5, k[c]));
+    } else if (stage == 3) {
+        for (int c = 0; c < 6; ++c) out[c] = __dadd_rn(e[c], k[c]);
+    } else if (!fixed) {
+        for (int c = 0; c < 6; ++c) out[c] = __dadd_rn(e[c], __ddiv_rn(S[c], 6.0));
+    } else {
+        for (int c = 0; c < 3; ++c) {
+            out[c] = e[c];
+            out[3 + c] = 0.0;
+        }
+    }
+}
+
+// Device-resident RK4 stage: the stage state is in (x .. vz) and body4; the
+// entity's state is saved in `save` at stage 1; S lives in `ksum`.  Writes
+// the next stage state (or the new state) back to (x .. vz) and body4, so
+// the next force evaluation reads it like any other state.
+__global__ void rk4_stage_kernel(float4 *body4, const double *mass, const uint8_t *fixed,
+                                 const double *partial, int splits, int n, double *x, double *y,
+                                 double *z, double *vx, double *vy, double *vz, double *save,
+                                 double *ksum, double dt, int stage)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const bool fx = fixed[i] != 0;
+    double a[3];
+    body_acc(partial, splits, n, i, fx, mass[i], a[0], a[1], a[2]);
+    double *st[6] = {x, y, z, vx, vy, vz};
+    double q[6], e[6], S[6], out[6];
+    for (int c = 0; c < 6; ++c) q[c] = st[c][i];
+    if (stage == 1) {
+        for (int c = 0; c < 6; ++c) {
+            e[c] = q[c];
+            save[(size_t)c * n + i] = q[c];
+        }
+    } else {
+        for (int c = 0; c < 6; ++c) {
+            e[c] = save[(size_t)c * n + i];
+            S[c] = ksum[(size_t)c * n + i];
+        }
+    }
+    rk4_stage(stage, q, a, e, S, fx, dt, out);
+    if (stage < 4)
+        for (int c = 0; c < 6; ++c) ksum[(size_t)c * n + i] = S[c];
+    for (int c = 0; c < 6; ++c) st[c][i] = out[c];
+    float4 b = body4[i];
+    b.x = (float)out[0];
+    b.y = (float)out[1];
+    b.z = (float)out[2];
+    body4[i] = b;
+}
+
+__global__ void euler_aos_kernel(const Entity *in, Entity *out, const Acceleration *acc, int n,
+                                 double dt)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Entity en = in[i];
+    const Acceleration a = acc[i];
+    const double dt2 = __dmul_rn(dt, dt);
+    double unused = 0.0;
+    verlet_axis(en.x, en.vx, unused, a.x, dt, dt2, true, 0.0);
+    verlet_axis(en.y, en.vy, unused, a.y, dt, dt2, true, 0.0);
+    verlet_axis(en.z, en.vz, unused, a.z, dt, dt2, true, 0.0);
+    out[i] = en;
+}
+
+// RK4 stage over Entity arrays: `ent` the entities, `q` the stage state, f
+// its accelerations; writes the next stage state (stages 1-3: the entity with
+// x, v replaced, rk4.rs:50-62) or the new state (stage 4) to `out`, which may
+// alias q.
+__global__ void rk4_aos_stage_kernel(const Entity *ent, const Entity *q_in,
+                                     const Acceleration *f, double *ksum, Entity *out, int n,
+                                     double dt, int stage)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Entity en = ent[i];
+    const Entity qe = q_in[i];
+    const Acceleration fa = f[i];
+    const double q[6] = {qe.x, qe.y, qe.z, qe.vx, qe.vy, qe.vz};
+    const double e[6] = {en.x, en.y, en.z, en.vx, en.vy, en.vz};
+    const double a[3] = {fa.x, fa.y, fa.z};
+    double S[6] = {0, 0, 0, 0, 0, 0}, r[6];
+    if (stage > 1)
+        for (int c = 0; c < 6; ++c) S[c] = ksum[(size_t)c * n + i];
+    rk4_stage(stage, q, a, e, S, en.fixed, dt, r);
+    if (stage < 4)
+        for (int c = 0; c < 6; ++c) ksum[(size_t)c * n + i] = S[c];
+    Entity o = en;
+    o.x = r[0]; o.y = r[1]; o.z = r[2];
+    o.vx = r[3]; o.vy = r[4]; o.vz = r[5];
+    out[i] = o;
 }
 
 template <typename T>
@@ -273,7 +422,51 @@ int launch_verlet(DeviceBodies &b, const double *partial, int splits, double dt,
     if (b.n == 0) return PHYSIM_OK;
     verlet_kernel<<<blocks_for(b.n), kThreads, 0, stream>>>(
         b.body4, b.m, b.fixed, partial, splits, (int)b.n, b.x, b.y, b.z, b.vx, b.vy, b.vz, b.px, b.py,
-        b.pz, dt, initial ? 1 : 0);
+        b.pz, dt, 1.0 / dt, initial ? 1 : 0);
+    PG_CUDA(cudaGetLastError());
+    return PHYSIM_OK;
+}
+
+int launch_euler(DeviceBodies &b, const double *partial, int splits, double dt,
+                 cudaStream_t stream)
+{
+    if (b.n == 0) return PHYSIM_OK;
+    euler_kernel<<<blocks_for(b.n), kThreads, 0, stream>>>(b.body4, b.m, b.fixed, partial, splits,
+                                                           (int)b.n, b.x, b.y, b.z, b.vx, b.vy,
+                                                           b.vz, dt);
+    PG_CUDA(cudaGetLastError());
+    return PHYSIM_OK;
+}
+
+int launch_rk4_stage(DeviceBodies &b, const double *partial, int splits, double dt, int stage,
+                     double *save, double *ksum, cudaStream_t stream)
+{
+    if (b.n == 0) return PHYSIM_OK;
+    PG_CHECK(stage >= 1 && stage <= 4, PHYSIM_ERR_ARGUMENT, "rk4 stage %d", stage);
+    rk4_stage_kernel<<<blocks_for(b.n), kThreads, 0, stream>>>(
+        b.body4, b.m, b.fixed, partial, splits, (int)b.n, b.x, b.y, b.z, b.vx, b.vy, b.vz, save,
+        ksum, dt, stage);
+    PG_CUDA(cudaGetLastError());
+    return PHYSIM_OK;
+}
+
+int launch_euler_aos(const Entity *d_in, Entity *d_out, const Acceleration *d_acc, size_t n,
+                     double dt, cudaStream_t stream)
+{
+    if (n == 0) return PHYSIM_OK;
+    euler_aos_kernel<<<blocks_for(n), kThreads, 0, stream>>>(d_in, d_out, d_acc, (int)n, dt);
+    PG_CUDA(cudaGetLastError());
+    return PHYSIM_OK;
+}
+
+int launch_rk4_aos_stage(const Entity *d_ent, const Entity *d_q, const Acceleration *d_f,
+                         double *ksum, Entity *d_out, size_t n, double dt, int stage,
+                         cudaStream_t stream)
+{
+    if (n == 0) return PHYSIM_OK;
+    PG_CHECK(stage >= 1 && stage <= 4, PHYSIM_ERR_ARGUMENT, "rk4 stage %d", stage);
+    rk4_aos_stage_kernel<<<blocks_for(n), kThreads, 0, stream>>>(d_ent, d_q, d_f, ksum, d_out,
+                                                                 (int)n, dt, stage);
     PG_CUDA(cudaGetLastError());
     return PHYSIM_OK;
 }
@@ -284,7 +477,7 @@ int launch_verlet_aos(const Entity *d_in, const Entity *d_prev, Entity *d_out,
 {
     if (n == 0) return PHYSIM_OK;
     verlet_aos_kernel<<<blocks_for(n), kThreads, 0, stream>>>(d_in, d_prev, d_out, d_acc, (int)n,
-                                                              dt, initial ? 1 : 0);
+                                                              dt, 1.0 / dt, initial ? 1 : 0);
     PG_CUDA(cudaGetLastError());
     return PHYSIM_OK;
 }

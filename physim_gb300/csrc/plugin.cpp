@@ -329,6 +329,13 @@ static ElementState *element_new(int kind, const uint8_t *config, uintptr_t len)
     el->traversal = PHYSIM_TRAVERSAL_EXACT;
     if (it != props.end() && it->second.kind == json::Value::String && it->second.str == "warp")
         el->traversal = PHYSIM_TRAVERSAL_WARP;
+    auto qd = props.find("quadrupole");
+    el->multipole = (qd != props.end() && qd->second.kind == json::Value::Bool &&
+                     qd->second.boolean)
+                        ? kMultipoleQuadrupole
+                        : kMultipoleMonopole;
+    const double ct = num("com_theta", 0.0);
+    el->com_theta = ct > 0.0 ? ct : 0.0;
     return el;
 }
 
@@ -375,6 +382,10 @@ static char *element_descriptions(int kind, void *obj, RustStringAllocFn alloc)
              "reference tree. Default=1\",";
         s += "\"traversal\":\"exact: every body uses its own interaction list; warp: a cell is "
              "accepted only when all 32 bodies of a warp accept it. Default=exact\",";
+        s += "\"quadrupole\":\"true adds each accepted cell's quadrupole moment to its "
+             "monopole. Default=false\",";
+        s += "\"com_theta\":\"If > 0, a cell is also opened unless its bodies lie within "
+             "com_theta times the distance to its centre of mass. Default=0 (off)\",";
     }
     s += "\"e\":\"Easing factor. Modify G*Ma*Mb*(r-e)^-2. Default=1.0\",";
     s += "\"device\":\"CUDA device ordinal. Default=0\"}";

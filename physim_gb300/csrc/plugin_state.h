@@ -11,12 +11,17 @@ namespace pg {
 
 struct BhWorkspace;
 
+constexpr int kMultipoleMonopole = 0;
+constexpr int kMultipoleQuadrupole = 1;
+
 struct ElementState {
     int kind = 0;  // 0 simple_astro, 1 astro2, 2 astro
     double theta = 1.0;
     double e = 1.0;
     int leaf_size = 1;
     int traversal = PHYSIM_TRAVERSAL_EXACT;
+    int multipole = 0;       // kMultipoleMonopole / kMultipoleQuadrupole
+    double com_theta = 0.0;  // centre-of-mass guard, 0 = off
     int device = 0;
 
     // GPU resources, created by the first transform.
@@ -47,9 +52,18 @@ struct BhParams {
     int leaf_size = 1;
     int traversal = PHYSIM_TRAVERSAL_EXACT;
     bool compensated = true;
+    // Accuracy options beyond the reference (defaults: off, the reference's
+    // monopole cells and opening rule): quadrupole correction of accepted
+    // cells, and the centre-of-mass guard b_max < com_theta |x - c|.
+    int multipole = kMultipoleMonopole;
+    double com_theta = 0.0;
 };
 
 int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf);
+// Waits for the stream, then reports (and clears) the error flags the kernels
+// raise: PHYSIM_ERR_TREE for a traversal stack overflow, PHYSIM_ERR_TIMEOUT
+// for a radix-sort look-back wait that gave up.
+int bh_check(BhWorkspace *ws, cudaStream_t st);
 void bh_free(BhWorkspace *ws);
 // Accelerations of the bodies in b (f64 positions and f32 copies must be
 // current) into partial[c*n + i] (one split).

@@ -39,6 +39,22 @@ struct PhysimSim {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     double *diag = nullptr;  // 9 f64 diagnostics sums
+    // rk4 (rk4.rs:24-178): the entity state saved at stage 1 and the running
+    // sum of the k's, 6 x n f64 each
+    double *rk4_save = nullptr, *rk4_ksum = nullptr;
+};
+
+struct PhysimIntegrator {
+    uint32_t kind = 0;
+    int device = 0;
+    PhysimVerlet *verlet = nullptr;  // kind == verlet: previous_state lives here
+    cudaStream_t stream = nullptr;
+    Entity *d_ent = nullptr, *d_q = nullptr;  // entities, stage state
+    Acceleration *d_acc = nullptr;
+    double *d_ksum = nullptr;  // rk4 running sum of the k's, 6 x n
+    Entity *h_q = nullptr;     // pinned host copy of the stage state for acc_fn
+    Acceleration *h_acc = nullptr;
+    size_t cap = 0;
 };
 
 struct PhysimVerlet {
@@ -70,6 +86,9 @@ int sim_forces(PhysimSim *s, int *splits_out)
     p.leaf_size = (int)c.leaf_size;
     p.traversal = (int)c.traversal;
     p.compensated = c.compensated != 0;
+    p.multipole = c.multipole == PHYSIM_MULTIPOLE_QUADRUPOLE ? kMultipoleQuadrupole
+                                                             : kMultipoleMonopole;
+    p.com_theta = c.com_theta;
     *splits_out = 1;
     (void)n;
     return bh_accelerations(s->bh, s->b, p, s->partial, s->stream);
@@ -127,6 +146,7 @@ void physim_gpu_sim_config_default(PhysimSimConfig *cfg)
     cfg->dt = 1e-6;
     cfg->stream = nullptr;
     cfg->device = 0;
+    cfg->integrator = PHYSIM_INTEGRATOR_VERLET;
 }
 
 int physim_gpu_sim_create(const PhysimSimConfig *cfg, size_t n, PhysimSim **out)
@@ -139,8 +159,12 @@ int physim_gpu_sim_create(const PhysimSimConfig *cfg, size_t n, PhysimSim **out)
              "leaf_size %u outside 1..64", cfg->leaf_size);
     PG_CHECK(cfg->traversal <= PHYSIM_TRAVERSAL_WARP, PHYSIM_ERR_ARGUMENT, "unknown traversal");
     PG_CHECK(n < (size_t)INT32_MAX, PHYSIM_ERR_ARGUMENT, "too many bodies: %zu", n);
-    PG_CHECK(cfg->reserved[0] == 0 && cfg->reserved[1] == 0 && cfg->reserved[2] == 0,
-             PHYSIM_ERR_ARGUMENT, "reserved fields must be zero");
+    PG_CHECK(cfg->integrator <= PHYSIM_INTEGRATOR_RK4, PHYSIM_ERR_ARGUMENT,
+             "unknown integrator %u", cfg->integrator);
+    PG_CHECK(cfg->multipole <= PHYSIM_MULTIPOLE_QUADRUPOLE, PHYSIM_ERR_ARGUMENT,
+             "unknown multipole order %u", cfg->multipole);
+    PG_CHECK(cfg->com_theta >= 0.f && cfg->com_theta == cfg->com_theta, PHYSIM_ERR_ARGUMENT,
+             "com_theta must be >= 0");
     PG_CUDA(cudaSetDevice(cfg->device));
     PhysimSim *s = new (std::nothrow) PhysimSim();
     PG_CHECK(s, PHYSIM_ERR_MEMORY, "out of host memory");
@@ -172,6 +196,14 @@ int physim_gpu_sim_create(const PhysimSimConfig *cfg, size_t n, PhysimSim **out)
         rc = PHYSIM_ERR_MEMORY;
     }
     s->partial_cap = partial_elems;
+    if (rc == PHYSIM_OK && cfg->integrator == PHYSIM_INTEGRATOR_RK4) {
+        const size_t m = 6 * (n ? n : 1) * sizeof(double);
+        if (cudaMalloc((void **)&s->rk4_save, m) != cudaSuccess ||
+            cudaMalloc((void **)&s->rk4_ksum, m) != cudaSuccess) {
+            set_error("cudaMalloc of the rk4 stage arrays failed");
+            rc = PHYSIM_ERR_MEMORY;
+        }
+    }
     if (rc != PHYSIM_OK) {
         physim_gpu_sim_destroy(s);
         return rc;
@@ -197,6 +229,23 @@ int physim_gpu_sim_upload(PhysimSim *s, const Entity *state, size_t n)
     return PHYSIM_OK;
 }
 
+namespace {
+
+// The gravity phase of one force evaluation: the captured graph, or the
+// kernels themselves when the stream cannot be captured.
+int sim_gravity(PhysimSim *s, int *splits)
+{
+    if (s->use_graph && !s->graph_exec) PG_TRY(sim_capture(s));
+    if (s->graph_exec) {
+        PG_CUDA(cudaGraphLaunch(s->graph_exec, s->stream));
+        *splits = s->cfg.gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO ? s->plan.splits : 1;
+        return PHYSIM_OK;
+    }
+    return sim_forces(s, splits);
+}
+
+}  // namespace
+
 int physim_gpu_sim_step(PhysimSim *s, uint32_t steps)
 {
     PG_CHECK(s, PHYSIM_ERR_ARGUMENT, "null simulation");
@@ -206,15 +255,23 @@ int physim_gpu_sim_step(PhysimSim *s, uint32_t steps)
         if (s->n == 0) break;
         int splits = 1;
         if (s->profiling) PG_CUDA(cudaEventRecord(s->ev[0], s->stream));
-        if (s->use_graph && !s->graph_exec) PG_TRY(sim_capture(s));
-        if (s->graph_exec) {
-            PG_CUDA(cudaGraphLaunch(s->graph_exec, s->stream));
-            splits = s->cfg.gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO ? s->plan.splits : 1;
+        if (s->cfg.integrator == PHYSIM_INTEGRATOR_RK4) {
+            // four force evaluations at the stage states (rk4.rs:33,57,82,108)
+            for (int stage = 1; stage <= 4; ++stage) {
+                PG_TRY(sim_gravity(s, &splits));
+                if (stage == 4 && s->profiling) PG_CUDA(cudaEventRecord(s->ev[1], s->stream));
+                PG_TRY(launch_rk4_stage(s->b, s->partial, splits, s->cfg.dt, stage, s->rk4_save,
+                                        s->rk4_ksum, s->stream));
+            }
         } else {
-            PG_TRY(sim_forces(s, &splits));
+            PG_TRY(sim_gravity(s, &splits));
+            if (s->profiling) PG_CUDA(cudaEventRecord(s->ev[1], s->stream));
+            if (s->cfg.integrator == PHYSIM_INTEGRATOR_EULER)
+                PG_TRY(launch_euler(s->b, s->partial, splits, s->cfg.dt, s->stream));
+            else
+                PG_TRY(launch_verlet(s->b, s->partial, splits, s->cfg.dt, !s->history,
+                                     s->stream));
         }
-        if (s->profiling) PG_CUDA(cudaEventRecord(s->ev[1], s->stream));
-        PG_TRY(launch_verlet(s->b, s->partial, splits, s->cfg.dt, !s->history, s->stream));
         if (s->profiling) PG_CUDA(cudaEventRecord(s->ev[2], s->stream));
         s->history = true;
     }
@@ -266,7 +323,7 @@ int physim_gpu_sim_download(PhysimSim *s, Entity *state, size_t n)
                                 s->stream));
     }
     PG_CUDA(cudaStreamSynchronize(s->stream));
-    return PHYSIM_OK;
+    return bh_check(s->bh, s->stream);
 }
 
 int physim_gpu_sim_accelerations(PhysimSim *s, Acceleration *acc, size_t n)
@@ -284,6 +341,7 @@ int physim_gpu_sim_accelerations(PhysimSim *s, Acceleration *acc, size_t n)
     PG_CUDA(cudaMemcpyAsync(h.data(), s->acc_soa, 3 * n * sizeof(double), cudaMemcpyDeviceToHost,
                             s->stream));
     PG_CUDA(cudaStreamSynchronize(s->stream));
+    PG_TRY(bh_check(s->bh, s->stream));
     for (size_t i = 0; i < n; ++i) {
         acc[i].x = h[i];
         acc[i].y = h[n + i];
@@ -349,7 +407,7 @@ int physim_gpu_sim_synchronize(PhysimSim *s)
     PG_CHECK(s, PHYSIM_ERR_ARGUMENT, "null simulation");
     PG_CUDA(cudaSetDevice(s->cfg.device));
     PG_CUDA(cudaStreamSynchronize(s->stream));
-    return PHYSIM_OK;
+    return bh_check(s->bh, s->stream);
 }
 
 void *physim_gpu_sim_stream(PhysimSim *s) { return s ? (void *)s->stream : nullptr; }
@@ -357,8 +415,9 @@ void *physim_gpu_sim_stream(PhysimSim *s) { return s ? (void *)s->stream : nullp
 int physim_gpu_sim_launches_per_step(PhysimSim *s)
 {
     if (!s) return 0;
-    if (s->cfg.gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO) return 2;
-    return bh_launches(s->bh) + 1;
+    const int per_eval = s->cfg.gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO ? 2
+                                                                       : bh_launches(s->bh) + 1;
+    return s->cfg.integrator == PHYSIM_INTEGRATOR_RK4 ? 4 * per_eval : per_eval;
 }
 
 void physim_gpu_sim_destroy(PhysimSim *s)
@@ -370,6 +429,8 @@ void physim_gpu_sim_destroy(PhysimSim *s)
     if (s->partial) cudaFree(s->partial);
     if (s->acc_soa) cudaFree(s->acc_soa);
     if (s->diag) cudaFree(s->diag);
+    if (s->rk4_save) cudaFree(s->rk4_save);
+    if (s->rk4_ksum) cudaFree(s->rk4_ksum);
     bh_free(s->bh);
     if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
     if (s->graph) cudaGraphDestroy(s->graph);
@@ -455,6 +516,136 @@ void physim_gpu_verlet_destroy(PhysimVerlet *v)
     if (v->d_acc) cudaFree(v->d_acc);
     if (v->stream) cudaStreamDestroy(v->stream);
     delete v;
+}
+
+// ------------------------------------------------------------------------
+// verlet / euler / rk4 over host arrays with an acc_fn callback
+// ------------------------------------------------------------------------
+namespace {
+
+void integrator_release(PhysimIntegrator *it)
+{
+    if (it->d_ent) cudaFree(it->d_ent);
+    if (it->d_q) cudaFree(it->d_q);
+    if (it->d_acc) cudaFree(it->d_acc);
+    if (it->d_ksum) cudaFree(it->d_ksum);
+    if (it->h_q) cudaFreeHost(it->h_q);
+    if (it->h_acc) cudaFreeHost(it->h_acc);
+    it->d_ent = it->d_q = nullptr;
+    it->d_acc = nullptr;
+    it->d_ksum = nullptr;
+    it->h_q = nullptr;
+    it->h_acc = nullptr;
+    it->cap = 0;
+}
+
+int integrator_reserve(PhysimIntegrator *it, size_t n)
+{
+    if (n <= it->cap) return PHYSIM_OK;
+    integrator_release(it);
+    PG_CUDA(cudaMalloc((void **)&it->d_ent, n * sizeof(Entity)));
+    PG_CUDA(cudaMalloc((void **)&it->d_q, n * sizeof(Entity)));
+    PG_CUDA(cudaMalloc((void **)&it->d_acc, n * sizeof(Acceleration)));
+    PG_CUDA(cudaMallocHost((void **)&it->h_acc, n * sizeof(Acceleration)));
+    if (it->kind == PHYSIM_INTEGRATOR_RK4) {
+        PG_CUDA(cudaMalloc((void **)&it->d_ksum, 6 * n * sizeof(double)));
+        PG_CUDA(cudaMallocHost((void **)&it->h_q, n * sizeof(Entity)));
+    }
+    it->cap = n;
+    return PHYSIM_OK;
+}
+
+// acc_fn(state) into zeroed accelerations, copied to d_acc
+int integrator_eval(PhysimIntegrator *it, const Entity *state, size_t n, PhysimAccFn acc_fn,
+                    void *user)
+{
+    memset(it->h_acc, 0, n * sizeof(Acceleration));
+    acc_fn(user, state, n, it->h_acc);
+    PG_CUDA(cudaMemcpyAsync(it->d_acc, it->h_acc, n * sizeof(Acceleration),
+                            cudaMemcpyHostToDevice, it->stream));
+    return PHYSIM_OK;
+}
+
+}  // namespace
+
+int physim_gpu_integrator_create(uint32_t kind, int32_t device, PhysimIntegrator **out)
+{
+    PG_CHECK(out, PHYSIM_ERR_ARGUMENT, "null argument");
+    *out = nullptr;
+    PG_CHECK(kind <= PHYSIM_INTEGRATOR_RK4, PHYSIM_ERR_ARGUMENT, "unknown integrator %u", kind);
+    PhysimIntegrator *it = new (std::nothrow) PhysimIntegrator();
+    PG_CHECK(it, PHYSIM_ERR_MEMORY, "out of host memory");
+    it->kind = kind;
+    it->device = device;
+    if (kind == PHYSIM_INTEGRATOR_VERLET) {
+        int rc = physim_gpu_verlet_create(device, &it->verlet);
+        if (rc != PHYSIM_OK) {
+            delete it;
+            return rc;
+        }
+    }
+    *out = it;
+    return PHYSIM_OK;
+}
+
+int physim_gpu_integrator_integrate(PhysimIntegrator *it, const Entity *entities,
+                                    Entity *new_state, size_t n, PhysimAccFn acc_fn, void *user,
+                                    double dt)
+{
+    PG_CHECK(it && acc_fn, PHYSIM_ERR_ARGUMENT, "null argument");
+    PG_CHECK(n == 0 || (entities && new_state), PHYSIM_ERR_ARGUMENT, "null argument");
+    PG_CUDA(cudaSetDevice(it->device));
+    if (it->kind == PHYSIM_INTEGRATOR_VERLET) {
+        // verlet.rs:92-106: one acc_fn call, then the (Taylor or regular) step
+        std::vector<Acceleration> acc(n ? n : 1);
+        memset(acc.data(), 0, acc.size() * sizeof(Acceleration));
+        acc_fn(user, entities, n, acc.data());
+        return physim_gpu_verlet_integrate(it->verlet, entities, new_state, n, acc.data(), dt);
+    }
+    if (!it->stream) PG_CUDA(cudaStreamCreateWithFlags(&it->stream, cudaStreamNonBlocking));
+    if (n == 0) {
+        acc_fn(user, entities, 0, nullptr);
+        return PHYSIM_OK;
+    }
+    PG_TRY(integrator_reserve(it, n));
+    PG_CUDA(cudaMemcpyAsync(it->d_ent, entities, n * sizeof(Entity), cudaMemcpyHostToDevice,
+                            it->stream));
+    if (it->kind == PHYSIM_INTEGRATOR_EULER) {
+        // euler.rs:25-47
+        PG_TRY(integrator_eval(it, entities, n, acc_fn, user));
+        PG_TRY(launch_euler_aos(it->d_ent, it->d_q, it->d_acc, n, dt, it->stream));
+    } else {
+        // rk4.rs:33-178: the stage states are formed on the device and handed
+        // to acc_fn on the host
+        const Entity *q_host = entities;
+        for (int stage = 1; stage <= 4; ++stage) {
+            PG_TRY(integrator_eval(it, q_host, n, acc_fn, user));
+            const Entity *d_q_in = stage == 1 ? it->d_ent : it->d_q;
+            PG_TRY(launch_rk4_aos_stage(it->d_ent, d_q_in, it->d_acc, it->d_ksum, it->d_q, n, dt,
+                                        stage, it->stream));
+            if (stage < 4) {
+                PG_CUDA(cudaMemcpyAsync(it->h_q, it->d_q, n * sizeof(Entity),
+                                        cudaMemcpyDeviceToHost, it->stream));
+                PG_CUDA(cudaStreamSynchronize(it->stream));
+                q_host = it->h_q;
+            }
+        }
+    }
+    PG_CUDA(cudaMemcpyAsync(new_state, it->d_q, n * sizeof(Entity), cudaMemcpyDeviceToHost,
+                            it->stream));
+    PG_CUDA(cudaStreamSynchronize(it->stream));
+    return PHYSIM_OK;
+}
+
+void physim_gpu_integrator_destroy(PhysimIntegrator *it)
+{
+    if (!it) return;
+    cudaSetDevice(it->device);
+    if (it->stream) cudaStreamSynchronize(it->stream);
+    integrator_release(it);
+    if (it->verlet) physim_gpu_verlet_destroy(it->verlet);
+    if (it->stream) cudaStreamDestroy(it->stream);
+    delete it;
 }
 
 }  // extern "C"

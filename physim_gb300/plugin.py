@@ -132,20 +132,79 @@ class GpuVerlet:
             pass
 
 
-class Pipeline:
-    """pipeline.rs:137-173 restated: per step, zeroed accelerations, every
-    transform in order (`transform_fn`), then the integrator."""
+class GpuIntegrator:
+    """The verlet, euler or rk4 integrator element over host arrays, in the
+    shape of physim's IntegratorElement::integrate(entities, new_state,
+    acc_fn, dt) (physim-core/src/plugin/integrator.rs:5-13): `acc_fn(state,
+    acc)` adds into zeroed accelerations and is called once (verlet, euler)
+    or four times (rk4); the updates run on the GPU."""
 
-    def __init__(self, transforms: Iterable[TransformElementHandler], integrator: GpuVerlet,
-                 dt: float):
+    KINDS = {"verlet": _lib.INTEGRATOR_VERLET, "euler": _lib.INTEGRATOR_EULER,
+             "rk4": _lib.INTEGRATOR_RK4}
+
+    def __init__(self, kind: str = "verlet", device: int = 0):
+        h = C.c_void_p()
+        check(lib.physim_gpu_integrator_create(self.KINDS[kind], device, C.byref(h)),
+              "physim_gpu_integrator_create")
+        self.kind = kind
+        self.handle = h
+
+    def integrate(self, entities: np.ndarray, acc_fn, dt: float) -> np.ndarray:
+        entities = as_entities(entities)
+        new_state = np.empty_like(entities)
+        error: list[BaseException] = []
+
+        def cb(_user, sp, n, ap):
+            try:
+                st = np.ctypeslib.as_array(C.cast(sp, C.POINTER(C.c_uint8)),
+                                           (n * ENTITY.itemsize,)).view(ENTITY)
+                ac = np.ctypeslib.as_array(C.cast(ap, C.POINTER(C.c_uint8)),
+                                           (n * ACCELERATION.itemsize,)).view(ACCELERATION)
+                acc_fn(st, ac)
+            except BaseException as exc:  # surfaced after the C call returns
+                error.append(exc)
+
+        fn = _lib.AccFn(cb) if len(entities) else _lib.AccFn(lambda *a: None)
+        rc = lib.physim_gpu_integrator_integrate(self.handle, entities.ctypes.data,
+                                                 new_state.ctypes.data, len(entities), fn, None,
+                                                 dt)
+        if error:
+            raise error[0]
+        check(rc, "physim_gpu_integrator_integrate")
+        return new_state
+
+    def close(self) -> None:
+        if self.handle:
+            lib.physim_gpu_integrator_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Pipeline:
+    """pipeline.rs:137-173 restated: per step the integrator is handed
+    `transform_fn` (every transform in order adding into the accelerations
+    it is given) and produces the new state."""
+
+    def __init__(self, transforms: Iterable[TransformElementHandler],
+                 integrator: GpuVerlet | GpuIntegrator, dt: float):
         self.transforms = list(transforms)
         self.integrator = integrator
         self.dt = dt
 
-    def step(self, state: np.ndarray) -> np.ndarray:
-        acc = np.zeros(len(state), dtype=ACCELERATION)
+    def transform_fn(self, state: np.ndarray, acc: np.ndarray) -> None:
         for t in self.transforms:
             t.transform(state, acc)
+
+    def step(self, state: np.ndarray) -> np.ndarray:
+        if isinstance(self.integrator, GpuIntegrator):
+            return self.integrator.integrate(state, self.transform_fn, self.dt)
+        acc = np.zeros(len(state), dtype=ACCELERATION)
+        self.transform_fn(state, acc)
         return self.integrator.integrate(state, acc, self.dt)
 
     def run(self, state: np.ndarray, iterations: int) -> np.ndarray:

@@ -148,6 +148,24 @@ class GpuExecutor(Executor):
         return units
 
 
+class PlainExecutor(Executor):
+    """The baseline the served mix is compared with: every job, direct sum or
+    Barnes-Hut, as a plain device-resident simulation, in ticks of about
+    `tick_ms` (long enough that the host's polling leaves the GPU idle for
+    about 1% of the time; short enough that a job cut off by the end of a
+    run gets credit for the steps it took).  Run it under a Server with
+    max_units=1 and max_batch=1 to execute the jobs one at a time in arrival
+    order."""
+
+    def __init__(self, device: int = 0, download: bool = True, tick_ms: float = 100.0):
+        self.device = device
+        self.download = download
+        self.tick_ms = tick_ms
+
+    def make_units(self, jobs: list[JobSpec]) -> list[Unit]:
+        return [_SimUnit(j, self) for j in jobs]
+
+
 class _CudaTick:
     def __init__(self, stream_ptr: int, device: int):
         import torch
@@ -220,7 +238,8 @@ class _SimUnit(Unit):
                                         leaf_size=job.leaf_size, traversal="warp",
                                         device=ex.device))
         self.tick = _CudaTick(self.sim.stream, ex.device)
-        est_ms = max(job.n * 1.6e-6, 0.05)
+        est_ms = max(job.n * 1.6e-6, 0.05) if job.gravity != "simple_astro" else \
+            max(job.n * job.n / 2.0e12 * 1e3, 0.02)
         self.k_full = int(max(1, ex.tick_ms / est_ms))
         self.left = job.steps
         self.reported = False
@@ -266,7 +285,7 @@ class Server:
         self.clock = clock
         self.max_units = max_units
         self.pending: collections.deque[JobSpec] = collections.deque()
-        self.arrivals: list[JobSpec] = []  # heap by arrival time (not yet arrived)
+        self.arrivals: list[tuple[float, int, JobSpec]] = []  # heap: not yet arrived
         self.units: list[Unit] = []
         self.in_use = 0
         self.results: list[JobResult] = []
@@ -283,11 +302,12 @@ class Server:
     def submit(self, jobs: Iterable[JobSpec]) -> None:
         with self._lock:
             for j in jobs:
-                heapq.heappush(self.arrivals, j)
+                # (arrival, id): jobs arriving at the same time keep their order
+                heapq.heappush(self.arrivals, (j.arrival, j.id, j))
 
     def _admit(self, now: float) -> None:
-        while self.arrivals and self.arrivals[0].arrival <= now:
-            j = heapq.heappop(self.arrivals)
+        while self.arrivals and self.arrivals[0][0] <= now:
+            j = heapq.heappop(self.arrivals)[2]
             if j.device_bytes() > self.budget:
                 self.rejected.append(j)  # can never fit
             else:

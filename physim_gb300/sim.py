@@ -6,12 +6,14 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import (GRAVITY_ASTRO, GRAVITY_ASTRO2, GRAVITY_SIMPLE_ASTRO, TRAVERSAL_EXACT,
-                   TRAVERSAL_WARP, PhysimSimConfig, check, lib)
+from ._lib import (GRAVITY_ASTRO, GRAVITY_ASTRO2, GRAVITY_SIMPLE_ASTRO, INTEGRATOR_EULER,
+                   INTEGRATOR_RK4, INTEGRATOR_VERLET, TRAVERSAL_EXACT, TRAVERSAL_WARP,
+                   PhysimSimConfig, check, lib)
 from .entity import ACCELERATION, ENTITY, as_entities
 
 GRAVITY = {"simple_astro": GRAVITY_SIMPLE_ASTRO, "astro2": GRAVITY_ASTRO2, "astro": GRAVITY_ASTRO}
 TRAVERSAL = {"exact": TRAVERSAL_EXACT, "warp": TRAVERSAL_WARP}
+INTEGRATOR = {"verlet": INTEGRATOR_VERLET, "euler": INTEGRATOR_EULER, "rk4": INTEGRATOR_RK4}
 
 
 @dataclass
@@ -25,6 +27,10 @@ class SimConfig:
     compensated: bool = True
     device: int = 0
     stream: int | None = None  # a cudaStream_t (e.g. torch.cuda.Stream().cuda_stream)
+    integrator: str = "verlet"  # verlet, euler or rk4 (integrators/src/)
+    # accuracy options of astro/astro2 beyond the reference (off by default)
+    quadrupole: bool = False  # add the cells' quadrupole moments
+    com_theta: float = 0.0    # > 0: also require b_max < com_theta |x - c| to accept a cell
 
     def to_c(self) -> PhysimSimConfig:
         c = PhysimSimConfig()
@@ -38,6 +44,9 @@ class SimConfig:
         c.compensated = 1 if self.compensated else 0
         c.device = self.device
         c.stream = self.stream or None
+        c.integrator = INTEGRATOR[self.integrator]
+        c.multipole = 1 if self.quadrupole else 0
+        c.com_theta = self.com_theta
         return c
 
 
@@ -88,11 +97,13 @@ class Simulation:
         nn, lvl = np.zeros(cap, np.uint8), np.zeros(cap, np.uint8)
         cen = np.zeros(4 * cap, np.float64)
         com = np.zeros(4 * cap, np.float32)
+        quad = np.zeros(8 * cap, np.float32)
         s = PhysimTreeSnapshot()
         s.cap_nodes = cap
         for name, arr in (("keys", keys), ("order", order), ("node_begin", nb),
                           ("node_count", nc), ("node_child", ch), ("node_nchild", nn),
-                          ("node_level", lvl), ("node_centre", cen), ("node_com", com)):
+                          ("node_level", lvl), ("node_centre", cen), ("node_com", com),
+                          ("node_quad", quad)):
             setattr(s, name, arr.ctypes.data)
         check(lib.physim_gpu_sim_tree_snapshot(self.handle, C.byref(s)),
               "physim_gpu_sim_tree_snapshot")
@@ -100,6 +111,8 @@ class Simulation:
         return {"keys": keys, "order": order, "begin": nb[:m], "count": nc[:m], "child": ch[:m],
                 "nchild": nn[:m], "level": lvl[:m], "centre": cen[:4 * m].reshape(4, m),
                 "com": com[:4 * m].reshape(m, 4), "n_nodes": int(s.n_nodes),
+                "quad": np.concatenate([quad[:4 * m].reshape(m, 4),
+                                        quad[4 * m:8 * m].reshape(m, 4)], axis=1),
                 "extent": s.extent, "flags": int(s.flags)}
 
     def diagnostics(self, potential: bool = False) -> dict:

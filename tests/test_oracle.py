@@ -153,6 +153,101 @@ def test_verlet_known_steps(oracle_mod):
     assert s3["vx"][0] == s2["vx"][0] + 4.0 * 0.5
 
 
+def test_euler_known_step(oracle_mod):
+    """euler.rs:29-37 by hand; fixed bodies drift (euler ignores `fixed`)."""
+    from physim_gb300.entity import accelerations, entities
+    s = entities(2)
+    s["x"], s["vx"], s["mass"] = 1.0, 2.0, 1.0
+    s["fixed"][1] = 1
+    a = accelerations(2)
+    a["x"] = 4.0
+    s1 = oracle_mod.euler_step(s, a, 0.5)
+    assert np.all(s1["x"] == 1.0 + 2.0 * 0.5 + 0.5 * 4.0 * 0.25)
+    assert np.all(s1["vx"] == 2.0 + 4.0 * 0.5)
+    assert s1["fixed"][1] == 1
+
+
+def _rk4_numpy(s, acc_of, dt):
+    """rk4.rs:24-178 restated with numpy arrays (independent of the C oracle)."""
+    x = np.stack([s["x"], s["y"], s["z"]], 1)
+    v = np.stack([s["vx"], s["vy"], s["vz"]], 1)
+    ks = []
+    qx, qv = x, v
+    for c in (0.5, 0.5, 1.0, None):
+        a = acc_of(qx)
+        kx, kv = dt * qv, dt * a
+        ks.append((kx, kv))
+        if c is not None:
+            qx, qv = (x + 0.5 * kx, v + 0.5 * kv) if c == 0.5 else (x + kx, v + kv)
+    sx = ks[0][0] + 2.0 * ks[1][0] + 2.0 * ks[2][0] + ks[3][0]
+    sv = ks[0][1] + 2.0 * ks[1][1] + 2.0 * ks[2][1] + ks[3][1]
+    nx, nv = x + sx / 6.0, v + sv / 6.0
+    fixed = s["fixed"].astype(bool)
+    nx[fixed], nv[fixed] = x[fixed], 0.0
+    return nx, nv
+
+
+def test_rk4_matches_numpy_restatement(oracle_mod):
+    """The C rk4 step equals an independent numpy restatement bit for bit
+    (harmonic force a = -k x, evaluated on the stage states), including a
+    fixed body (rk4.rs:165-171: position kept, velocity zeroed)."""
+    from physim_gb300 import ics
+    s = ics.cube_with_stars(64, seed=9)
+    s["fixed"][2] = 1
+    k = 3.7
+
+    def acc_fn(state, acc):
+        acc["x"] += -k * state["x"]
+        acc["y"] += -k * state["y"]
+        acc["z"] += -k * state["z"]
+
+    got = oracle_mod.rk4_step(s, acc_fn, 1e-2)
+    nx, nv = _rk4_numpy(s, lambda q: -k * q, 1e-2)
+    assert np.array_equal(np.stack([got["x"], got["y"], got["z"]], 1), nx)
+    assert np.array_equal(np.stack([got["vx"], got["vy"], got["vz"]], 1), nv)
+    assert got["vx"][2] == 0.0 and got["x"][2] == s["x"][2]
+
+
+def test_rk4_harmonic_accuracy(oracle_mod):
+    """One-body harmonic oscillator: rk4's global error is O(dt^4)."""
+    from physim_gb300.entity import entities
+    s = entities(1)
+    s["x"], s["mass"] = 1.0, 1.0
+
+    def acc_fn(state, acc):
+        acc["x"] += -state["x"]
+
+    errs = []
+    for dt in (0.1, 0.05):
+        q = s.copy()
+        for _ in range(int(round(1.0 / dt))):
+            q = oracle_mod.rk4_step(q, acc_fn, dt)
+        errs.append(abs(q["x"][0] - np.cos(1.0)))
+    assert errs[1] < errs[0] / 12  # 2^4 = 16 in the limit
+
+
+def test_pipeline_integrators(oracle_mod):
+    """The pipeline loop with each integrator equals stepping by hand (field
+    by field: the Entity padding bytes are not state)."""
+    from physim_gb300 import ics
+
+    def same(a, b):
+        return all(a[f].tobytes() == b[f].tobytes() for f in a.dtype.names)
+
+    s = ics.cube_with_stars(100, seed=4, stars=ics.STARS_2)
+    e, dt = 0.01, 1e-5
+    want = s
+    for _ in range(3):
+        want = oracle_mod.rk4_step(want, lambda st, ac: oracle_mod.simple_astro(st, e, ac), dt)
+    got = oracle_mod.run_pipeline(s, "simple_astro", 3, dt, e, integrator="rk4")
+    assert same(got, want)
+    want = s
+    for _ in range(3):
+        want = oracle_mod.euler_step(want, oracle_mod.simple_astro(want, e), dt)
+    got = oracle_mod.run_pipeline(s, "simple_astro", 3, dt, e, integrator="euler")
+    assert same(got, want)
+
+
 def test_barnes_hut_theta_negative_is_direct_sum(oracle_mod):
     """theta < 0 opens every cell, so astro2/astro equal simple_astro up to
     summation order."""

@@ -157,3 +157,17 @@ def test_served_mix_distribution():
     assert all(100 <= j.steps <= 5000 for j in jobs)
     arr = [j.arrival for j in jobs]
     assert arr == sorted(arr) and arr[-1] < 20.0
+
+
+def test_one_at_a_time_baseline():
+    """max_units=1 / max_batch=1 runs the jobs strictly one after another in
+    arrival order (the plain baseline of the served mix)."""
+    ex = FakeExecutor(k=1000)
+    jobs = [job(i, 1000 + i, 50, t=0.0) for i in range(6)]
+    srv = Server(ex, hbm_budget=1 << 40, max_units=1, max_batch=1)
+    ex.server = srv
+    srv.submit(jobs)
+    res = srv.run(poll=0.0)
+    assert [r.spec.id for r in res] == list(range(6))
+    assert ex.batches == [[i] for i in range(6)]
+    assert srv.max_running == 1
