@@ -288,6 +288,7 @@ def measure_direct(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
     sim = pg.Simulation(state, pg.SimConfig(gravity="simple_astro", e=E, dt=DT, device=device,
                                             stream=stream.cuda_stream))
+    plan = sim.autotune()
     sim.set_profiling(True)
     with torch.cuda.stream(stream):
         sim.step(args.warmup)
@@ -319,6 +320,7 @@ def measure_direct(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict
             traffic = None
     out = {"value": all_pairs / (total_ms / 1e3) / 1e9, "ms_per_step": total_ms / args.steps,
            "bodies": n, "pairs_per_step": pairs_step, "wall_s": wall, "gpu_launches": launches,
+           "plan": plan,
            "roofline": {"bound": "fp32", "kernel": "direct_forces_kernel", "achieved": achieved,
                         "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                         "traffic": traffic,
@@ -733,6 +735,7 @@ def run_ours(args, dist: Dist):
     }
     if direct:
         line["config"]["pairs_per_step"] = direct["pairs_per_step"]
+        line["config"]["pair_kernel_plan"] = direct["plan"]
         for k in ("roofline", "e2e", "gpu_launches", "cpu_baseline", "clocks"):
             if k in direct:
                 line[k] = direct[k]

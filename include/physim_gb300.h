@@ -276,6 +276,21 @@ int physim_gpu_sim_accelerations(PhysimSim *sim, Acceleration *acc, size_t n);
 int physim_gpu_sim_synchronize(PhysimSim *sim);
 /* The cudaStream_t the simulation runs on. */
 void *physim_gpu_sim_stream(PhysimSim *sim);
+/* Pair-kernel plan of a simple_astro simulation: threads per block, bodies
+ * per thread, j-range splits, candidates timed, time of one force pass. */
+typedef struct PhysimDirectTuning {
+    uint32_t block;
+    uint32_t ipt;
+    uint32_t splits;
+    uint32_t candidates;
+    double force_ms;
+} PhysimDirectTuning;
+
+/* Times every candidate pair-kernel plan on the simulation's bodies (force
+ * passes only; the state is not advanced) and keeps the fastest.  The
+ * simulation starts with a heuristic plan; this makes the choice by
+ * measurement.  No-op for astro/astro2.  out may be NULL. */
+int physim_gpu_sim_autotune(PhysimSim *sim, PhysimDirectTuning *out);
 /* Number of kernel launches one step enqueues (for launch accounting). */
 int physim_gpu_sim_launches_per_step(PhysimSim *sim);
 /* Records CUDA events around the gravity kernels and the integrator of each

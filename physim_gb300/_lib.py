@@ -85,6 +85,11 @@ class PhysimDiagnostics(C.Structure):
                 ("energy", C.c_double)]
 
 
+class PhysimDirectTuning(C.Structure):
+    _fields_ = [("block", C.c_uint32), ("ipt", C.c_uint32), ("splits", C.c_uint32),
+                ("candidates", C.c_uint32), ("force_ms", C.c_double)]
+
+
 class PhysimEnsembleTuning(C.Structure):
     _fields_ = [("block", C.c_uint32), ("ipt", C.c_uint32), ("chunk_bodies", C.c_uint32),
                 ("candidates", C.c_uint32), ("force_ms", C.c_double)]
@@ -121,6 +126,7 @@ def _load() -> C.CDLL:
         "physim_gpu_sim_destroy": (None, [vp]),
         "physim_gpu_sim_diagnostics": (C.c_int, [vp, C.POINTER(PhysimDiagnostics), C.c_int]),
         "physim_gpu_sim_tree_snapshot": (C.c_int, [vp, C.POINTER(PhysimTreeSnapshot)]),
+        "physim_gpu_sim_autotune": (C.c_int, [vp, C.POINTER(PhysimDirectTuning)]),
         "physim_gpu_sim_bh_stats": (C.c_int, [vp, C.POINTER(C.c_uint64),
                                               C.POINTER(C.c_uint64), C.POINTER(dbl)]),
         "physim_gpu_ensemble_create": (C.c_int, [C.POINTER(PhysimSimConfig), vp, sz,

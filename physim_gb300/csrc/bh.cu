@@ -67,6 +67,8 @@ constexpr int kSortPasses = 8;
 // Look-back spin limit per digit (each spin is one L2 load, ~0.5 us worst
 // case), far above any wait of a running predecessor tile.
 constexpr int kLookbackSpins = 1 << 20;
+// Predecessor tiles a look-back reads per round trip.
+constexpr int kLookbackWindow = 8;
 
 struct LevelInfo {
     int32_t begin[kMaxLevels + 2];
@@ -340,21 +342,32 @@ radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restri
         st[d] = ((ep + 2ull) << 32) | count;
     } else {
         st[(size_t)tile * kRadixBuckets + d] = ((ep + 1ull) << 32) | count;
+        // walk back kLookbackWindow tiles per round trip: the window's words
+        // are loaded together, then summed up to the first inclusive prefix
         int t = tile - 1;
         int spins = 0;
         for (;;) {
-            const unsigned long long w = st[(size_t)t * kRadixBuckets + d];
-            const unsigned long long tag = w >> 32;
-            if (tag == ep + 2ull) {
-                excl += (uint32_t)w;
-                break;
+            unsigned long long w[kLookbackWindow];
+#pragma unroll
+            for (int j = 0; j < kLookbackWindow; ++j)
+                w[j] = t - j >= 0 ? st[(size_t)(t - j) * kRadixBuckets + d] : 0ull;
+            int used = 0;
+            bool done = false;
+#pragma unroll
+            for (int j = 0; j < kLookbackWindow; ++j) {
+                if (done || used != j) continue;
+                const unsigned long long tag = w[j] >> 32;
+                if (tag == ep + 2ull) {
+                    excl += (uint32_t)w[j];
+                    done = true;
+                } else if (tag == ep + 1ull) {
+                    excl += (uint32_t)w[j];
+                    ++used;  // t - j > 0 here: tile 0 publishes its inclusive prefix at once
+                }
             }
-            if (tag == ep + 1ull) {
-                excl += (uint32_t)w;
-                --t;  // t > 0 here: tile 0 publishes its inclusive prefix at once
-                continue;
-            }
-            if (++spins > kLookbackSpins) {
+            if (done) break;
+            t -= used;
+            if (used == 0 && ++spins > kLookbackSpins) {
                 atomicOr(&flags[kFlagSort], 1u);
                 break;
             }
@@ -438,10 +451,18 @@ __global__ void root_kernel(NodeArrays nd, LevelInfo *lv, int n,
 }
 
 // The top levels hold few, large nodes whose child ranges would take long
-// binary searches.  For levels <= kTop, child ranges come from a table of
-// cell starts at level kTop instead: top[p] = first sorted index whose
-// level-kTop prefix is >= p (so empty cells point at the next cell), top[cells] = n.
-__host__ __device__ inline int top_levels(int nchild) { return nchild == 8 ? 5 : 7; }
+// binary searches.  For levels < K, child ranges come from a table of cell
+// starts at level K instead: top[p] = first sorted index whose level-K
+// prefix is >= p (so empty cells point at the next cell), top[cells] = n.
+// K grows with the body count (more top levels are then large): the table
+// has nchild^K cells, K = ceil(log_nchild n) within [5, 7] for the octree
+// (at most 2M cells) and [7, 10] for the quadtree (at most 1M cells).
+inline int top_levels(int nchild, long long n)
+{
+    int k = 0;
+    for (long long c = 1; c < n; c *= nchild) ++k;
+    return nchild == 8 ? std::min(std::max(k, 5), 7) : std::min(std::max(k, 7), 10);
+}
 
 __global__ void top_mark_kernel(const uint64_t *__restrict__ keys, int n, int shift,
                                 int32_t *__restrict__ top)
@@ -506,9 +527,8 @@ __global__ void __launch_bounds__(1024) top_fill_kernel(int32_t *__restrict__ to
 __device__ __forceinline__ void child_bounds(const uint64_t *__restrict__ keys, int b, int e,
                                              int shift, int nchild, int *bounds,
                                              const int32_t *__restrict__ top, int level, int D,
-                                             int bits)
+                                             int bits, int K)
 {
-    const int K = top_levels(nchild);
     if (level < K) {
         const uint64_t prefix = keys[b] >> (bits * (D - level));
         for (int c = 0; c < nchild; ++c)
@@ -539,18 +559,6 @@ __device__ __forceinline__ bool node_splits(const uint64_t *__restrict__ keys, i
     return level < D && cnt > leaf && keys[b] != keys[b + cnt - 1];
 }
 
-__device__ int node_child_count(const uint64_t *__restrict__ keys, const NodeArrays &nd, int node,
-                                int leaf, int level, int D, int bits, int nchild,
-                                const int32_t *__restrict__ top)
-{
-    const int b = nd.begin[node], cnt = nd.count[node];
-    if (!node_splits(keys, b, cnt, leaf, level, D)) return 0;
-    int bounds[9];
-    child_bounds(keys, b, b + cnt, bits * (D - level - 1), nchild, bounds, top, level, D, bits);
-    int k = 0;
-    for (int c = 0; c < nchild; ++c) k += bounds[c + 1] > bounds[c];
-    return k;
-}
 
 // One level of the build in one launch: the level's nodes are cut into tiles
 // of kBuildThreads, claimed in launch order from an atomic counter; each
@@ -567,8 +575,8 @@ __device__ int node_child_count(const uint64_t *__restrict__ keys, const NodeArr
 // builds read as not ready.
 __global__ void __launch_bounds__(kBuildThreads)
 level_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, LevelInfo *lv, int level, int leaf,
-             int nchild, const int32_t *__restrict__ top, unsigned long long *__restrict__ status,
-             uint32_t *__restrict__ flags)
+             int nchild, const int32_t *__restrict__ top, int K,
+             unsigned long long *__restrict__ status, uint32_t *__restrict__ flags)
 {
     const int D = tree_levels(nchild), bits = level_bits(nchild);
     const int cnt = lv->count[level];
@@ -598,39 +606,46 @@ level_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, LevelInfo *lv, in
             split = node_splits(keys, b, c, leaf, level, D);
             if (split) {
                 child_bounds(keys, b, b + c, bits * (D - level - 1), nchild, bounds, top, level, D,
-                             bits);
+                             bits, K);
                 for (int q = 0; q < nchild; ++q) nc += bounds[q + 1] > bounds[q];
             }
         }
         uint32_t T;
         const uint32_t local = block_exclusive_scan(nc, ws, T);
-        if (threadIdx.x == 0) {
+        if (threadIdx.x < 32) {
+            // warp-wide look-back: lane l reads the word of tile t - l, so
+            // 32 predecessors cost one round trip
+            const int lane = threadIdx.x;
             uint32_t excl = 0;
             if (tile == 0) {
-                st[0] = ((tag + 2ull) << 32) | T;
+                if (lane == 0) st[0] = ((tag + 2ull) << 32) | T;
             } else {
-                st[tile] = ((tag + 1ull) << 32) | T;
+                if (lane == 0) st[tile] = ((tag + 1ull) << 32) | T;
                 int t = tile - 1, spins = 0;
                 for (;;) {
-                    const unsigned long long w = st[t];
+                    const unsigned long long w = t - lane >= 0 ? st[t - lane] : 0ull;
                     const unsigned long long wt = w >> 32;
-                    if (wt == tag + 2ull) {
-                        excl += (uint32_t)w;
-                        break;
-                    }
-                    if (wt == tag + 1ull) {
-                        excl += (uint32_t)w;
-                        --t;
+                    const uint32_t incl = __ballot_sync(0xffffffffu, wt == tag + 2ull);
+                    const uint32_t ready = __ballot_sync(0xffffffffu, wt == tag + 1ull) | incl;
+                    // lanes up to and including the first inclusive word, if all ready
+                    const int stop = incl ? __ffs(incl) - 1 : 31;
+                    const uint32_t need = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
+                    if ((ready & need) == need) {
+                        uint32_t v = lane <= stop ? (uint32_t)w : 0u;
+                        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                        excl += v;
+                        if (incl) break;
+                        t -= 32;  // t - 31 > 0 here: tile 0's word is inclusive
                         continue;
                     }
                     if (++spins > kLookbackSpins) {
-                        atomicOr(&flags[kFlagSort], 1u);
+                        if (lane == 0) atomicOr(&flags[kFlagSort], 1u);
                         break;
                     }
                 }
-                st[tile] = ((tag + 2ull) << 32) | (excl + T);
+                if (lane == 0) st[tile] = ((tag + 2ull) << 32) | (excl + T);
             }
-            s_excl = (int32_t)excl;
+            if (lane == 0) s_excl = (int32_t)excl;
         }
         __syncthreads();
         const int32_t P = s_excl;
@@ -939,6 +954,25 @@ __device__ __forceinline__ bool com_guard(const TravArgs &a, float4 geo, float4 
     return bmax * bmax < a.com_theta * a.com_theta * r2;
 }
 
+// Two interactions of one body (nq = -position, both lanes) with sources
+// (x, y, z, m) given as float2 planes, through packed FP32 instructions; the
+// arithmetic of each lane is that of pair_acc.
+__device__ __forceinline__ void pair_acc2(float2 nqx, float2 nqy, float2 nqz, float2 x, float2 y,
+                                          float2 z, float2 m, float2 e2, float2 &ax, float2 &ay,
+                                          float2 &az)
+{
+    const float2 dx = add2(x, nqx), dy = add2(y, nqy), dz = add2(z, nqz);
+    float2 r2 = mul2(dz, dz);
+    r2 = fma2(dy, dy, r2);
+    r2 = fma2(dx, dx, r2);
+    const float2 w = add2(r2, e2);
+    const float2 q = fma2(r2, mul2(w, w), make_float2(kPairGuard, kPairGuard));
+    const float2 s = mul2(m, make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y)));
+    ax = fma2(dx, s, ax);
+    ay = fma2(dy, s, ay);
+    az = fma2(dz, s, az);
+}
+
 __device__ __forceinline__ void fold(float &hi, float &lo, float &t)
 {
     float s, err;
@@ -1115,13 +1149,32 @@ traverse_warp_kernel(TravArgs a_in)
     // back, so each is evaluated by its own loop: plain pairs for bodies,
     // pair + quadrupole (kQuad) for cells.
     int nc = 0;  // queued cells
+    const float2 nqx = make_float2(-q.x, -q.x), nqy = make_float2(-q.y, -q.y);
+    const float2 nqz = make_float2(-q.z, -q.z), e2 = make_float2(a.e, a.e);
     auto flush = [&]() {
+        // bodies: staged as planes of (x, y, z, m) so that entries 2k and
+        // 2k + 1 load as one float2 per component and two interactions go
+        // through packed FADD2/FMUL2/FFMA2 (an odd count is padded with a
+        // massless entry, which adds exactly zero)
         for (int j0 = 0; j0 < nq; j0 += 32) {
             const int m = min(32, nq - j0);
             __syncwarp();
-            if (lane < m) tile[warp][lane] = a.sbody[queue[warp][j0 + lane]];
+            float4 bj = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (lane < m) bj = a.sbody[queue[warp][j0 + lane]];
+            float *pl = reinterpret_cast<float *>(&tile[warp][0]);
+            pl[lane] = bj.x;
+            pl[32 + lane] = bj.y;
+            pl[64 + lane] = bj.z;
+            pl[96 + lane] = bj.w;
             __syncwarp();
-            for (int j = 0; j < m; ++j) pair_acc(q.x, q.y, q.z, tile[warp][j], a.e, ax, ay, az);
+            const float2 *px2 = reinterpret_cast<const float2 *>(pl);
+            float2 sx = make_float2(0.f, 0.f), sy = sx, sz = sx;
+            for (int jj = 0; jj < (m + 1) >> 1; ++jj)
+                pair_acc2(nqx, nqy, nqz, px2[jj], px2[16 + jj], px2[32 + jj], px2[48 + jj], e2,
+                          sx, sy, sz);
+            ax += sx.x + sx.y;
+            ay += sy.x + sy.y;
+            az += sz.x + sz.y;
         }
         for (int j0 = 0; j0 < nc; j0 += 32) {
             const int m = min(32, nc - j0);
@@ -1295,7 +1348,7 @@ struct BhWorkspace {
     unsigned long long *level_status = nullptr;  // look-back words of the level build
     unsigned long long *extent_bits = nullptr;
     unsigned long long *stats = nullptr;  // node visits, pair interactions of the last traversal
-    int32_t *top = nullptr;               // cell starts of the top tree level (see top_levels)
+    int32_t *top = nullptr;               // cell starts of tree level K (see top_levels)
     int32_t *top_blockmin = nullptr;      // per-1024-cell minima while filling `top`
     uint32_t *flags = nullptr;
     int launches = 0;
@@ -1377,8 +1430,9 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf)
     PG_WA(w->nd.quad_b, ncap);
     PG_WA(w->nd.arrivals, ncap);
     PG_WA(w->stats, 4);
-    PG_WA(w->top, (size_t)(1 << 15) + 1);
-    PG_WA(w->top_blockmin, 32);
+    // top tables of both tree kinds fit 2^21 + 1 entries
+    PG_WA(w->top, ((size_t)1 << 21) + 1);
+    PG_WA(w->top_blockmin, ((size_t)1 << 21) / 1024);
     PG_WA(w->lv, 1);
     PG_WA(w->level_status, ncap / kBuildThreads + 2);
     PG_WA(w->extent_bits, 1);
@@ -1497,7 +1551,7 @@ static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, c
     root_kernel<<<1, 32, 0, st>>>(ws->nd, ws->lv, n, ws->extent_bits);
     launches += 2;
     const int D = tree_levels(p.nchild);
-    const int K = top_levels(p.nchild);
+    const int K = top_levels(p.nchild, n);
     const int top_cells = 1 << (level_bits(p.nchild) * K);
     PG_CUDA(cudaMemsetAsync(ws->top, 0xff, top_cells * sizeof(int32_t), st));
     top_mark_kernel<<<cdiv(n, 256), 256, 0, st>>>(ws->keys[cur], n, level_bits(p.nchild) * (D - K),
@@ -1507,7 +1561,7 @@ static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, c
     launches += 3;
     for (int level = 0; level < D; ++level) {
         level_kernel<<<ws->grid_build, kBuildThreads, 0, st>>>(
-            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->top,
+            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->top, K,
             ws->level_status, ws->flags);
         launches += 1;
     }

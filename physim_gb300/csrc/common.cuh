@@ -68,36 +68,6 @@ __device__ __forceinline__ float rsqrt_approx(float x)
     return y;
 }
 
-// a / b correctly rounded (round to nearest even), given r = RN(1/b).
-// GB300 issues f64 instructions at a small fraction of its f32 rate, so the
-// integrators avoid a full division sequence per body: the quotient is
-// q0 = RN(a r), corrected once with the FMA residual (Markstein, IBM J. Res.
-// Dev. 34(1), 1990): q1 = RN(q0 + RN(a - q0 b) r), which is within an ulp of
-// a / b.  The residual of q1, rem = a - q1 b, is then exact (one FMA), and
-// q1 is accepted only if |rem| < ulp(q1) b / 2, i.e. |a/b - q1| < ulp(q1) / 2,
-// which makes q1 the correctly rounded quotient.  Anything else -- a zero,
-// subnormal, infinite or NaN operand or quotient, q1 a power of two (whose
-// lower neighbour is closer), or a quotient within rounding of a tie -- takes
-// the ordinary correctly rounded division, so the result always equals
-// __ddiv_rn(a, b).
-__device__ __forceinline__ double div_rn_by(double a, double b, double r)
-{
-    const double q0 = __dmul_rn(a, r);
-    const double q1 = __fma_rn(__fma_rn(-q0, b, a), r, q0);
-    const unsigned long long qb = (unsigned long long)__double_as_longlong(q1);
-    const int ex = (int)((qb >> 52) & 0x7ff);
-    const unsigned long long frac = qb & 0xfffffffffffffull;
-    if (ex > 54 && ex < 0x7ff && frac != 0ull) {
-        const double rem = __fma_rn(-q1, b, a);
-        // ulp(q1) / 2 = 2^(ex - 1023 - 53), a normal double for ex > 54
-        const double half_ulp = __longlong_as_double((long long)(ex - 53) << 52);
-        const double lim = __dmul_rn(half_ulp, fabs(b));
-        // lim must be a normal double so that it is exact
-        if (fabs(rem) < lim && lim >= 2.2250738585072014e-308 && lim < 1.0e300) return q1;
-    }
-    return __ddiv_rn(a, b);
-}
-
 // Knuth's TwoSum: s + err == a + b exactly.
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &err)
 {

@@ -44,7 +44,7 @@ direct_forces_kernel(const float4 *__restrict__ body, int n, int n_jtiles, int c
 struct Shape {
     int block, ipt;
 };
-constexpr Shape kShapes[] = {{256, 4}, {128, 4}, {128, 2}, {256, 2}};
+constexpr Shape kShapes[] = {{256, 4}, {128, 4}, {128, 2}, {256, 2}, {128, 8}};
 
 template <int BLOCK, int IPT>
 void *kernel_ptr(bool comp)
@@ -59,6 +59,7 @@ void *shape_kernel(int block, int ipt, bool comp)
     if (block == 128 && ipt == 4) return kernel_ptr<128, 4>(comp);
     if (block == 128 && ipt == 2) return kernel_ptr<128, 2>(comp);
     if (block == 256 && ipt == 2) return kernel_ptr<256, 2>(comp);
+    if (block == 128 && ipt == 8) return kernel_ptr<128, 8>(comp);
     return nullptr;
 }
 

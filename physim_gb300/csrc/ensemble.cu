@@ -36,7 +36,6 @@ struct MemberInfo {
     int32_t splits;
     float e;
     double dt;
-    double rdt;  // RN(1/dt), for the velocity division (div_rn_by)
 };
 
 struct WorkUnit {
@@ -109,7 +108,7 @@ __global__ void ensemble_verlet_kernel(float4 *body4, const double *__restrict__
             vn = __dadd_rn(v[c], __dmul_rn(a[c], dt));
         } else {
             xn = __dadd_rn(__dsub_rn(__dmul_rn(2.0, q[c]), pr[c]), __dmul_rn(a[c], dt2));
-            vn = div_rn_by(__dsub_rn(xn, q[c]), dt, m.rdt);
+            vn = __ddiv_rn(__dsub_rn(xn, q[c]), dt);
         }
         pr[c] = q[c];
         q[c] = xn;
@@ -175,7 +174,7 @@ __global__ void ensemble_pack_kernel(Entity *out, int n, int off, const uint8_t 
 struct Shape {
     int block, ipt;
 };
-constexpr Shape kShapes[] = {{128, 2}, {128, 4}, {256, 4}, {256, 2}};
+constexpr Shape kShapes[] = {{128, 2}, {128, 4}, {256, 4}, {256, 2}, {128, 8}};
 constexpr int kChunks[] = {4096, 8192, 16384, 65536};
 constexpr int kMinChunk = 4096;  // smallest j chunk any plan uses (sizes the partial sums)
 
@@ -192,6 +191,7 @@ void *ens_kernel(int block, int ipt, bool comp)
     if (block == 128 && ipt == 4) return ens_kernel_ptr<128, 4>(comp);
     if (block == 256 && ipt == 4) return ens_kernel_ptr<256, 4>(comp);
     if (block == 256 && ipt == 2) return ens_kernel_ptr<256, 2>(comp);
+    if (block == 128 && ipt == 8) return ens_kernel_ptr<128, 8>(comp);
     return nullptr;
 }
 
@@ -375,7 +375,6 @@ int physim_gpu_ensemble_create(const PhysimSimConfig *cfg, const size_t *sizes, 
         mi.n = (int32_t)sizes[k];
         mi.e = (float)E->cfg.e;
         mi.dt = E->cfg.dt;
-        mi.rdt = 1.0 / E->cfg.dt;
         E->members[k] = mi;
         slots += (long long)pad_bodies(sizes[k]);
         partial_elems += 3LL * (long long)sizes[k] * cdiv((long long)sizes[k], kMinChunk);
@@ -486,7 +485,6 @@ int physim_gpu_ensemble_set_member(PhysimEnsemble *E, size_t index, double e, do
     PG_CUDA(cudaSetDevice(E->device));
     E->members[index].e = (float)fabs(e);
     E->members[index].dt = dt;
-    E->members[index].rdt = 1.0 / dt;
     PG_CUDA(cudaMemcpyAsync(E->d_members + index, &E->members[index], sizeof(MemberInfo),
                             cudaMemcpyHostToDevice, E->stream));
     const unsigned long long r = steps_remaining;

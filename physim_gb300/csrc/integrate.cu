@@ -114,9 +114,8 @@ __global__ void combine_soa_kernel(const double *__restrict__ mass, const uint8_
 }
 
 // verlet.rs:33-39 (initial, Taylor step) and verlet.rs:64-70 (regular).
-// rdt = RN(1/dt) for the division (x' - x) / dt (see div_rn_by).
 __device__ __forceinline__ void verlet_axis(double &x, double &v, double &p, double a, double dt,
-                                            double dt2, bool initial, double rdt)
+                                            double dt2, bool initial)
 {
     double xn, vn;
     if (initial) {
@@ -126,7 +125,7 @@ __device__ __forceinline__ void verlet_axis(double &x, double &v, double &p, dou
     } else {
         // 2*x - prev + a*dt^2 ; (x' - x)/dt
         xn = __dadd_rn(__dsub_rn(__dmul_rn(2.0, x), p), __dmul_rn(a, dt2));
-        vn = div_rn_by(__dsub_rn(xn, x), dt, rdt);
+        vn = __ddiv_rn(__dsub_rn(xn, x), dt);
     }
     p = x;
     x = xn;
@@ -137,7 +136,7 @@ __global__ void verlet_kernel(float4 *body4, const double *mass, const uint8_t *
                               const double *partial,
                               int splits, int n, double *x, double *y, double *z, double *vx,
                               double *vy, double *vz, double *px, double *py, double *pz,
-                              double dt, double rdt, int initial)
+                              double dt, int initial)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -148,9 +147,9 @@ __global__ void verlet_kernel(float4 *body4, const double *mass, const uint8_t *
     double xi = x[i], yi = y[i], zi = z[i];
     double vxi = vx[i], vyi = vy[i], vzi = vz[i];
     double pxi = px[i], pyi = py[i], pzi = pz[i];
-    verlet_axis(xi, vxi, pxi, ax, dt, dt2, initial, rdt);
-    verlet_axis(yi, vyi, pyi, ay, dt, dt2, initial, rdt);
-    verlet_axis(zi, vzi, pzi, az, dt, dt2, initial, rdt);
+    verlet_axis(xi, vxi, pxi, ax, dt, dt2, initial);
+    verlet_axis(yi, vyi, pyi, ay, dt, dt2, initial);
+    verlet_axis(zi, vzi, pzi, az, dt, dt2, initial);
     x[i] = xi; y[i] = yi; z[i] = zi;
     vx[i] = vxi; vy[i] = vyi; vz[i] = vzi;
     px[i] = pxi; py[i] = pyi; pz[i] = pzi;
@@ -161,8 +160,7 @@ __global__ void verlet_kernel(float4 *body4, const double *mass, const uint8_t *
 }
 
 __global__ void verlet_aos_kernel(const Entity *in, const Entity *prev, Entity *out,
-                                  const Acceleration *acc, int n, double dt, double rdt,
-                                  int initial)
+                                  const Acceleration *acc, int n, double dt, int initial)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -175,9 +173,9 @@ __global__ void verlet_aos_kernel(const Entity *in, const Entity *prev, Entity *
         py = prev[i].y;
         pz = prev[i].z;
     }
-    verlet_axis(en.x, en.vx, px, a.x, dt, dt2, initial, rdt);
-    verlet_axis(en.y, en.vy, py, a.y, dt, dt2, initial, rdt);
-    verlet_axis(en.z, en.vz, pz, a.z, dt, dt2, initial, rdt);
+    verlet_axis(en.x, en.vx, px, a.x, dt, dt2, initial);
+    verlet_axis(en.y, en.vy, py, a.y, dt, dt2, initial);
+    verlet_axis(en.z, en.vz, pz, a.z, dt, dt2, initial);
     out[i] = en;
 }
 
@@ -196,9 +194,9 @@ __global__ void euler_kernel(float4 *body4, const double *mass, const uint8_t *f
     double xi = x[i], yi = y[i], zi = z[i];
     double vxi = vx[i], vyi = vy[i], vzi = vz[i];
     double unused = 0.0;
-    verlet_axis(xi, vxi, unused, ax, dt, dt2, true, 0.0);
-    verlet_axis(yi, vyi, unused, ay, dt, dt2, true, 0.0);
-    verlet_axis(zi, vzi, unused, az, dt, dt2, true, 0.0);
+    verlet_axis(xi, vxi, unused, ax, dt, dt2, true);
+    verlet_axis(yi, vyi, unused, ay, dt, dt2, true);
+    verlet_axis(zi, vzi, unused, az, dt, dt2, true);
     x[i] = xi; y[i] = yi; z[i] = zi;
     vx[i] = vxi; vy[i] = vyi; vz[i] = vzi;
     b.x = (float)xi;
@@ -293,9 +291,9 @@ __global__ void euler_aos_kernel(const Entity *in, Entity *out, const Accelerati
     const Acceleration a = acc[i];
     const double dt2 = __dmul_rn(dt, dt);
     double unused = 0.0;
-    verlet_axis(en.x, en.vx, unused, a.x, dt, dt2, true, 0.0);
-    verlet_axis(en.y, en.vy, unused, a.y, dt, dt2, true, 0.0);
-    verlet_axis(en.z, en.vz, unused, a.z, dt, dt2, true, 0.0);
+    verlet_axis(en.x, en.vx, unused, a.x, dt, dt2, true);
+    verlet_axis(en.y, en.vy, unused, a.y, dt, dt2, true);
+    verlet_axis(en.z, en.vz, unused, a.z, dt, dt2, true);
     out[i] = en;
 }
 
@@ -422,7 +420,7 @@ int launch_verlet(DeviceBodies &b, const double *partial, int splits, double dt,
     if (b.n == 0) return PHYSIM_OK;
     verlet_kernel<<<blocks_for(b.n), kThreads, 0, stream>>>(
         b.body4, b.m, b.fixed, partial, splits, (int)b.n, b.x, b.y, b.z, b.vx, b.vy, b.vz, b.px, b.py,
-        b.pz, dt, 1.0 / dt, initial ? 1 : 0);
+        b.pz, dt, initial ? 1 : 0);
     PG_CUDA(cudaGetLastError());
     return PHYSIM_OK;
 }
@@ -477,7 +475,7 @@ int launch_verlet_aos(const Entity *d_in, const Entity *d_prev, Entity *d_out,
 {
     if (n == 0) return PHYSIM_OK;
     verlet_aos_kernel<<<blocks_for(n), kThreads, 0, stream>>>(d_in, d_prev, d_out, d_acc, (int)n,
-                                                              dt, 1.0 / dt, initial ? 1 : 0);
+                                                              dt, initial ? 1 : 0);
     PG_CUDA(cudaGetLastError());
     return PHYSIM_OK;
 }

@@ -9,6 +9,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "common.cuh"
@@ -274,6 +275,77 @@ int physim_gpu_sim_step(PhysimSim *s, uint32_t steps)
         }
         if (s->profiling) PG_CUDA(cudaEventRecord(s->ev[2], s->stream));
         s->history = true;
+    }
+    return PHYSIM_OK;
+}
+
+int physim_gpu_sim_autotune(PhysimSim *s, PhysimDirectTuning *out)
+{
+    PG_CHECK(s, PHYSIM_ERR_ARGUMENT, "null simulation");
+    PG_CHECK(s->uploaded, PHYSIM_ERR_ARGUMENT, "autotune before upload");
+    PG_CUDA(cudaSetDevice(s->cfg.device));
+    if (s->cfg.gravity != PHYSIM_GRAVITY_SIMPLE_ASTRO || s->n == 0) {
+        if (out) memset(out, 0, sizeof *out);
+        return PHYSIM_OK;
+    }
+    DirectPlan cand[16];
+    const int k = direct_candidates((int)s->n, s->cfg.device, s->cfg.compensated != 0, cand, 16);
+    int max_splits = 1;
+    for (int c = 0; c < k; ++c) max_splits = std::max(max_splits, cand[c].splits);
+    const size_t need = (size_t)max_splits * 3 * s->n;
+    if (need > s->partial_cap) {
+        PG_CUDA(cudaStreamSynchronize(s->stream));
+        if (s->partial) cudaFree(s->partial);
+        s->partial = nullptr;
+        s->partial_cap = 0;
+        PG_CUDA(cudaMalloc((void **)&s->partial, need * sizeof(double)));
+        s->partial_cap = need;
+    }
+    cudaEvent_t a, b;
+    PG_CUDA(cudaEventCreate(&a));
+    PG_CUDA(cudaEventCreate(&b));
+    int best = -1;
+    double best_ms = 1e300;
+    int rc = PHYSIM_OK;
+    for (int c = 0; c < k && rc == PHYSIM_OK; ++c) {
+        // one untimed and two timed force passes (the state is not advanced)
+        float total = 0.f;
+        for (int rep = 0; rep < 3 && rc == PHYSIM_OK; ++rep) {
+            if (cudaEventRecord(a, s->stream) != cudaSuccess) rc = PHYSIM_ERR_CUDA;
+            if (rc == PHYSIM_OK)
+                rc = launch_direct(cand[c], s->b.body4, (float)s->cfg.e, s->partial, s->stream);
+            if (rc == PHYSIM_OK && (cudaEventRecord(b, s->stream) != cudaSuccess ||
+                                    cudaEventSynchronize(b) != cudaSuccess))
+                rc = PHYSIM_ERR_CUDA;
+            float ms = 0.f;
+            if (rc == PHYSIM_OK) cudaEventElapsedTime(&ms, a, b);
+            if (rep > 0) total += ms;
+        }
+        if (rc == PHYSIM_OK && total / 2.0 < best_ms) {
+            best_ms = total / 2.0;
+            best = c;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc != PHYSIM_OK) {
+        if (rc == PHYSIM_ERR_CUDA) set_error("autotune: a CUDA call failed");
+        return rc;
+    }
+    if (best >= 0) {
+        s->plan = cand[best];
+        // the captured gravity phase used the old plan
+        if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+        if (s->graph) cudaGraphDestroy(s->graph);
+        s->graph_exec = nullptr;
+        s->graph = nullptr;
+    }
+    if (out) {
+        out->block = (uint32_t)s->plan.block;
+        out->ipt = (uint32_t)s->plan.ipt;
+        out->splits = (uint32_t)s->plan.splits;
+        out->candidates = (uint32_t)k;
+        out->force_ms = best_ms;
     }
     return PHYSIM_OK;
 }

@@ -134,6 +134,15 @@ class Simulation:
               "physim_gpu_sim_bh_stats")
         return {"node_visits": v.value, "interactions": i.value, "traversal_ms": t.value}
 
+    def autotune(self) -> dict:
+        """Times the candidate pair-kernel plans (simple_astro) and keeps the
+        fastest; returns the chosen plan."""
+        from ._lib import PhysimDirectTuning
+        t = PhysimDirectTuning()
+        check(lib.physim_gpu_sim_autotune(self.handle, C.byref(t)), "physim_gpu_sim_autotune")
+        return {"block": t.block, "ipt": t.ipt, "splits": t.splits, "candidates": t.candidates,
+                "force_ms": t.force_ms}
+
     def set_profiling(self, enable: bool = True) -> None:
         check(lib.physim_gpu_sim_set_profiling(self.handle, 1 if enable else 0),
               "physim_gpu_sim_set_profiling")
