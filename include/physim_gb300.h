@@ -380,6 +380,11 @@ int physim_gpu_ensemble_set_member(PhysimEnsemble *ens, size_t index, double e, 
 /* Times every candidate kernel shape and j-chunk length on the members' data
  * (force passes only; the state is not advanced) and keeps the fastest. */
 int physim_gpu_ensemble_autotune(PhysimEnsemble *ens, PhysimEnsembleTuning *out);
+/* Re-sizes member `index` to n bodies, 0 <= n <= the count it was created
+ * with, reusing its slot (continuous batching: a finished member's slot takes
+ * the next job).  Waits for the stream; the member takes no steps until it is
+ * uploaded (n bodies) and given a step budget by set_member. */
+int physim_gpu_ensemble_resize_member(PhysimEnsemble *ens, size_t index, size_t n);
 /* Enqueues `steps` steps of every member with steps left (asynchronous). */
 int physim_gpu_ensemble_step(PhysimEnsemble *ens, uint32_t steps);
 int physim_gpu_ensemble_download(PhysimEnsemble *ens, size_t index, Entity *state, size_t n);

@@ -135,6 +135,7 @@ def _load() -> C.CDLL:
         "physim_gpu_ensemble_set_member": (C.c_int, [vp, sz, dbl, dbl, C.c_uint64]),
         "physim_gpu_ensemble_autotune": (C.c_int, [vp, C.POINTER(PhysimEnsembleTuning)]),
         "physim_gpu_ensemble_step": (C.c_int, [vp, u32]),
+        "physim_gpu_ensemble_resize_member": (C.c_int, [vp, sz, sz]),
         "physim_gpu_ensemble_download": (C.c_int, [vp, sz, vp, sz]),
         "physim_gpu_ensemble_progress": (C.c_int, [vp, vp, vp]),
         "physim_gpu_ensemble_synchronize": (C.c_int, [vp]),

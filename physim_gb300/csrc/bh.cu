@@ -43,9 +43,12 @@ namespace {
 
 constexpr int kRadixBits = 8;
 constexpr int kRadixBuckets = 1 << kRadixBits;
-constexpr int kSortThreads = 256;
+// 8,192 keys per tile: few tiles keep the look-back chains of a pass short
+// (all tiles of a 1M-key sort are resident at once, so a pass's time is set
+// by how far an inclusive prefix must travel from tile 0)
+constexpr int kSortThreads = 512;
 constexpr int kSortItems = 16;
-constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 keys per block
+constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr int kSortWarps = kSortThreads / 32;
 
 constexpr int kBuildThreads = 256;
@@ -283,7 +286,7 @@ radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restri
                   unsigned long long *__restrict__ status, const uint32_t *__restrict__ epoch_ptr,
                   uint32_t *__restrict__ flags)
 {
-    static_assert(kSortThreads == kRadixBuckets, "one thread per digit");
+    static_assert(kSortThreads >= kRadixBuckets, "one thread per digit");
     __shared__ uint32_t h[kSortWarps][kRadixBuckets];
     __shared__ uint32_t digit_off[kRadixBuckets];
     __shared__ uint32_t ws[33];
@@ -296,7 +299,9 @@ radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restri
     uint32_t digit_base;
     {
         uint32_t total;
-        digit_base = block_exclusive_scan(ghist[pass * kRadixBuckets + threadIdx.x], ws, total);
+        const uint32_t c = threadIdx.x < kRadixBuckets ? ghist[pass * kRadixBuckets + threadIdx.x]
+                                                       : 0u;
+        digit_base = block_exclusive_scan(c, ws, total);
     }
     const int tile = s_tile;
     const int base = tile * kSortTile + warp * (kSortItems * 32);
@@ -326,55 +331,58 @@ radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restri
     }
     __syncthreads();
     // this tile's count of digit d, and the warps' exclusive offsets within it
+    // (threads 0..255, one digit each)
     const int d = threadIdx.x;
-    uint32_t count = 0;
-    for (int w = 0; w < kSortWarps; ++w) {
-        const uint32_t c = h[w][d];
-        h[w][d] = count;
-        count += c;
-    }
-    // tag base of this sort and pass: the passes share the status array
-    const unsigned long long ep =
-        ((unsigned long long)(*epoch_ptr & 0x03ffffffu) * kSortPasses + (unsigned)pass) * 4ull;
-    volatile unsigned long long *st = status;
-    uint32_t excl = 0;
-    if (tile == 0) {
-        st[d] = ((ep + 2ull) << 32) | count;
-    } else {
-        st[(size_t)tile * kRadixBuckets + d] = ((ep + 1ull) << 32) | count;
-        // walk back kLookbackWindow tiles per round trip: the window's words
-        // are loaded together, then summed up to the first inclusive prefix
-        int t = tile - 1;
-        int spins = 0;
-        for (;;) {
-            unsigned long long w[kLookbackWindow];
+    if (d < kRadixBuckets) {
+        uint32_t count = 0;
+        for (int w = 0; w < kSortWarps; ++w) {
+            const uint32_t c = h[w][d];
+            h[w][d] = count;
+            count += c;
+        }
+        // tag base of this sort and pass: the passes share the status array
+        const unsigned long long ep =
+            ((unsigned long long)(*epoch_ptr & 0x03ffffffu) * kSortPasses + (unsigned)pass) * 4ull;
+        volatile unsigned long long *st = status;
+        uint32_t excl = 0;
+        if (tile == 0) {
+            st[d] = ((ep + 2ull) << 32) | count;
+        } else {
+            st[(size_t)tile * kRadixBuckets + d] = ((ep + 1ull) << 32) | count;
+            // walk back kLookbackWindow tiles per round trip: the window's words
+            // are loaded together, then summed up to the first inclusive prefix
+            int t = tile - 1;
+            int spins = 0;
+            for (;;) {
+                unsigned long long w[kLookbackWindow];
 #pragma unroll
-            for (int j = 0; j < kLookbackWindow; ++j)
-                w[j] = t - j >= 0 ? st[(size_t)(t - j) * kRadixBuckets + d] : 0ull;
-            int used = 0;
-            bool done = false;
+                for (int j = 0; j < kLookbackWindow; ++j)
+                    w[j] = t - j >= 0 ? st[(size_t)(t - j) * kRadixBuckets + d] : 0ull;
+                int used = 0;
+                bool done = false;
 #pragma unroll
-            for (int j = 0; j < kLookbackWindow; ++j) {
-                if (done || used != j) continue;
-                const unsigned long long tag = w[j] >> 32;
-                if (tag == ep + 2ull) {
-                    excl += (uint32_t)w[j];
-                    done = true;
-                } else if (tag == ep + 1ull) {
-                    excl += (uint32_t)w[j];
-                    ++used;  // t - j > 0 here: tile 0 publishes its inclusive prefix at once
+                for (int j = 0; j < kLookbackWindow; ++j) {
+                    if (done || used != j) continue;
+                    const unsigned long long tag = w[j] >> 32;
+                    if (tag == ep + 2ull) {
+                        excl += (uint32_t)w[j];
+                        done = true;
+                    } else if (tag == ep + 1ull) {
+                        excl += (uint32_t)w[j];
+                        ++used;  // t - j > 0 here: tile 0 publishes its inclusive prefix at once
+                    }
+                }
+                if (done) break;
+                t -= used;
+                if (used == 0 && ++spins > kLookbackSpins) {
+                    atomicOr(&flags[kFlagSort], 1u);
+                    break;
                 }
             }
-            if (done) break;
-            t -= used;
-            if (used == 0 && ++spins > kLookbackSpins) {
-                atomicOr(&flags[kFlagSort], 1u);
-                break;
-            }
+            st[(size_t)tile * kRadixBuckets + d] = ((ep + 2ull) << 32) | (excl + count);
         }
-        st[(size_t)tile * kRadixBuckets + d] = ((ep + 2ull) << 32) | (excl + count);
+        digit_off[d] = digit_base + excl;
     }
-    digit_off[d] = digit_base + excl;
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < kSortItems; ++r) {
@@ -417,7 +425,8 @@ struct NodeArrays {
     float4 *com;   // x, y, z, mass (f32)
     int4 *meta;    // (id | nchild << 28, first child, first body, body count)
     int32_t *parent;   // parent node, -1 for the root
-    double4 *msum;     // f64 mass and mass-weighted position sums (M, Mx, My, Mz)
+    float4 *msum_hi;   // mass and mass-weighted position sums (M, Mx, My, Mz) as
+    float4 *msum_lo;   //   double-float pairs (hi + lo)
     float4 *quad_a;    // second moments about the centre of mass: Sxx, Syy, Szz, trace
     float4 *quad_b;    // Sxy, Sxz, Syz, 0
     uint32_t *arrivals;  // children finished, for the bottom-up moment pass (kept at 0)
@@ -448,6 +457,8 @@ __global__ void root_kernel(NodeArrays nd, LevelInfo *lv, int n,
     nd.c64[nd.cap] = 0.0;
     nd.c64[2 * (size_t)nd.cap] = 0.0;
     nd.c64[3 * (size_t)nd.cap] = X;
+    nd.geo[0] = make_float4(0.f, 0.f, 0.f, (float)X);
+    nd.meta[0] = make_int4(0, -1, 0, n);
 }
 
 // The top levels hold few, large nodes whose child ranges would take long
@@ -655,6 +666,8 @@ level_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, LevelInfo *lv, in
                 const int fc = child_base + P + (int)local;
                 nd.child[node] = fc;
                 nd.nchild[node] = (uint8_t)nc;
+                nd.meta[node] = make_int4(node | ((int)nc << 28), fc, nd.begin[node],
+                                          nd.count[node]);
                 const size_t cap = nd.cap;
                 const double pcx = nd.c64[node], pcy = nd.c64[cap + node];
                 const double pcz = nd.c64[2 * cap + node], pext = nd.c64[3 * cap + node];
@@ -669,11 +682,18 @@ level_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, LevelInfo *lv, in
                     nd.child[ci] = -1;
                     nd.nchild[ci] = 0;
                     nd.level[ci] = (uint8_t)(level + 1);
-                    nd.c64[ci] = (q & 1) ? __dadd_rn(pcx, h) : __dsub_rn(pcx, h);
-                    nd.c64[cap + ci] = (q & 2) ? __dadd_rn(pcy, h) : __dsub_rn(pcy, h);
-                    nd.c64[2 * cap + ci] =
+                    const double cx = (q & 1) ? __dadd_rn(pcx, h) : __dsub_rn(pcx, h);
+                    const double cy = (q & 2) ? __dadd_rn(pcy, h) : __dsub_rn(pcy, h);
+                    const double cz =
                         nchild == 8 ? ((q & 4) ? __dadd_rn(pcz, h) : __dsub_rn(pcz, h)) : pcz;
+                    nd.c64[ci] = cx;
+                    nd.c64[cap + ci] = cy;
+                    nd.c64[2 * cap + ci] = cz;
                     nd.c64[3 * cap + ci] = h;
+                    // f32 geometry and leaf metadata; the metadata is rewritten
+                    // if the child splits at the next level
+                    nd.geo[ci] = make_float4((float)cx, (float)cy, (float)cz, (float)h);
+                    nd.meta[ci] = make_int4(ci, -1, bounds[q], bounds[q + 1] - bounds[q]);
                 }
             } else {
                 nd.child[node] = -1;
@@ -696,44 +716,62 @@ level_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, LevelInfo *lv, in
 // 5. moments: mass, centre of mass and (optionally) second moments of every
 //    cell, bottom up in one launch
 // ---------------------------------------------------------------------------
-// Each leaf sums its own bodies: mass and mass-weighted positions in f64 (the
-// f32 centre of mass is then within one rounding of the exact one, as the
-// reference's f64 arithmetic needs where a cell's centre of mass lies very
-// close to a body that interacts with it, e.g. a quadtree cell holding a
-// heavy body that a body far above it in z accepts), second moments in f32.
-// A leaf whose bodies all sit at one position keeps that exact position, so a
-// body there cancels against it as the reference's equal-centre skip does.
-// A parent is finished by the thread of its last child to arrive (atomic
-// count of arrivals after a fence; nothing waits), which combines the
-// children in child order -- so results do not depend on the arrival order --
-// and continues upwards:
-//   M = sum M_c,  M c = sum (M c)_c   (f64 sums),
-//   S = sum_c [S_c + M_c (c_c - c)(c_c - c)^T]   (second moments about c).
-// A massless cell sits at its geometric centre.  Every node also gets its f32
-// geometry and packed traversal metadata here.
+// Each leaf sums its own bodies: mass and mass-weighted positions in f64,
+// kept as double-float (hi + lo f32) pairs.  A parent is finished by the
+// thread of its last child to arrive (atomic count of arrivals after a fence;
+// nothing waits), which adds the children's pairs in child order -- so
+// results do not depend on the arrival order -- and continues upwards.  This
+// upward walk is divergent (one thread per finished node), so it uses f32
+// arithmetic only: GB300 issues f64 instructions at a small fraction of its
+// f32 rate, and a divergent f64 instruction costs as much as a full one.
+// The f32 centre of mass c = S / M is the double-float quotient rounded
+// once, within one rounding of the exact value (the reference computes it in
+// f64; its precision matters where a cell's centre of mass lies very close
+// to a body that interacts with it, e.g. a quadtree cell holding a heavy body
+// that a body far above it in z accepts).  A leaf whose bodies all sit at one
+// position keeps that exact position, so a body there cancels against it as
+// the reference's equal-centre skip does; a massless cell sits at its
+// geometric centre.  Second moments (kQuad) are f32, combined with the
+// parallel-axis rule S = sum_c [S_c + M_c (c_c - c)(c_c - c)^T].
 __device__ __forceinline__ void store_quad(const NodeArrays &nd, int i, const float s[6])
 {
     nd.quad_a[i] = make_float4(s[0], s[1], s[2], s[0] + s[1] + s[2]);
     nd.quad_b[i] = make_float4(s[3], s[4], s[5], 0.f);
 }
 
-__device__ __forceinline__ void node_geometry(const NodeArrays &nd, int i)
+// (ah, al) + (bh, bl) as a normalised double-float pair.
+__device__ __forceinline__ void df_add(float &ah, float &al, float bh, float bl)
 {
-    const size_t cap = nd.cap;
-    nd.geo[i] = make_float4((float)nd.c64[i], (float)nd.c64[cap + i], (float)nd.c64[2 * cap + i],
-                            (float)nd.c64[3 * cap + i]);
-    nd.meta[i] = make_int4(i | ((int)nd.nchild[i] << 28), nd.child[i], nd.begin[i], nd.count[i]);
+    float s, e;
+    two_sum(ah, bh, s, e);
+    e += al + bl;
+    ah = s + e;
+    al = e - (ah - s);
 }
 
-// f32 centre of mass from the f64 sums (one f64 reciprocal, three products).
-__device__ __forceinline__ float4 com_from_sums(const NodeArrays &nd, int i, double4 m)
+// The f64 value v as a double-float pair.
+__device__ __forceinline__ void df_from(double v, float &h, float &l)
 {
-    if (m.x != 0.0) {
-        const double r = __drcp_rn(m.x);
-        return make_float4((float)(m.y * r), (float)(m.z * r), (float)(m.w * r), (float)m.x);
-    }
-    return make_float4((float)nd.c64[i], (float)nd.c64[nd.cap + i],
-                       (float)nd.c64[2 * (size_t)nd.cap + i], 0.f);
+    h = __double2float_rn(v);
+    l = __double2float_rn(__dsub_rn(v, (double)h));
+}
+
+// f32 rounding of (sh + sl) / (mh + ml): an f32 quotient corrected once with
+// its exact residual (TwoProduct by FMA).
+__device__ __forceinline__ float df_div(float sh, float sl, float mh, float ml)
+{
+    const float q = sh / mh;
+    const float p = q * mh;
+    const float pe = fmaf(q, mh, -p);
+    const float r = fmaf(-q, ml, ((sh - p) - pe) + sl);
+    return q + r / mh;
+}
+
+__device__ __forceinline__ float4 df_com(const float4 h, const float4 l, float4 geo)
+{
+    if (h.x == 0.f && l.x == 0.f) return make_float4(geo.x, geo.y, geo.z, 0.f);
+    return make_float4(df_div(h.y, l.y, h.x, l.x), df_div(h.z, l.z, h.x, l.x),
+                       df_div(h.w, l.w, h.x, l.x), h.x + l.x);
 }
 
 __global__ void moments_kernel(NodeArrays nd, const LevelInfo *__restrict__ lv,
@@ -743,23 +781,28 @@ __global__ void moments_kernel(NodeArrays nd, const LevelInfo *__restrict__ lv,
     const int total = lv->total;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
         if (nd.child[i] >= 0) continue;
-        node_geometry(nd, i);
         const int b = nd.begin[i], e = b + nd.count[i];
         const float4 p0 = sbody[b];
-        double4 ms = make_double4(0.0, 0.0, 0.0, 0.0);
+        double m0 = 0.0, m1 = 0.0, m2 = 0.0, m3 = 0.0;
         bool same = true;
         for (int j = b; j < e; ++j) {
             const double m = smass[j];
-            ms.x += m;
-            ms.y = fma(m, spos[j], ms.y);
-            ms.z = fma(m, spos[n + j], ms.z);
-            ms.w = fma(m, spos[2 * (size_t)n + j], ms.w);
+            m0 += m;
+            m1 = fma(m, spos[j], m1);
+            m2 = fma(m, spos[n + j], m2);
+            m3 = fma(m, spos[2 * (size_t)n + j], m3);
             const float4 p = sbody[j];
             same = same && p.x == p0.x && p.y == p0.y && p.z == p0.z;
         }
-        nd.msum[i] = ms;
-        const float4 com = same ? make_float4(p0.x, p0.y, p0.z, (float)ms.x)
-                                : com_from_sums(nd, i, ms);
+        float4 h, l;
+        df_from(m0, h.x, l.x);
+        df_from(m1, h.y, l.y);
+        df_from(m2, h.z, l.z);
+        df_from(m3, h.w, l.w);
+        nd.msum_hi[i] = h;
+        nd.msum_lo[i] = l;
+        const float4 com = same ? make_float4(p0.x, p0.y, p0.z, h.x + l.x)
+                                : df_com(h, l, nd.geo[i]);
         nd.com[i] = com;
         if (quad) {
             float q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -785,19 +828,18 @@ __global__ void moments_kernel(NodeArrays nd, const LevelInfo *__restrict__ lv,
             if (arrived + 1u != (uint32_t)nd.nchild[par]) break;
             __threadfence();
             nd.arrivals[par] = 0u;  // ready for the next build
-            node_geometry(nd, par);
             const int fc = nd.child[par], nc = nd.nchild[par];
-            double4 pm = make_double4(0.0, 0.0, 0.0, 0.0);
-            for (int k = fc; k < fc + nc; ++k) {
-                const double2 *q2 = reinterpret_cast<const double2 *>(&nd.msum[k]);
-                const double2 lo = __ldcg(q2), hi = __ldcg(q2 + 1);
-                pm.x += lo.x;
-                pm.y += lo.y;
-                pm.z += hi.x;
-                pm.w += hi.y;
+            float4 ph = __ldcg(&nd.msum_hi[fc]), pl = __ldcg(&nd.msum_lo[fc]);
+            for (int k = fc + 1; k < fc + nc; ++k) {
+                const float4 ch = __ldcg(&nd.msum_hi[k]), cl = __ldcg(&nd.msum_lo[k]);
+                df_add(ph.x, pl.x, ch.x, cl.x);
+                df_add(ph.y, pl.y, ch.y, cl.y);
+                df_add(ph.z, pl.z, ch.z, cl.z);
+                df_add(ph.w, pl.w, ch.w, cl.w);
             }
-            nd.msum[par] = pm;
-            const float4 cp = com_from_sums(nd, par, pm);
+            nd.msum_hi[par] = ph;
+            nd.msum_lo[par] = pl;
+            const float4 cp = df_com(ph, pl, nd.geo[par]);
             nd.com[par] = cp;
             if (quad) {
                 float t[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -1152,26 +1194,32 @@ traverse_warp_kernel(TravArgs a_in)
     const float2 nqx = make_float2(-q.x, -q.x), nqy = make_float2(-q.y, -q.y);
     const float2 nqz = make_float2(-q.z, -q.z), e2 = make_float2(a.e, a.e);
     auto flush = [&]() {
-        // bodies: staged as planes of (x, y, z, m) so that entries 2k and
-        // 2k + 1 load as one float2 per component and two interactions go
-        // through packed FADD2/FMUL2/FFMA2 (an odd count is padded with a
-        // massless entry, which adds exactly zero)
+        // bodies: entries 2k and 2k + 1 are staged interleaved as
+        // (x, x', y, y')(z, z', m, m'), so two 128-bit loads give the float2
+        // operands of two interactions, which go through packed
+        // FADD2/FMUL2/FFMA2 (an odd count is padded with a massless entry,
+        // which adds exactly zero)
+        // the next tile's bodies are loaded while the current one is evaluated
+        float4 nb = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (lane < nq) nb = a.sbody[queue[warp][lane]];
         for (int j0 = 0; j0 < nq; j0 += 32) {
             const int m = min(32, nq - j0);
             __syncwarp();
-            float4 bj = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (lane < m) bj = a.sbody[queue[warp][j0 + lane]];
-            float *pl = reinterpret_cast<float *>(&tile[warp][0]);
-            pl[lane] = bj.x;
-            pl[32 + lane] = bj.y;
-            pl[64 + lane] = bj.z;
-            pl[96 + lane] = bj.w;
+            const float4 bj = nb;
+            nb = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (j0 + 32 + lane < nq) nb = a.sbody[queue[warp][j0 + 32 + lane]];
+            float *pl = reinterpret_cast<float *>(&tile[warp][lane & ~1]) + (lane & 1);
+            pl[0] = bj.x;
+            pl[2] = bj.y;
+            pl[4] = bj.z;
+            pl[6] = bj.w;
             __syncwarp();
-            const float2 *px2 = reinterpret_cast<const float2 *>(pl);
             float2 sx = make_float2(0.f, 0.f), sy = sx, sz = sx;
-            for (int jj = 0; jj < (m + 1) >> 1; ++jj)
-                pair_acc2(nqx, nqy, nqz, px2[jj], px2[16 + jj], px2[32 + jj], px2[48 + jj], e2,
-                          sx, sy, sz);
+            for (int jj = 0; jj < (m + 1) >> 1; ++jj) {
+                const float4 A = tile[warp][2 * jj], B = tile[warp][2 * jj + 1];
+                pair_acc2(nqx, nqy, nqz, make_float2(A.x, A.y), make_float2(A.z, A.w),
+                          make_float2(B.x, B.y), make_float2(B.z, B.w), e2, sx, sy, sz);
+            }
             ax += sx.x + sx.y;
             ay += sy.x + sy.y;
             az += sz.x + sz.y;
@@ -1333,6 +1381,7 @@ inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
 // ---------------------------------------------------------------------------
 struct BhWorkspace {
     int device = 0;
+    cudaStream_t stream = nullptr;  // allocations and frees are ordered on it
     size_t cap_n = 0;
     int grid_build = 0;  // blocks of the per-level build kernels
     uint64_t *keys[2] = {nullptr, nullptr};
@@ -1364,24 +1413,22 @@ static void ws_release(BhWorkspace *ws)
 {
     void *p[] = {ws->keys[0],  ws->keys[1],   ws->vals[0],       ws->vals[1],     ws->sort_meta,
                  ws->sort_status,
-                 ws->sbody,    ws->spos,      ws->smass,      ws->nd.msum,
+                 ws->sbody,    ws->spos,      ws->smass,      ws->nd.msum_hi, ws->nd.msum_lo,
                  ws->nd.begin, ws->nd.count,  ws->nd.child,      ws->nd.nchild,   ws->nd.level,
                  ws->nd.c64,   ws->nd.geo,    ws->nd.com,        ws->lv,          ws->level_status,
                  ws->extent_bits, ws->flags, ws->nd.meta, ws->stats,
                  ws->top, ws->top_blockmin, ws->nd.parent, ws->nd.quad_a, ws->nd.quad_b,
                  ws->nd.arrivals};
-    for (void *q : p)
-        if (q) cudaFree(q);
+    for (void *q : p) dev_free(q, ws->stream);
 }
 
 template <typename T>
-static int wsalloc(T *&p, size_t count)
+static int wsalloc(T *&p, size_t count, cudaStream_t st)
 {
-    PG_CUDA(cudaMalloc((void **)&p, (count ? count : 1) * sizeof(T)));
-    return PHYSIM_OK;
+    return dev_alloc(p, count, st);
 }
 
-int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf)
+int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf, cudaStream_t stream)
 {
     leaf = leaf < 1 ? 1 : leaf;
     if (ws && n <= ws->cap_n && leaf >= ws->leaf_min) return PHYSIM_OK;
@@ -1393,6 +1440,7 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf)
     BhWorkspace *w = new (std::nothrow) BhWorkspace();
     PG_CHECK(w, PHYSIM_ERR_MEMORY, "out of host memory");
     w->device = device;
+    w->stream = stream;
     const size_t cap = n < 64 ? 64 : n;
     w->cap_n = cap;
     const int sms = device_sm_count(device);
@@ -1405,7 +1453,7 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf)
     w->leaf_min = leaf;
     int rc = PHYSIM_OK;
 #define PG_WA(ptr, cnt)                                                                     \
-    if (rc == PHYSIM_OK) rc = wsalloc(ptr, cnt)
+    if (rc == PHYSIM_OK) rc = wsalloc(ptr, cnt, stream)
     PG_WA(w->keys[0], cap);
     PG_WA(w->keys[1], cap);
     PG_WA(w->vals[0], cap);
@@ -1425,7 +1473,8 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf)
     PG_WA(w->nd.com, ncap);
     PG_WA(w->nd.meta, ncap);
     PG_WA(w->nd.parent, ncap);
-    PG_WA(w->nd.msum, ncap);
+    PG_WA(w->nd.msum_hi, ncap);
+    PG_WA(w->nd.msum_lo, ncap);
     PG_WA(w->nd.quad_a, ncap);
     PG_WA(w->nd.quad_b, ncap);
     PG_WA(w->nd.arrivals, ncap);
@@ -1439,18 +1488,19 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf)
     PG_WA(w->flags, 4);
 #undef PG_WA
     w->nd.cap = (int)ncap;
-    if (rc == PHYSIM_OK && (cudaMemset(w->flags, 0, 4 * sizeof(uint32_t)) != cudaSuccess ||
-                            cudaMemset(w->nd.arrivals, 0, ncap * sizeof(uint32_t)) != cudaSuccess ||
-                            cudaMemset(w->lv, 0, sizeof(LevelInfo)) != cudaSuccess ||
-                            cudaMemset(w->level_status, 0,
-                                       (ncap / kBuildThreads + 2) * sizeof(unsigned long long)) !=
-                                cudaSuccess ||
-                            cudaMemset(w->sort_meta, 0,
-                                       ((size_t)kSortPasses * kRadixBuckets + kSortPasses + 1) *
-                                           sizeof(uint32_t)) != cudaSuccess ||
-                            cudaMemset(w->sort_status, 0,
-                                       (size_t)kRadixBuckets * tiles *
-                                           sizeof(unsigned long long)) != cudaSuccess))
+    if (rc == PHYSIM_OK &&
+        (cudaMemsetAsync(w->flags, 0, 4 * sizeof(uint32_t), stream) != cudaSuccess ||
+         cudaMemsetAsync(w->nd.arrivals, 0, ncap * sizeof(uint32_t), stream) != cudaSuccess ||
+         cudaMemsetAsync(w->lv, 0, sizeof(LevelInfo), stream) != cudaSuccess ||
+         cudaMemsetAsync(w->level_status, 0,
+                         (ncap / kBuildThreads + 2) * sizeof(unsigned long long),
+                         stream) != cudaSuccess ||
+         cudaMemsetAsync(w->sort_meta, 0,
+                         ((size_t)kSortPasses * kRadixBuckets + kSortPasses + 1) * sizeof(uint32_t),
+                         stream) != cudaSuccess ||
+         cudaMemsetAsync(w->sort_status, 0,
+                         (size_t)kRadixBuckets * tiles * sizeof(unsigned long long),
+                         stream) != cudaSuccess))
         rc = PHYSIM_ERR_CUDA;
     if (rc != PHYSIM_OK) {
         ws_release(w);

@@ -12,13 +12,13 @@
 
 namespace pg {
 
-static int ensure_doubles(double *&p, size_t &cap, size_t need)
+static int ensure_doubles(double *&p, size_t &cap, size_t need, cudaStream_t st)
 {
     if (need <= cap) return PHYSIM_OK;
-    if (p) cudaFree(p);
+    dev_free(p, st);
     p = nullptr;
     cap = 0;
-    PG_CUDA(cudaMalloc((void **)&p, need * sizeof(double)));
+    PG_TRY(dev_alloc(p, need, st));
     cap = need;
     return PHYSIM_OK;
 }
@@ -34,12 +34,12 @@ static int accumulate_locked(ElementState *el, const Entity *state, size_t n, Ac
     }
     cudaStream_t st = el->stream;
     const bool tree = el->kind != 0;
-    PG_TRY(bodies_reserve(el->bodies, n, tree));
+    PG_TRY(bodies_reserve(el->bodies, n, tree, st));
     if (el->acc_cap < n) {
-        if (el->d_acc) cudaFree(el->d_acc);
+        dev_free(el->d_acc, st);
         el->d_acc = nullptr;
         el->acc_cap = 0;
-        PG_CUDA(cudaMalloc((void **)&el->d_acc, n * sizeof(Acceleration)));
+        PG_TRY(dev_alloc(el->d_acc, n, st));
         el->acc_cap = n;
     }
     PG_CUDA(cudaMemcpyAsync(el->bodies.aos, state, n * sizeof(Entity), cudaMemcpyHostToDevice, st));
@@ -52,11 +52,11 @@ static int accumulate_locked(ElementState *el, const Entity *state, size_t n, Ac
             el->plan_n = (int)n;
         }
         splits = el->plan.splits;
-        PG_TRY(ensure_doubles(el->partial, el->partial_cap, (size_t)splits * 3 * n));
+        PG_TRY(ensure_doubles(el->partial, el->partial_cap, (size_t)splits * 3 * n, st));
         PG_TRY(launch_direct(el->plan, el->bodies.body4, (float)el->e, el->partial, st));
     } else {
-        PG_TRY(ensure_doubles(el->partial, el->partial_cap, 3 * n));
-        PG_TRY(bh_reserve(el->bh, n, el->device, el->leaf_size));
+        PG_TRY(ensure_doubles(el->partial, el->partial_cap, 3 * n, st));
+        PG_TRY(bh_reserve(el->bh, n, el->device, el->leaf_size, st));
         BhParams p;
         p.nchild = el->kind == 1 ? 8 : 4;
         p.theta = el->theta;
@@ -85,10 +85,11 @@ void element_destroy(ElementState *el)
     if (el->ready) {
         cudaSetDevice(el->device);
         cudaStreamSynchronize(el->stream);
-        bodies_free(el->bodies);
-        if (el->d_acc) cudaFree(el->d_acc);
-        if (el->partial) cudaFree(el->partial);
+        bodies_free(el->bodies, el->stream);
+        dev_free(el->d_acc, el->stream);
+        dev_free(el->partial, el->stream);
         bh_free(el->bh);
+        cudaStreamSynchronize(el->stream);
         cudaStreamDestroy(el->stream);
     }
     delete el;

@@ -66,8 +66,22 @@ struct DeviceBodies {
     Entity *aos = nullptr;  // staging for host<->device copies
 };
 
-int bodies_reserve(DeviceBodies &b, size_t n, bool with_state);
-void bodies_free(DeviceBodies &b);
+// Stream-ordered device memory (cudaMallocAsync / cudaFreeAsync on the
+// owner's stream).  cudaMalloc and cudaFree synchronise the whole device, so
+// objects created and destroyed while others run (the server's jobs) would
+// stall every stream; stream-ordered allocation does not, and the device's
+// default pool keeps freed memory for reuse.  count 0 allocates one element.
+int dev_alloc_bytes(void **p, size_t bytes, cudaStream_t stream);
+void dev_free(void *p, cudaStream_t stream);
+template <typename T>
+inline int dev_alloc(T *&p, size_t count, cudaStream_t stream)
+{
+    return dev_alloc_bytes((void **)&p, (count ? count : 1) * sizeof(T), stream);
+}
+
+// `stream` orders the allocations (and frees) with the owner's work.
+int bodies_reserve(DeviceBodies &b, size_t n, bool with_state, cudaStream_t stream);
+void bodies_free(DeviceBodies &b, cudaStream_t stream);
 
 // Unpacks an Entity array already on the device into the SoA arrays.
 int launch_unpack(DeviceBodies &b, const Entity *d_aos, size_t n, bool full_state,

@@ -11,8 +11,9 @@
 //      code as the per-simulation kernel;
 //   2. one kernel combining the partial sums and applying verlet in f64 for
 //      every member with steps left, then counting the step.
-// A run of steps is captured once into a CUDA graph and replayed.  The
-// autotuner times the candidate kernel shapes (threads x bodies per thread)
+// One step is captured once (per work plan) into a CUDA graph and replayed
+// for every step.  Members can be resized in place (a finished member's slot
+// takes the next job; the work plan is rebuilt).  The autotuner times the candidate kernel shapes (threads x bodies per thread)
 // and j-chunk lengths on the members' own data and keeps the fastest.
 #include <stdlib.h>
 #include <string.h>
@@ -171,6 +172,24 @@ __global__ void ensemble_pack_kernel(Entity *out, int n, int off, const uint8_t 
     out[i] = en;
 }
 
+// A member's slot range [off, off + slot_len): the first n slots belong to
+// member k, the rest are padding (member -1, zero mass, fixed).
+__global__ void ensemble_slot_kernel(int32_t *slot_member, float4 *body4, uint8_t *fixed,
+                                     double *m, int off, int slot_len, int n, int k)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= slot_len) return;
+    const int s = off + i;
+    if (i < n) {
+        slot_member[s] = k;
+    } else {
+        slot_member[s] = -1;
+        body4[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        fixed[s] = 1;
+        m[s] = 0.0;
+    }
+}
+
 struct Shape {
     int block, ipt;
 };
@@ -208,6 +227,7 @@ struct PhysimEnsemble {
     bool own_stream = false;
     cudaStream_t stream = nullptr;
     std::vector<size_t> sizes;
+    std::vector<size_t> caps;  // bodies each member's slot was created for
     std::vector<int32_t> offsets;
     std::vector<MemberInfo> members;
     int slots = 0;
@@ -242,10 +262,9 @@ struct PhysimEnsemble {
 namespace {
 
 template <typename T>
-int ealloc(T *&p, size_t count)
+int ealloc(PhysimEnsemble *E, T *&p, size_t count)
 {
-    PG_CUDA(cudaMalloc((void **)&p, (count ? count : 1) * sizeof(T)));
-    return PHYSIM_OK;
+    return dev_alloc(p, count, E->stream);
 }
 
 void drop_graph(PhysimEnsemble *E)
@@ -286,9 +305,9 @@ int plan_ensemble(PhysimEnsemble *E, int block, int ipt, int chunk)
     std::vector<WorkUnit> sorted(units.size());
     for (size_t i = 0; i < order.size(); ++i) sorted[i] = units[order[i]];
     if (sorted.size() > E->units_cap) {
-        if (E->d_units) cudaFree(E->d_units);
+        dev_free(E->d_units, E->stream);
         E->d_units = nullptr;
-        PG_TRY(ealloc(E->d_units, sorted.size()));
+        PG_TRY(ealloc(E, E->d_units, sorted.size()));
         E->units_cap = sorted.size();
     }
     PG_CUDA(cudaMemcpyAsync(E->d_units, sorted.data(), sorted.size() * sizeof(WorkUnit),
@@ -338,8 +357,8 @@ void free_ensemble(PhysimEnsemble *E)
     void *p[] = {E->body4, E->fixed, E->x,  E->y,  E->z,  E->vx, E->vy, E->vz, E->px, E->py,
                  E->pz,    E->m,     E->radius, E->id, E->slot_member, E->d_members, E->d_units,
                  E->remaining, E->done, E->counter, E->partial, E->staging};
-    for (void *q : p)
-        if (q) cudaFree(q);
+    for (void *q : p) dev_free(q, E->stream);
+    if (E->stream) cudaStreamSynchronize(E->stream);
 }
 
 }  // namespace
@@ -361,6 +380,7 @@ int physim_gpu_ensemble_create(const PhysimSimConfig *cfg, const size_t *sizes, 
     E->cfg.e = fabs(cfg->e);
     E->device = cfg->device;
     E->sizes.assign(sizes, sizes + count);
+    E->caps.assign(sizes, sizes + count);
     long long slots = 0;
     long long partial_elems = 0;
     E->members.resize(count);
@@ -394,7 +414,7 @@ int physim_gpu_ensemble_create(const PhysimSimConfig *cfg, const size_t *sizes, 
         rc = PHYSIM_ERR_CUDA;
     }
 #define EA(ptr, cnt)                                                                        \
-    if (rc == PHYSIM_OK) rc = ealloc(ptr, cnt)
+    if (rc == PHYSIM_OK) rc = ealloc(E, ptr, cnt)
     EA(E->body4, slots);
     EA(E->fixed, slots);
     EA(E->x, slots);
@@ -456,9 +476,9 @@ int physim_gpu_ensemble_upload(PhysimEnsemble *E, size_t index, const Entity *st
              index, E->sizes[index], n);
     PG_CUDA(cudaSetDevice(E->device));
     if (n > E->staging_cap) {
-        if (E->staging) cudaFree(E->staging);
+        dev_free(E->staging, E->stream);
         E->staging = nullptr;
-        PG_TRY(ealloc(E->staging, n));
+        PG_TRY(ealloc(E, E->staging, n));
         E->staging_cap = n;
     }
     PG_CUDA(cudaMemcpyAsync(E->staging, state, n * sizeof(Entity), cudaMemcpyHostToDevice,
@@ -560,13 +580,39 @@ int physim_gpu_ensemble_autotune(PhysimEnsemble *E, PhysimEnsembleTuning *out)
     return PHYSIM_OK;
 }
 
+int physim_gpu_ensemble_resize_member(PhysimEnsemble *E, size_t index, size_t n)
+{
+    PG_CHECK(E, PHYSIM_ERR_ARGUMENT, "null ensemble");
+    PG_CHECK(index < E->members.size(), PHYSIM_ERR_ARGUMENT, "member %zu out of range", index);
+    PG_CHECK(n <= E->caps[index], PHYSIM_ERR_ARGUMENT,
+             "member %zu was created for %zu bodies, not %zu", index, E->caps[index], n);
+    PG_CUDA(cudaSetDevice(E->device));
+    PG_CUDA(cudaStreamSynchronize(E->stream));
+    const int off = E->members[index].off;
+    const int slot_len = (int)pad_bodies(E->caps[index]);
+    ensemble_slot_kernel<<<cdiv(slot_len, 256), 256, 0, E->stream>>>(
+        E->slot_member, E->body4, E->fixed, E->m, off, slot_len, (int)n, (int)index);
+    PG_CUDA(cudaGetLastError());
+    E->members[index].n = (int32_t)n;
+    E->sizes[index] = n;
+    const unsigned long long zero = 0ull;
+    PG_CUDA(cudaMemcpyAsync(E->done + index, &zero, sizeof zero, cudaMemcpyHostToDevice,
+                            E->stream));
+    PG_CUDA(cudaMemcpyAsync(E->remaining + index, &zero, sizeof zero, cudaMemcpyHostToDevice,
+                            E->stream));
+    drop_graph(E);
+    return plan_ensemble(E, E->block, E->ipt, E->chunk);
+}
+
 int physim_gpu_ensemble_step(PhysimEnsemble *E, uint32_t steps)
 {
     PG_CHECK(E, PHYSIM_ERR_ARGUMENT, "null ensemble");
     if (steps == 0) return PHYSIM_OK;
     PG_CUDA(cudaSetDevice(E->device));
-    if (!E->graph_exec || E->graph_steps != steps) {
-        drop_graph(E);
+    // one step is captured once per plan and replayed `steps` times, so the
+    // step count of a call and re-plans (members resized) cost no re-capture
+    // of long graphs
+    if (!E->graph_exec) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         PG_CUDA(cudaStreamIsCapturing(E->stream, &cs));
         if (cs != cudaStreamCaptureStatusNone) {  // the caller is capturing: plain launches
@@ -574,8 +620,7 @@ int physim_gpu_ensemble_step(PhysimEnsemble *E, uint32_t steps)
             return PHYSIM_OK;
         }
         PG_CUDA(cudaStreamBeginCapture(E->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = PHYSIM_OK;
-        for (uint32_t k = 0; k < steps && rc == PHYSIM_OK; ++k) rc = enqueue_step(E);
+        int rc = enqueue_step(E);
         cudaGraph_t g = nullptr;
         const cudaError_t ce = cudaStreamEndCapture(E->stream, &g);
         if (rc != PHYSIM_OK || ce != cudaSuccess) {
@@ -589,9 +634,9 @@ int physim_gpu_ensemble_step(PhysimEnsemble *E, uint32_t steps)
             return PHYSIM_ERR_CUDA;
         }
         E->graph = g;
-        E->graph_steps = steps;
+        E->graph_steps = 1;
     }
-    PG_CUDA(cudaGraphLaunch(E->graph_exec, E->stream));
+    for (uint32_t k = 0; k < steps; ++k) PG_CUDA(cudaGraphLaunch(E->graph_exec, E->stream));
     return PHYSIM_OK;
 }
 
@@ -603,9 +648,9 @@ int physim_gpu_ensemble_download(PhysimEnsemble *E, size_t index, Entity *state,
              index, E->sizes[index], n);
     PG_CUDA(cudaSetDevice(E->device));
     if (n > E->staging_cap) {
-        if (E->staging) cudaFree(E->staging);
+        dev_free(E->staging, E->stream);
         E->staging = nullptr;
-        PG_TRY(ealloc(E->staging, n));
+        PG_TRY(ealloc(E, E->staging, n));
         E->staging_cap = n;
     }
     const int off = E->members[index].off;

@@ -325,49 +325,65 @@ __global__ void rk4_aos_stage_kernel(const Entity *ent, const Entity *q_in,
     out[i] = o;
 }
 
-template <typename T>
-int dalloc(T **p, size_t count)
+}  // namespace
+
+int dev_alloc_bytes(void **p, size_t bytes, cudaStream_t stream)
 {
-    if (count == 0) count = 1;
-    cudaError_t err = cudaMalloc((void **)p, count * sizeof(T));
+    *p = nullptr;
+    int device = 0;
+    if (cudaGetDevice(&device) == cudaSuccess && device >= 0 && device < 64) {
+        // keep freed blocks in the device's default pool for reuse (a
+        // setting of this process's pool only)
+        static bool pool_set[64] = {false};
+        if (!pool_set[device]) {
+            cudaMemPool_t pool;
+            if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+                uint64_t keep = ~0ull;
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            }
+            pool_set[device] = true;
+        }
+    }
+    cudaError_t err = cudaMallocAsync(p, bytes ? bytes : 1, stream);
     if (err != cudaSuccess) {
         *p = nullptr;
-        set_error("cudaMalloc of %zu bytes failed: %s", count * sizeof(T),
-                  cudaGetErrorString(err));
+        set_error("device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(err));
         return PHYSIM_ERR_MEMORY;
     }
     return PHYSIM_OK;
 }
 
-}  // namespace
+void dev_free(void *p, cudaStream_t stream)
+{
+    if (p) cudaFreeAsync(p, stream);
+}
 
-void bodies_free(DeviceBodies &b)
+void bodies_free(DeviceBodies &b, cudaStream_t stream)
 {
     void *ptrs[] = {b.body4, b.fixed, b.x,  b.y,  b.z,      b.vx, b.vy,
                     b.vz,    b.px,    b.py, b.pz, b.m,      b.radius, b.id, b.aos};
-    for (void *p : ptrs)
-        if (p) cudaFree(p);
+    for (void *p : ptrs) dev_free(p, stream);
     b = DeviceBodies();
 }
 
-int bodies_reserve(DeviceBodies &b, size_t n, bool with_state)
+int bodies_reserve(DeviceBodies &b, size_t n, bool with_state, cudaStream_t stream)
 {
     size_t need = pad_bodies(n);
     if (need <= b.cap && (!with_state || b.x)) {
         b.n = n;
         return PHYSIM_OK;
     }
-    bodies_free(b);
+    bodies_free(b, stream);
     b.cap = need;
     b.n = n;
-    PG_TRY(dalloc(&b.body4, need));
-    PG_TRY(dalloc(&b.fixed, need));
-    PG_TRY(dalloc(&b.aos, need));
-    PG_TRY(dalloc(&b.m, need));
+    PG_TRY(dev_alloc(b.body4, need, stream));
+    PG_TRY(dev_alloc(b.fixed, need, stream));
+    PG_TRY(dev_alloc(b.aos, need, stream));
+    PG_TRY(dev_alloc(b.m, need, stream));
     if (with_state) {
         double **d[] = {&b.x, &b.y, &b.z, &b.vx, &b.vy, &b.vz, &b.px, &b.py, &b.pz, &b.radius};
-        for (double **p : d) PG_TRY(dalloc(p, need));
-        PG_TRY(dalloc(&b.id, need));
+        for (double **p : d) PG_TRY(dev_alloc(*p, need, stream));
+        PG_TRY(dev_alloc(b.id, need, stream));
     }
     return PHYSIM_OK;
 }

@@ -59,7 +59,8 @@ struct BhParams {
     double com_theta = 0.0;
 };
 
-int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf);
+// Allocations (and the frees of bh_free) are ordered on `stream`.
+int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf, cudaStream_t stream);
 // Waits for the stream, then reports (and clears) the error flags the kernels
 // raise: PHYSIM_ERR_TREE for a traversal stack overflow, PHYSIM_ERR_TIMEOUT
 // for a radix-sort look-back wait that gave up.

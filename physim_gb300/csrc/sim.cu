@@ -183,27 +183,20 @@ int physim_gpu_sim_create(const PhysimSimConfig *cfg, size_t n, PhysimSim **out)
         }
         s->own_stream = true;
     }
-    rc = bodies_reserve(s->b, n, true);
+    rc = bodies_reserve(s->b, n, true, s->stream);
     size_t partial_elems = 3 * (n ? n : 1);
     if (rc == PHYSIM_OK && cfg->gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO) {
         s->plan = plan_direct((int)n, cfg->device, cfg->compensated != 0);
         partial_elems *= (size_t)s->plan.splits;
     }
     if (rc == PHYSIM_OK && cfg->gravity != PHYSIM_GRAVITY_SIMPLE_ASTRO)
-        rc = bh_reserve(s->bh, n, cfg->device, (int)cfg->leaf_size);
-    if (rc == PHYSIM_OK && cudaMalloc((void **)&s->partial, partial_elems * sizeof(double)) !=
-                               cudaSuccess) {
-        set_error("cudaMalloc of partial sums failed");
-        rc = PHYSIM_ERR_MEMORY;
-    }
+        rc = bh_reserve(s->bh, n, cfg->device, (int)cfg->leaf_size, s->stream);
+    if (rc == PHYSIM_OK) rc = dev_alloc(s->partial, partial_elems, s->stream);
     s->partial_cap = partial_elems;
     if (rc == PHYSIM_OK && cfg->integrator == PHYSIM_INTEGRATOR_RK4) {
-        const size_t m = 6 * (n ? n : 1) * sizeof(double);
-        if (cudaMalloc((void **)&s->rk4_save, m) != cudaSuccess ||
-            cudaMalloc((void **)&s->rk4_ksum, m) != cudaSuccess) {
-            set_error("cudaMalloc of the rk4 stage arrays failed");
-            rc = PHYSIM_ERR_MEMORY;
-        }
+        const size_t m = 6 * (n ? n : 1);
+        rc = dev_alloc(s->rk4_save, m, s->stream);
+        if (rc == PHYSIM_OK) rc = dev_alloc(s->rk4_ksum, m, s->stream);
     }
     if (rc != PHYSIM_OK) {
         physim_gpu_sim_destroy(s);
@@ -294,11 +287,10 @@ int physim_gpu_sim_autotune(PhysimSim *s, PhysimDirectTuning *out)
     for (int c = 0; c < k; ++c) max_splits = std::max(max_splits, cand[c].splits);
     const size_t need = (size_t)max_splits * 3 * s->n;
     if (need > s->partial_cap) {
-        PG_CUDA(cudaStreamSynchronize(s->stream));
-        if (s->partial) cudaFree(s->partial);
+        dev_free(s->partial, s->stream);
         s->partial = nullptr;
         s->partial_cap = 0;
-        PG_CUDA(cudaMalloc((void **)&s->partial, need * sizeof(double)));
+        PG_TRY(dev_alloc(s->partial, need, s->stream));
         s->partial_cap = need;
     }
     cudaEvent_t a, b;
@@ -405,7 +397,7 @@ int physim_gpu_sim_accelerations(PhysimSim *s, Acceleration *acc, size_t n)
     PG_CHECK(s->uploaded, PHYSIM_ERR_ARGUMENT, "accelerations before upload");
     if (n == 0) return PHYSIM_OK;
     PG_CUDA(cudaSetDevice(s->cfg.device));
-    if (!s->acc_soa) PG_CUDA(cudaMalloc((void **)&s->acc_soa, 3 * n * sizeof(double)));
+    if (!s->acc_soa) PG_TRY(dev_alloc(s->acc_soa, 3 * n, s->stream));
     int splits = 1;
     PG_TRY(sim_forces(s, &splits));
     PG_TRY(launch_combine_soa(s->b, s->partial, splits, s->acc_soa, s->stream));
@@ -457,7 +449,7 @@ int physim_gpu_sim_diagnostics(PhysimSim *s, PhysimDiagnostics *out, int with_po
     PG_CHECK(s && out, PHYSIM_ERR_ARGUMENT, "null argument");
     PG_CHECK(s->uploaded, PHYSIM_ERR_ARGUMENT, "diagnostics before upload");
     PG_CUDA(cudaSetDevice(s->cfg.device));
-    if (!s->diag) PG_CUDA(cudaMalloc((void **)&s->diag, 9 * sizeof(double)));
+    if (!s->diag) PG_TRY(dev_alloc(s->diag, 9, s->stream));
     PG_TRY(launch_diagnostics(s->b, s->cfg.e, s->diag, with_potential != 0, s->cfg.device,
                               s->stream));
     double h[9];
@@ -497,15 +489,16 @@ void physim_gpu_sim_destroy(PhysimSim *s)
     if (!s) return;
     cudaSetDevice(s->cfg.device);
     if (s->stream) cudaStreamSynchronize(s->stream);
-    bodies_free(s->b);
-    if (s->partial) cudaFree(s->partial);
-    if (s->acc_soa) cudaFree(s->acc_soa);
-    if (s->diag) cudaFree(s->diag);
-    if (s->rk4_save) cudaFree(s->rk4_save);
-    if (s->rk4_ksum) cudaFree(s->rk4_ksum);
-    bh_free(s->bh);
+    // the graph references the buffers: destroy it before they are freed
     if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
     if (s->graph) cudaGraphDestroy(s->graph);
+    bodies_free(s->b, s->stream);
+    dev_free(s->partial, s->stream);
+    dev_free(s->acc_soa, s->stream);
+    dev_free(s->diag, s->stream);
+    dev_free(s->rk4_save, s->stream);
+    dev_free(s->rk4_ksum, s->stream);
+    bh_free(s->bh);
     for (cudaEvent_t e : s->ev)
         if (e) cudaEventDestroy(e);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);

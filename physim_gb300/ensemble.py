@@ -33,10 +33,35 @@ class Ensemble:
             budget = UNLIMITED if steps is None else int(steps[k])
             self.set_member(k, e, dt, budget)
 
+    @classmethod
+    def slots(cls, capacities: Sequence[int], config: SimConfig) -> "Ensemble":
+        """An ensemble of empty member slots (each able to hold up to its
+        capacity of bodies), for continuous batching: resize_member + upload +
+        set_member put a job in a slot."""
+        self = cls.__new__(cls)
+        self.sizes = [int(c) for c in capacities]
+        sizes = (C.c_size_t * len(self.sizes))(*self.sizes)
+        h = C.c_void_p()
+        cfg = config.to_c()
+        check(lib.physim_gpu_ensemble_create(C.byref(cfg), sizes, len(self.sizes), C.byref(h)),
+              "physim_gpu_ensemble_create")
+        self.handle = h
+        self.config = config
+        for k in range(len(self.sizes)):
+            self.resize_member(k, 0)
+        return self
+
     def upload(self, index: int, state: np.ndarray) -> None:
         state = as_entities(state)
         check(lib.physim_gpu_ensemble_upload(self.handle, index, state.ctypes.data, len(state)),
               "physim_gpu_ensemble_upload")
+
+    def resize_member(self, index: int, n: int) -> None:
+        """Reuses member `index`'s slot for n bodies (at most its original
+        count); upload and set_member before it steps again."""
+        check(lib.physim_gpu_ensemble_resize_member(self.handle, index, n),
+              "physim_gpu_ensemble_resize_member")
+        self.sizes[index] = n
 
     def set_member(self, index: int, e: float, dt: float, steps_remaining: int = UNLIMITED) -> None:
         check(lib.physim_gpu_ensemble_set_member(self.handle, index, e, dt, steps_remaining),

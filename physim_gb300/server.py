@@ -55,6 +55,17 @@ class JobSpec:
         per = BYTES_PER_BODY_DIRECT if self.gravity == "simple_astro" else BYTES_PER_BODY_TREE
         return BYTES_FIXED + per * self.n
 
+    def step_seconds(self) -> float:
+        """Rough device seconds per step on one GB300 (scheduling estimates
+        only): N^2 pairs at 2.3e12 pairs/s for the direct sum, 1.4 us per
+        1,000 bodies plus launch latency for Barnes-Hut."""
+        if self.gravity == "simple_astro":
+            return self.n * self.n / 2.3e12 + 5e-6
+        return self.n * 1.4e-9 + 6e-5
+
+    def work_seconds(self) -> float:
+        return self.steps * self.step_seconds()
+
 
 @dataclass
 class JobResult:
@@ -126,21 +137,61 @@ class Unit:
 class Executor:
     def make_units(self, jobs: list[JobSpec]) -> list[Unit]: ...
 
+    def unit_cost(self, job: JobSpec) -> int:
+        """Units a job adds when admitted (0: it joins an existing unit)."""
+        return 1
+
 
 class GpuExecutor(Executor):
     """Runs direct-sum jobs of one admission round as one ensemble and each
     Barnes-Hut job as one device-resident simulation, each on its own stream;
-    a tick is about `tick_ms` of device work."""
+    a tick is about `tick_ms` of device work.  With `priorities`, a unit's
+    stream gets a CUDA stream priority by its per-step cost (cheap steps run
+    first when the GPU is contended), so short jobs are not held behind the
+    kernels of long ones."""
 
-    def __init__(self, device: int = 0, tick_ms: float = 20.0, download: bool = True):
+    def __init__(self, device: int = 0, tick_ms: float = 20.0, download: bool = True,
+                 priorities: bool = False, pool_slots: int = 0, pool_bodies: int = 32768):
         self.device = device
         self.tick_ms = tick_ms
         self.download = download
+        self.priorities = priorities
+        # pool_slots > 0: direct-sum jobs join one long-lived ensemble of
+        # pool_slots member slots (up to pool_bodies bodies each) as slots
+        # free up, instead of forming one ensemble per admission round
+        self.pool_slots = pool_slots
+        self.pool_bodies = pool_bodies
+        self.pool: _PoolUnit | None = None
+
+    def _pooled(self, job: JobSpec) -> bool:
+        return (self.pool_slots > 0 and job.gravity == "simple_astro"
+                and job.n <= self.pool_bodies)
+
+    def unit_cost(self, job: JobSpec) -> int:
+        if self._pooled(job):
+            return 0 if (self.pool is not None and self.pool.alive()) else 1
+        return 1
+
+    def stream_for(self, step_seconds: float):
+        """A torch stream for a unit (None: the unit makes its own)."""
+        if not self.priorities:
+            return None
+        import torch
+        # lower number = higher priority; torch clamps to the device's range
+        prio = -3 if step_seconds < 1e-4 else (-2 if step_seconds < 3e-4 else
+                                                 (-1 if step_seconds < 1e-3 else 0))
+        return torch.cuda.Stream(device=torch.device("cuda", self.device), priority=prio)
 
     def make_units(self, jobs: list[JobSpec]) -> list[Unit]:
-        direct = [j for j in jobs if j.gravity == "simple_astro"]
+        pooled = [j for j in jobs if self._pooled(j)]
+        direct = [j for j in jobs if j.gravity == "simple_astro" and not self._pooled(j)]
         tree = [j for j in jobs if j.gravity != "simple_astro"]
         units: list[Unit] = []
+        if pooled:
+            if self.pool is None or not self.pool.alive():
+                self.pool = _PoolUnit(self)
+                units.append(self.pool)
+            self.pool.add(pooled)
         if direct:
             units.append(_EnsembleUnit(direct, self))
         for j in tree:
@@ -187,7 +238,10 @@ class _EnsembleUnit(Unit):
         self.jobs = list(jobs)
         self.ex = ex
         states = [initial_state(j) for j in jobs]
-        cfg = SimConfig(gravity="simple_astro", e=0.01, dt=1e-5, device=ex.device)
+        self.torch_stream = ex.stream_for(max(j.step_seconds() for j in jobs)) \
+            if hasattr(ex, "stream_for") else None
+        cfg = SimConfig(gravity="simple_astro", e=0.01, dt=1e-5, device=ex.device,
+                        stream=self.torch_stream.cuda_stream if self.torch_stream else None)
         self.ens = Ensemble(states, cfg, steps=[j.steps for j in jobs],
                             params=[(j.e, j.dt) for j in jobs])
         self.tick = _CudaTick(self.ens.stream, ex.device)
@@ -228,15 +282,99 @@ class _EnsembleUnit(Unit):
         self.ens.close()
 
 
+class _PoolUnit(Unit):
+    """Continuous batching of direct-sum jobs: one ensemble of fixed member
+    slots; before every tick, jobs waiting for the pool take the free slots
+    (resize + upload + step budget), and after it, finished jobs are
+    downloaded and their slots freed.  Each job starts with the Taylor step
+    and stops at its own step count on the device, so its result is the same
+    as alone."""
+
+    def __init__(self, ex: GpuExecutor):
+        from . import Ensemble, SimConfig
+        self.ex = ex
+        self.jobs: list[JobSpec] = []
+        self.torch_stream = ex.stream_for(0.0)
+        cfg = SimConfig(gravity="simple_astro", e=0.01, dt=1e-5, device=ex.device,
+                        stream=self.torch_stream.cuda_stream if self.torch_stream else None)
+        self.ens = Ensemble.slots([ex.pool_bodies] * ex.pool_slots, cfg)
+        self.tick = _CudaTick(self.ens.stream, ex.device)
+        self.slot_job: list[JobSpec | None] = [None] * ex.pool_slots
+        self.slot_left = [0] * ex.pool_slots
+        self.waiting: collections.deque[JobSpec] = collections.deque()
+        self.tick_steps = 0
+        self.closed = False
+
+    def add(self, jobs: list[JobSpec]) -> None:
+        self.waiting.extend(jobs)
+        self.jobs.extend(jobs)
+
+    def _fill(self) -> None:
+        for k in range(len(self.slot_job)):
+            if not self.waiting:
+                break
+            if self.slot_job[k] is not None:
+                continue
+            j = self.waiting.popleft()
+            self.ens.resize_member(k, j.n)
+            self.ens.upload(k, initial_state(j))
+            self.ens.set_member(k, j.e, j.dt, j.steps)
+            self.slot_job[k] = j
+            self.slot_left[k] = j.steps
+
+    def launch_tick(self) -> None:
+        self._fill()
+        active = [k for k, j in enumerate(self.slot_job) if j is not None and self.slot_left[k]]
+        self.tick_steps = 0
+        if active:
+            est_ms = sum(self.slot_job[k].n ** 2 for k in active) / 2.0e12 * 1e3 + 0.02
+            steps = int(max(1, min(max(self.slot_left[k] for k in active),
+                                   self.ex.tick_ms / est_ms)))
+            self.ens.step(steps)
+            for k in active:
+                t = min(steps, self.slot_left[k])
+                self.slot_left[k] -= t
+                self.tick_steps += t
+        self.tick.record()
+
+    def tick_done(self) -> bool:
+        return self.tick.done()
+
+    def finished_jobs(self):
+        out = []
+        if not any(j is not None for j in self.slot_job):
+            return out
+        _, rem = self.ens.progress()
+        for k, j in enumerate(self.slot_job):
+            if j is not None and rem[k] == 0:
+                out.append((j, self.ens.download(k) if self.ex.download else None))
+                self.slot_job[k] = None
+                self.slot_left[k] = 0
+        return out
+
+    def alive(self) -> bool:
+        return not self.closed and (bool(self.waiting) or
+                                    any(j is not None for j in self.slot_job))
+
+    def close(self) -> None:
+        if not self.closed:
+            self.closed = True
+            self.ens.close()
+
+
 class _SimUnit(Unit):
     def __init__(self, job: JobSpec, ex: GpuExecutor):
         from . import SimConfig, Simulation
         self.jobs = [job]
         self.ex = ex
+        self.torch_stream = ex.stream_for(job.step_seconds()) \
+            if hasattr(ex, "stream_for") else None
         self.sim = Simulation(initial_state(job),
                               SimConfig(gravity=job.gravity, theta=job.theta, e=job.e, dt=job.dt,
                                         leaf_size=job.leaf_size, traversal="warp",
-                                        device=ex.device))
+                                        device=ex.device,
+                                        stream=(self.torch_stream.cuda_stream
+                                                if self.torch_stream else None)))
         self.tick = _CudaTick(self.sim.stream, ex.device)
         est_ms = max(job.n * 1.6e-6, 0.05) if job.gravity != "simple_astro" else \
             max(job.n * job.n / 2.0e12 * 1e3, 0.02)
@@ -277,7 +415,11 @@ class Server:
 
     def __init__(self, executor: Executor, hbm_budget: int = 150 << 30,
                  clock: Callable[[], float] = time.perf_counter,
-                 max_units: int = 64, max_batch: int = 16, keep_states: bool = False):
+                 max_units: int = 64, max_batch: int = 16, keep_states: bool = False,
+                 admission: str = "fifo"):
+        if admission not in ("fifo", "shortest"):
+            raise ValueError(f"unknown admission policy {admission!r}")
+        self.admission = admission
         self.executor = executor
         self.max_batch = max_batch
         self.keep_states = keep_states
@@ -313,17 +455,26 @@ class Server:
             else:
                 self.pending.append(j)
         batch = []
-        # first fit in arrival order; a job that does not fit now keeps its
-        # place and later (smaller) jobs may go ahead of it
+        # first fit in arrival order ("fifo") or in order of estimated device
+        # work ("shortest": shortest job first, ties by arrival); a job that
+        # does not fit now keeps its place and later (smaller) jobs may go
+        # ahead of it
+        if self.admission == "shortest" and len(self.pending) > 1:
+            self.pending = collections.deque(
+                sorted(self.pending, key=lambda j: (j.work_seconds(), j.arrival, j.id)))
         keep = collections.deque()
         room = self.budget - self.in_use
+        new_units = 0
+        cost = getattr(self.executor, "unit_cost", lambda job: 1)
         while self.pending:
             j = self.pending.popleft()
             need = j.device_bytes()
-            if (need <= room and len(self.units) + len(batch) < self.max_units
+            c = cost(j)
+            if (need <= room and len(self.units) + new_units + c <= self.max_units
                     and len(batch) < self.max_batch):
                 batch.append(j)
                 room -= need
+                new_units += c
             else:
                 keep.append(j)
         self.pending = keep

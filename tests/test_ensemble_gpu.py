@@ -107,3 +107,40 @@ def test_upload_resets_member():
     assert list(done) == [5, 2, 5]
     err = trajectory_errors(members[1], got1, _solo(members[1], 2))
     assert err["pos_rel_l2"] < 1e-6, err
+
+
+def test_resized_slots_match_solo_runs():
+    """Continuous batching: empty slots take new members of any size up to
+    their capacity, mid-run, while other members keep stepping; each equals
+    its solo run, and a slot shrunk to a smaller member leaves no stale
+    bodies behind (the larger previous occupant's bodies would add force)."""
+    import physim_gb300 as pg
+    from physim_gb300 import ics
+    from test_verlet_gpu import trajectory_errors
+    cfg = pg.SimConfig(gravity="simple_astro", e=0.01, dt=1e-5)
+    big = ics.cube_with_stars(3000, seed=900)
+    small = ics.plummer(700, seed=901, a=0.1)
+    other = ics.cube_with_stars(1500, seed=902)
+    ens = pg.Ensemble.slots([4096, 4096], cfg)
+    try:
+        ens.resize_member(0, len(big))
+        ens.upload(0, big)
+        ens.set_member(0, 0.01, 1e-5, 6)
+        ens.resize_member(1, len(other))
+        ens.upload(1, other)
+        ens.set_member(1, 0.01, 1e-5, 12)
+        ens.step(6)
+        got_big = ens.download(0)
+        ens.resize_member(0, len(small))  # slot 0 now holds a smaller job
+        ens.upload(0, small)
+        ens.set_member(0, 0.01, 1e-5, 5)
+        ens.step(6)
+        got_small = ens.download(0)
+        got_other = ens.download(1)
+        done, rem = ens.progress()
+    finally:
+        ens.close()
+    assert list(done) == [5, 12] and list(rem) == [0, 0]
+    for s, g, k in ((big, got_big, 6), (small, got_small, 5), (other, got_other, 12)):
+        err = trajectory_errors(s, g, _solo(s, k))
+        assert err["pos_rel_l2"] < 1e-6 and err["vel_rel_l2"] < 1e-6, err

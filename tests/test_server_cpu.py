@@ -171,3 +171,18 @@ def test_one_at_a_time_baseline():
     assert [r.spec.id for r in res] == list(range(6))
     assert ex.batches == [[i] for i in range(6)]
     assert srv.max_running == 1
+
+
+def test_shortest_job_first_admission():
+    """admission="shortest" admits pending jobs in order of estimated device
+    work; "fifo" in arrival order."""
+    jobs = [job(0, 30000, 4000), job(1, 2000, 100), job(2, 8000, 500), job(3, 1000, 50)]
+    for policy, want in (("fifo", [0, 1, 2, 3]), ("shortest", [3, 1, 2, 0])):
+        ex = FakeExecutor(k=10_000)
+        srv = Server(ex, hbm_budget=1 << 40, max_units=1, max_batch=1, admission=policy)
+        ex.server = srv
+        srv.submit(jobs)
+        srv.run(poll=0.0)
+        assert [b[0] for b in ex.batches] == want, policy
+    with pytest.raises(ValueError):
+        Server(FakeExecutor(), admission="random")

@@ -61,3 +61,32 @@ def test_budget_limits_concurrency():
     res = srv.run(until=300.0)
     assert len(res) == 6 and not srv.failed
     assert max(in_use for _, _, _, in_use in srv.queue_depth) <= 2 * one + 1
+
+
+@pytest.mark.parametrize("admission", ["fifo", "shortest"])
+def test_pool_mix_equals_alone(admission):
+    """Continuous batching of direct-sum jobs in a slot pool: more jobs than
+    slots arrive over time, finished jobs free their slots for waiting ones
+    (slots are resized in place), and every result still equals the job run
+    alone (relative L2 1e-6); Barnes-Hut jobs overlap with the pool."""
+    from physim_gb300.server import GpuExecutor, JobSpec, Server, initial_state
+    from test_verlet_gpu import trajectory_errors
+    jobs = [JobSpec(arrival=0.001 * i, id=i, n=n, steps=20 + 7 * (i % 5), seed=700 + i,
+                    ic="cube" if i % 2 else "plummer")
+            for i, n in enumerate([1200, 3000, 500, 2048, 4096, 700, 2500, 1800, 3500, 900])]
+    jobs.append(JobSpec(arrival=0.002, id=20, n=40_000, steps=12, gravity="astro2", theta=0.5,
+                        seed=720))
+    ex = GpuExecutor(tick_ms=2.0, pool_slots=4, pool_bodies=4096)
+    srv = Server(ex, hbm_budget=8 << 30, keep_states=True, admission=admission)
+    srv.submit(jobs)
+    res = srv.run(until=300.0)
+    assert not srv.failed and srv.unfinished() == 0
+    assert sorted(r.spec.id for r in res) == sorted(j.id for j in jobs)
+    for r in res:
+        alone = _alone(r.spec)
+        if r.spec.gravity == "astro2":
+            for f in ("x", "y", "z", "vx", "vy", "vz"):
+                assert r.state[f].tobytes() == alone[f].tobytes(), (r.spec.id, f)
+        else:
+            err = trajectory_errors(initial_state(r.spec), r.state, alone)
+            assert err["pos_rel_l2"] < 1e-6 and err["vel_rel_l2"] < 1e-6, (r.spec.id, err)
