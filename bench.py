@@ -61,6 +61,9 @@ def parse():
     p.add_argument("--precision-steps", type=int, default=200)
     p.add_argument("--precision-bodies", type=int, default=262_144)
     p.add_argument("--serve-seconds", type=float, default=15.0)
+    p.add_argument("--serve-admission", choices=["shortest", "fifo"], default="shortest",
+                   help="admission order of the served run (the one-at-a-time baselines run "
+                        "both orders)")
     p.add_argument("--serve-drain", type=float, default=30.0)
     p.add_argument("--ens-steps", type=int, default=200)
     p.add_argument("--ens-members", type=int, default=512)
@@ -676,7 +679,7 @@ def measure_served(args, dist: Dist, device: int) -> dict:
     until = args.serve_seconds + args.serve_drain
     jobs = served_mix(rate=50.0, seconds=args.serve_seconds, seed=5)
     served = _serve_once(jobs, GpuExecutor(device=device, tick_ms=25.0, download=True), until,
-                         admission="shortest")
+                         admission=args.serve_admission)
     plain_fifo = _serve_once(served_mix(rate=50.0, seconds=args.serve_seconds, seed=5),
                              PlainExecutor(device=device, download=True), until, max_units=1,
                              max_batch=1, admission="fifo")
@@ -686,9 +689,11 @@ def measure_served(args, dist: Dist, device: int) -> dict:
     offered_direct = sum(j.n * j.n * j.steps for j in jobs if j.gravity == "simple_astro")
     rate = served["aggregate_steps_per_s"]
     out = {"metric": "served-mix job latency (arrival to final state on the host)",
-           "admission": "shortest job first (estimated device work), HBM budget 150 GB, "
-                        "at most 64 units (one ensemble per admission round of direct-sum "
-                        "jobs, one simulation per Barnes-Hut job, each on its own stream)",
+           "admission": ("shortest job first (estimated device work)"
+                         if args.serve_admission == "shortest" else "arrival order")
+                        + ", HBM budget 150 GB, at most 64 units (one ensemble per admission "
+                          "round of direct-sum jobs, one simulation per Barnes-Hut job, each on "
+                          "its own stream)",
            "jobs_arrived": len(jobs), "arrival_seconds": args.serve_seconds,
            "drain_seconds": args.serve_drain, "offered_direct_pairs": offered_direct}
     out.update(served)
