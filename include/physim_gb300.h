@@ -265,6 +265,41 @@ int physim_gpu_sim_upload(PhysimSim *sim, const Entity *state, size_t n);
  * reference's operation order, so given the same accelerations the new state
  * is bit-identical to the reference integrator's. */
 int physim_gpu_sim_step(PhysimSim *sim, uint32_t steps);
+/* The `cube` and `plummer` initialiser elements (astro/src/initialisers.rs:15-133,
+ * :212-358) with the reference's properties, generated on the device.  The
+ * reference's uniform variates come from a ChaCha8 stream that cannot be
+ * reproduced; here variate k (0..2) of body i is the SplitMix64 finaliser of
+ * seed + (3i + k + 1) * 0x9E3779B97F4A7C15, scaled to [0, 1) with 53 bits.  Given
+ * the variates, positions, velocities, masses and radii follow the reference's
+ * formulas in f64. */
+typedef struct PhysimCubeParams {
+    uint64_t seed;     /* default 0 */
+    double spin;       /* v = (y, -x, 0) * spin, default 0 */
+    double size;       /* x, y in [-size, size), z in [0, size), default 1 */
+    double mass;       /* total mass, default 1 */
+    double centre[3];  /* default (0, 0, 0) */
+    uint64_t id;       /* default 0 */
+} PhysimCubeParams;
+
+typedef struct PhysimPlummerParams {
+    uint64_t seed;     /* default 0 */
+    double mass;       /* total mass, default 1 */
+    double a;          /* Plummer radius, default 1 */
+    double spin;       /* tangential speed factor, default 0 */
+    double centre[3];  /* default (0, 0, 0) */
+    double v[3];       /* bulk velocity, default (0, 0, 0) */
+    uint64_t id;       /* default 0 */
+} PhysimPlummerParams;
+
+/* Fill the simulation's state with n = its body count generated bodies (like
+ * physim_gpu_sim_upload: the next step is the Taylor first step). */
+int physim_gpu_sim_init_cube(PhysimSim *sim, const PhysimCubeParams *p);
+int physim_gpu_sim_init_plummer(PhysimSim *sim, const PhysimPlummerParams *p);
+/* The same bodies written to a host Entity array (generated on `device`). */
+int physim_gpu_generate_cube(const PhysimCubeParams *p, Entity *out, size_t n, int32_t device);
+int physim_gpu_generate_plummer(const PhysimPlummerParams *p, Entity *out, size_t n,
+                                int32_t device);
+
 /* Waits for the stream, then copies the current state out.  This call, sim_accelerations
  * and sim_synchronize report a Barnes-Hut traversal stack overflow
  * (PHYSIM_ERR_TREE) or a radix-sort wait that gave up (PHYSIM_ERR_TIMEOUT) raised by

@@ -81,6 +81,8 @@ def load() -> C.CDLL:
         "bh_model_keys": (None, [vp, sz, i32, vp]),
         "bh_model_build": (C.c_long, [vp, sz, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, sz]),
         "bh_model_accel": (i32, [vp, sz, i32, i32, dbl, dbl, i32, dbl, vp, sz, vp]),
+        "oracle_cube": (None, [C.c_uint64, dbl, dbl, dbl, d3, C.c_uint64, sz, vp]),
+        "oracle_plummer": (None, [C.c_uint64, dbl, dbl, dbl, d3, d3, C.c_uint64, sz, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -309,4 +311,27 @@ def bh_model_accel(state: np.ndarray, theta: float, e: float, idx: np.ndarray, n
                           1 if quad else 0, com_theta, idx.ctypes.data, len(idx),
                           out.ctypes.data) != 0:
         raise MemoryError("bh_model_accel: out of memory")
+    return out
+
+
+def cube(props: dict) -> np.ndarray:
+    """The `cube` initialiser restated (same variates as the GPU generator)."""
+    from physim_gb300.initialisers import CUBE_DEFAULTS
+    q = {**CUBE_DEFAULTS, **props}
+    ENTITY, _ = _entity_dtype()
+    out = np.zeros(int(q["n"]), dtype=ENTITY)
+    load().oracle_cube(int(q["seed"]), float(q["spin"]), float(q["size"]), float(q["mass"]),
+                       (C.c_double * 3)(*q["centre"]), int(q["id"]), len(out), out.ctypes.data)
+    return out
+
+
+def plummer(props: dict) -> np.ndarray:
+    """The `plummer` initialiser restated (same variates as the GPU generator)."""
+    from physim_gb300.initialisers import PLUMMER_DEFAULTS
+    q = {**PLUMMER_DEFAULTS, **props}
+    ENTITY, _ = _entity_dtype()
+    out = np.zeros(int(q["n"]), dtype=ENTITY)
+    load().oracle_plummer(int(q["seed"]), float(q["mass"]), float(q["a"]), float(q["spin"]),
+                          (C.c_double * 3)(*q["centre"]), (C.c_double * 3)(*q["v"]),
+                          int(q["id"]), len(out), out.ctypes.data)
     return out

@@ -21,6 +21,7 @@
  *   verlet          integrators/src/verlet.rs:24-107
  *   euler           integrators/src/euler.rs:17-49
  *   rk4             integrators/src/rk4.rs:24-178
+ *   cube, plummer   astro/src/initialisers.rs:81-106, :286-330 (own variates)
  *   pipeline step   physim-core/src/pipeline.rs:137-141,166-173
  *
  * Parity status: the reference is Rust and cannot be built here, and its own
@@ -701,4 +702,75 @@ int oracle_max_threads(void)
 #else
     return 1;
 #endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* Initialisers `cube` (astro/src/initialisers.rs:81-106, with Entity::random */
+/* physim-core/src/lib.rs:115-128) and `plummer` (initialisers.rs:286-330),  */
+/* with the uniform variates of the GPU generator (the reference's ChaCha8    */
+/* stream cannot be reproduced): variate k of body i is the SplitMix64        */
+/* finaliser of seed + (3i + k + 1) * 0x9E3779B97F4A7C15, times 2^-53.        */
+/* ------------------------------------------------------------------------ */
+static double oracle_uniform53(uint64_t seed, uint64_t i, int k)
+{
+    uint64_t z = seed + (3ull * i + (uint64_t)k + 1ull) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * 0x1.0p-53;
+}
+
+void oracle_cube(uint64_t seed, double spin, double size, double mass, const double centre[3],
+                 uint64_t id, size_t n, Entity *out)
+{
+    const double entity_mass = mass / (double)n;
+    for (size_t i = 0; i < n; ++i) {
+        Entity e;
+        memset(&e, 0, sizeof e);
+        e.x = -1.0 + 2.0 * oracle_uniform53(seed, i, 0); /* random_range(-1.0..1.0) */
+        e.y = -1.0 + 2.0 * oracle_uniform53(seed, i, 1);
+        e.z = oracle_uniform53(seed, i, 2);               /* random_range(0.0..1.0) */
+        e.radius = 0.02;
+        e.x *= size;
+        e.y *= size;
+        e.z *= size;
+        e.vx = e.y * spin;
+        e.vy = -e.x * spin;
+        e.x += centre[0];
+        e.y += centre[1];
+        e.z += centre[2];
+        e.mass = entity_mass;
+        e.id = (uintptr_t)id;
+        out[i] = e;
+    }
+}
+
+void oracle_plummer(uint64_t seed, double mass, double a, double spin, const double centre[3],
+                    const double v[3], uint64_t id, size_t n, Entity *out)
+{
+    const double PI = 3.14159265358979311600;
+    const double m = mass / (double)n;
+    for (size_t i = 0; i < n; ++i) {
+        const double c0 = oracle_uniform53(seed, i, 0);
+        const double c1 = oracle_uniform53(seed, i, 1);
+        const double c2 = oracle_uniform53(seed, i, 2);
+        const double r = a * sqrt(pow(c0, -2.0 / 3.0) - 1.0);
+        const double theta = PI * c2;
+        const double phi = 2.0 * PI * c1;
+        Entity e;
+        memset(&e, 0, sizeof e);
+        e.x = r * sin(theta) * cos(phi) + centre[0];
+        e.y = r * sin(theta) * sin(phi) + centre[1];
+        e.z = r * cos(theta) + centre[2];
+        e.mass = m;
+        e.radius = 0.01; /* Entity::new2(x, y, z, m, 0.01) */
+        const double r2 = r * r;
+        const double a2 = a * a;
+        const double v_phi = spin * sqrt(mass * r2 / pow(r2 + a2, 1.5));
+        e.vx = -v_phi * sin(phi) + v[0];
+        e.vy = v_phi * cos(phi) + v[1];
+        e.vz = 0.0 + v[2];
+        e.id = (uintptr_t)id;
+        out[i] = e;
+    }
 }

@@ -85,6 +85,17 @@ class PhysimDiagnostics(C.Structure):
                 ("energy", C.c_double)]
 
 
+class PhysimCubeParams(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("spin", C.c_double), ("size", C.c_double),
+                ("mass", C.c_double), ("centre", C.c_double * 3), ("id", C.c_uint64)]
+
+
+class PhysimPlummerParams(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("mass", C.c_double), ("a", C.c_double),
+                ("spin", C.c_double), ("centre", C.c_double * 3), ("v", C.c_double * 3),
+                ("id", C.c_uint64)]
+
+
 class PhysimDirectTuning(C.Structure):
     _fields_ = [("block", C.c_uint32), ("ipt", C.c_uint32), ("splits", C.c_uint32),
                 ("candidates", C.c_uint32), ("force_ms", C.c_double)]
@@ -127,6 +138,10 @@ def _load() -> C.CDLL:
         "physim_gpu_sim_diagnostics": (C.c_int, [vp, C.POINTER(PhysimDiagnostics), C.c_int]),
         "physim_gpu_sim_tree_snapshot": (C.c_int, [vp, C.POINTER(PhysimTreeSnapshot)]),
         "physim_gpu_sim_autotune": (C.c_int, [vp, C.POINTER(PhysimDirectTuning)]),
+        "physim_gpu_sim_init_cube": (C.c_int, [vp, C.POINTER(PhysimCubeParams)]),
+        "physim_gpu_sim_init_plummer": (C.c_int, [vp, C.POINTER(PhysimPlummerParams)]),
+        "physim_gpu_generate_cube": (C.c_int, [C.POINTER(PhysimCubeParams), vp, sz, i32]),
+        "physim_gpu_generate_plummer": (C.c_int, [C.POINTER(PhysimPlummerParams), vp, sz, i32]),
         "physim_gpu_sim_bh_stats": (C.c_int, [vp, C.POINTER(C.c_uint64),
                                               C.POINTER(C.c_uint64), C.POINTER(dbl)]),
         "physim_gpu_ensemble_create": (C.c_int, [C.POINTER(PhysimSimConfig), vp, sz,

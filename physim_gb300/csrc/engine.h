@@ -127,6 +127,10 @@ int launch_verlet_aos(const Entity *d_in, const Entity *d_prev, Entity *d_out,
 int launch_diagnostics(const DeviceBodies &b, double e, double *d_out, bool potential,
                        int device, cudaStream_t stream);
 
+// The cube (kind 0, PhysimCubeParams) or plummer (kind 1, PhysimPlummerParams)
+// initialiser written as n Entities to d_out (init.cu).
+int launch_generate(int kind, const void *params, Entity *d_out, size_t n, cudaStream_t stream);
+
 // Device count / SM count helpers (cached).
 int device_sm_count(int device);
 

@@ -225,6 +225,44 @@ int physim_gpu_sim_upload(PhysimSim *s, const Entity *state, size_t n)
 
 namespace {
 
+int sim_generate(PhysimSim *s, int kind, const void *params)
+{
+    PG_CHECK(s && params, PHYSIM_ERR_ARGUMENT, "null argument");
+    PG_CUDA(cudaSetDevice(s->cfg.device));
+    if (s->n) {
+        PG_TRY(launch_generate(kind, params, s->b.aos, s->n, s->stream));
+        PG_TRY(launch_unpack(s->b, s->b.aos, s->n, true, s->stream));
+    }
+    s->history = false;
+    s->uploaded = true;
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    return PHYSIM_OK;
+}
+
+int generate_host(int kind, const void *params, Entity *out, size_t n, int32_t device)
+{
+    PG_CHECK(params && (out || n == 0), PHYSIM_ERR_ARGUMENT, "null argument");
+    if (n == 0) return PHYSIM_OK;
+    PG_CUDA(cudaSetDevice(device));
+    cudaStream_t st;
+    PG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    Entity *d = nullptr;
+    int rc = dev_alloc(d, n, st);
+    if (rc == PHYSIM_OK) rc = launch_generate(kind, params, d, n, st);
+    if (rc == PHYSIM_OK &&
+        cudaMemcpyAsync(out, d, n * sizeof(Entity), cudaMemcpyDeviceToHost, st) != cudaSuccess) {
+        set_error("copy of generated bodies failed");
+        rc = PHYSIM_ERR_CUDA;
+    }
+    dev_free(d, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess && rc == PHYSIM_OK) {
+        set_error("generation failed");
+        rc = PHYSIM_ERR_CUDA;
+    }
+    cudaStreamDestroy(st);
+    return rc;
+}
+
 // The gravity phase of one force evaluation: the captured graph, or the
 // kernels themselves when the stream cannot be captured.
 int sim_gravity(PhysimSim *s, int *splits)
@@ -239,6 +277,27 @@ int sim_gravity(PhysimSim *s, int *splits)
 }
 
 }  // namespace
+
+int physim_gpu_sim_init_cube(PhysimSim *s, const PhysimCubeParams *p)
+{
+    return sim_generate(s, 0, p);
+}
+
+int physim_gpu_sim_init_plummer(PhysimSim *s, const PhysimPlummerParams *p)
+{
+    return sim_generate(s, 1, p);
+}
+
+int physim_gpu_generate_cube(const PhysimCubeParams *p, Entity *out, size_t n, int32_t device)
+{
+    return generate_host(0, p, out, n, device);
+}
+
+int physim_gpu_generate_plummer(const PhysimPlummerParams *p, Entity *out, size_t n,
+                                int32_t device)
+{
+    return generate_host(1, p, out, n, device);
+}
 
 int physim_gpu_sim_step(PhysimSim *s, uint32_t steps)
 {

@@ -64,6 +64,42 @@ class Simulation:
         self.handle = h
         self.upload(state)
 
+    @classmethod
+    def generated(cls, kind: str, props: dict, config: SimConfig) -> "Simulation":
+        """A simulation whose bodies are generated on the device by the `cube`
+        or `plummer` initialiser (physim_gb300.initialisers) -- no host-side
+        generation or upload."""
+        from . import initialisers
+        n, p = (initialisers.cube_params(props) if kind == "cube"
+                else initialisers.plummer_params(props))
+        self = cls.__new__(cls)
+        self.n = n
+        self.config = config
+        h = C.c_void_p()
+        cfg = config.to_c()
+        check(lib.physim_gpu_sim_create(C.byref(cfg), n, C.byref(h)), "physim_gpu_sim_create")
+        self.handle = h
+        fn = lib.physim_gpu_sim_init_cube if kind == "cube" else lib.physim_gpu_sim_init_plummer
+        check(fn(self.handle, C.byref(p)), "physim_gpu_sim_init_" + kind)
+        return self
+
+    def run(self, steps: int, sink=None) -> None:
+        """Advances `steps` steps, handing the state to `sink.render` before
+        the first step and after every sink.print_n-th step (the states a
+        physim renderer receives, pipeline.rs:130-181)."""
+        if sink is None:
+            self.step(steps)
+            return
+        sink.render(self.download())
+        every = max(1, int(sink.print_n))
+        done = 0
+        while done < steps:
+            k = min(every, steps - done)
+            self.step(k)
+            done += k
+            if done % every == 0:
+                sink.render(self.download(), iteration=done)
+
     def upload(self, state: np.ndarray) -> None:
         state = as_entities(state)
         check(lib.physim_gpu_sim_upload(self.handle, state.ctypes.data, len(state)),
