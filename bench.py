@@ -9,7 +9,10 @@ N(N-1) pair interactions plus the f64 kick-drift.  Prints one JSON line.
             flushed between timed steps).
   e2e       the same metric through the plugin C ABI with host Entity arrays:
             simple_astro_transform + physim_gpu_verlet_integrate per step,
-            host<->device copies inside the timed region (wall clock).
+            host<->device transfers inside the timed region (wall clock).  On a
+            device that reaches pageable host memory (Grace over NVLink-C2C)
+            the kernels read and write the host arrays in place ("transfer":
+            "direct"); value_with_copies is the same run with cudaMemcpyAsync.
   roofline  the pair kernel against the FP32 peak: 20 flop per pair
             (Nyland, Harris & Prins, GPU Gems 3 ch. 31) / event time, peak =
             SMs x 128 FP32 lanes x 2 x max SM clock.
@@ -260,6 +263,33 @@ def _device_context(dist: Dist):
     return device, props.multi_processor_count
 
 
+def host_array_steps(pg, element, props, state, steps, device, mode):
+    """Wall-clock seconds of `steps` plugin pipeline steps on host Entity
+    arrays with host access `mode`, the transfers inside the timed region;
+    returns (seconds, the mode the calls used).  Each step is physim's
+    pipeline step (pipeline.rs:137-173, verlet.rs:85-106): fresh zeroed
+    accelerations, the element's transform into them, the verlet update into
+    the reused new_state array, which becomes the next state."""
+    pg.set_host_access(mode)
+    used = pg.host_access(device)
+    el = pg.TransformElementHandler(element, props)
+    verlet = pg.GpuVerlet(device)
+    cur = state.copy()
+    nxt = np.empty_like(cur)
+    el.transform(cur, pg.accelerations(len(cur)))  # warm: allocations, module load
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        acc = np.zeros(len(cur), dtype=pg.ACCELERATION)
+        el.transform(cur, acc)
+        verlet.integrate(cur, acc, DT, out=nxt)
+        cur, nxt = nxt, cur
+    seconds = time.perf_counter() - t0
+    el.destroy()
+    verlet.close()
+    pg.set_host_access("auto")
+    return seconds, used
+
+
 def _timed_steps(sim, stream, steps: int, flush) -> tuple[list[float], list[float]]:
     """Per-step CUDA-event times on the simulation's stream, L2 flushed between
     steps outside the events.  Returns (step ms, gravity-kernel ms)."""
@@ -338,24 +368,15 @@ def measure_direct(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict
 
     if not args.skip_e2e:
         e2e_steps = args.e2e_steps or max(2, min(args.steps, 3))
-        el = pg.TransformElementHandler("simple_astro", {"e": E, "device": device})
-        verlet = pg.GpuVerlet(device)
-        cur = state.copy()
-        el.transform(cur, pg.accelerations(n))  # warm: allocations, module load
-        times = []
-        for _ in range(e2e_steps):
-            t0 = time.perf_counter()
-            acc = np.zeros(n, dtype=pg.ACCELERATION)
-            el.transform(cur, acc)
-            cur = verlet.integrate(cur, acc, DT)
-            times.append(time.perf_counter() - t0)
-        el.destroy()
-        verlet.close()
-        t_e2e = dist.max(sum(times))
-        out["e2e"] = {"value": dist.sum(float(pairs_step * e2e_steps)) / t_e2e / 1e9,
-                      "unit": "Gpair-interactions/s",
+        props = {"e": E, "device": device}
+        runs = {m: host_array_steps(pg, "simple_astro", props, state, e2e_steps, device, m)
+                for m in ("copy", "auto")}
+        rate = {m: dist.sum(float(pairs_step * e2e_steps)) / dist.max(t) / 1e9
+                for m, (t, _) in runs.items()}
+        out["e2e"] = {"value": rate["auto"], "unit": "Gpair-interactions/s",
                       "h2d_bytes_per_step": n * (80 + 24) + n * (80 + 24),
                       "d2h_bytes_per_step": n * 24 + n * 80, "steps": e2e_steps,
+                      "transfer": runs["auto"][1], "value_with_copies": rate["copy"],
                       "path": "simple_astro_transform + physim_gpu_verlet_integrate on host "
                               "Entity arrays (pipeline.rs:137-173)"}
     if dist.rank == 0 and not args.no_cpu_baseline:
@@ -478,24 +499,14 @@ def measure_bh(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict:
                                   "flop_per_interaction": FLOP_PER_PAIR,
                                   "kernel_ms": trav_ms}}
     if not args.skip_e2e:
-        el = pg.TransformElementHandler("astro2", {"theta": 0.5, "e": E, "leaf_size": 16,
-                                                   "traversal": "warp", "device": device})
-        verlet = pg.GpuVerlet(device)
-        cur = state.copy()
-        el.transform(cur, pg.accelerations(n))
-        times = []
-        for _ in range(args.bh_e2e_steps):
-            t0 = time.perf_counter()
-            acc = np.zeros(n, dtype=pg.ACCELERATION)
-            el.transform(cur, acc)
-            cur = verlet.integrate(cur, acc, DT)
-            times.append(time.perf_counter() - t0)
-        el.destroy()
-        verlet.close()
-        t_e2e = dist.max(sum(times))
-        out["e2e"] = {"value": dist.sum(float(args.bh_e2e_steps)) / t_e2e, "unit": "steps/s",
+        props = {"theta": 0.5, "e": E, "leaf_size": 16, "traversal": "warp", "device": device}
+        runs = {m: host_array_steps(pg, "astro2", props, state, args.bh_e2e_steps, device, m)
+                for m in ("copy", "auto")}
+        rate = {m: dist.sum(float(args.bh_e2e_steps)) / dist.max(t) for m, (t, _) in runs.items()}
+        out["e2e"] = {"value": rate["auto"], "unit": "steps/s",
                       "h2d_bytes_per_step": n * (80 + 24) * 2, "d2h_bytes_per_step": n * 104,
-                      "steps": args.bh_e2e_steps,
+                      "steps": args.bh_e2e_steps, "transfer": runs["auto"][1],
+                      "value_with_copies": rate["copy"],
                       "path": "astro2_transform (leaf_size 16, warp) + physim_gpu_verlet_integrate "
                               "on host Entity arrays"}
     if dist.rank == 0 and not args.no_cpu_baseline:

@@ -202,6 +202,27 @@ enum {
 /* Message for the last failing call on this thread ("" if none). */
 const char *physim_gpu_last_error(void);
 
+/* How the calls that take the caller's host arrays (the elements' transform
+ * calls, physim_gpu_verlet_integrate) move them to and from the GPU.
+ *   COPY:   cudaMemcpyAsync into device buffers and back.
+ *   DIRECT: the kernels read and write the caller's arrays where they are,
+ *           in contiguous block-wide runs.  Needs a device that reaches
+ *           pageable host memory through the host's page tables
+ *           (cudaDevAttrPageableMemoryAccessUsesHostPageTables: a Grace-
+ *           Blackwell GPU over NVLink-C2C); a call on another device then
+ *           fails with PHYSIM_ERR_ARGUMENT.
+ *   AUTO:   DIRECT where the device supports it, else COPY (the default).
+ * Results are bit-identical in every mode.  The setting is process-wide and
+ * read at the start of each call. */
+typedef enum PhysimHostAccess {
+    PHYSIM_HOST_ACCESS_AUTO = 0,
+    PHYSIM_HOST_ACCESS_COPY = 1,
+    PHYSIM_HOST_ACCESS_DIRECT = 2
+} PhysimHostAccess;
+int physim_gpu_set_host_access(uint32_t mode);
+/* The mode that calls on `device` use now: COPY or DIRECT. */
+int physim_gpu_host_access(int32_t device, uint32_t *mode);
+
 /* Gravity elements, by the reference's element names. */
 typedef enum PhysimGravity {
     PHYSIM_GRAVITY_SIMPLE_ASTRO = 0, /* direct sum, transformers.rs:205-271 */

@@ -7,7 +7,7 @@ transform-element handler and pipeline step, device-resident simulations and
 seeded initial conditions.  Importing it loads the CUDA library and fails
 loudly if the library is missing; there is no CPU fallback.
 """
-from ._lib import LIB_PATH, PhysimError, last_error, lib
+from ._lib import LIB_PATH, PhysimError, host_access, last_error, lib, set_host_access
 from .entity import ACCELERATION, ENTITY, accelerations, entities, entity_new
 from .plugin import (GpuIntegrator, GpuVerlet, NullElement, Pipeline, TransformElementHandler,
                      register)
@@ -17,5 +17,6 @@ from .ensemble import Ensemble
 __all__ = [
     "LIB_PATH", "PhysimError", "last_error", "lib", "ACCELERATION", "ENTITY", "accelerations",
     "entities", "entity_new", "GpuIntegrator", "GpuVerlet", "NullElement", "Pipeline",
-    "TransformElementHandler", "register", "SimConfig", "Simulation", "Ensemble",
+    "TransformElementHandler", "register", "SimConfig", "Simulation", "Ensemble", "host_access",
+    "set_host_access",
 ]

@@ -29,6 +29,7 @@ INTEGRATOR_EULER = 1
 INTEGRATOR_RK4 = 2
 MULTIPOLE_MONOPOLE = 0
 MULTIPOLE_QUADRUPOLE = 1
+HOST_ACCESS = {"auto": 0, "copy": 1, "direct": 2}
 
 
 class CMessage(C.Structure):
@@ -123,6 +124,8 @@ def _load() -> C.CDLL:
         "register_plugin": (C.c_char_p, []),
         "set_callback_target": (None, [vp]),
         "physim_gpu_last_error": (C.c_char_p, []),
+        "physim_gpu_set_host_access": (C.c_int, [u32]),
+        "physim_gpu_host_access": (C.c_int, [i32, C.POINTER(u32)]),
         "physim_gpu_sim_config_default": (None, [C.POINTER(PhysimSimConfig)]),
         "physim_gpu_sim_create": (C.c_int, [C.POINTER(PhysimSimConfig), sz, C.POINTER(vp)]),
         "physim_gpu_sim_upload": (C.c_int, [vp, vp, sz]),
@@ -199,3 +202,17 @@ def last_error() -> str:
 def check(code: int, what: str) -> None:
     if code != PHYSIM_OK:
         raise PhysimError(code, what)
+
+
+def set_host_access(mode: str) -> None:
+    """How calls taking host arrays move them: "copy" (cudaMemcpyAsync),
+    "direct" (kernels read and write the host arrays in place over the
+    device's pageable-memory access) or "auto" (direct where supported)."""
+    check(lib.physim_gpu_set_host_access(HOST_ACCESS[mode]), "physim_gpu_set_host_access")
+
+
+def host_access(device: int = 0) -> str:
+    """The mode calls on `device` use now: "copy" or "direct"."""
+    out = C.c_uint32(0)
+    check(lib.physim_gpu_host_access(device, C.byref(out)), "physim_gpu_host_access")
+    return {1: "copy", 2: "direct"}[out.value]

@@ -2,10 +2,12 @@
 // host Entity array in, `acc[i] += a_i` out (astro/src/transformers.rs:122-160
 // for astro2, :31-69 for astro, :219-244 for simple_astro).
 //
-// Per call: the Entity array (80 B/body) and the caller's accelerations
-// (24 B/body) are copied to the device, unpacked to f32 (x,y,z,m) + f64
-// state, the gravity kernels run, the accelerations are added on the device
-// in f64 and copied back.  Fixed bodies keep their incoming value untouched.
+// Per call: the Entity array (80 B/body) is unpacked to f32 (x,y,z,m) + f64
+// state, the gravity kernels run, and the accelerations (24 B/body) are added
+// to the caller's in f64.  With host access DIRECT the unpack and accumulate
+// kernels read and write the caller's host arrays in place; with COPY both
+// arrays are copied to the device first and the accelerations copied back.
+// Fixed bodies keep their incoming value untouched.
 #include "common.cuh"
 #include "engine.h"
 #include "plugin_state.h"
@@ -34,17 +36,30 @@ static int accumulate_locked(ElementState *el, const Entity *state, size_t n, Ac
     }
     cudaStream_t st = el->stream;
     const bool tree = el->kind != 0;
+    bool direct = false;
+    PG_TRY(host_direct(el->device, &direct));
     PG_TRY(bodies_reserve(el->bodies, n, tree, st));
-    if (el->acc_cap < n) {
-        dev_free(el->d_acc, st);
-        el->d_acc = nullptr;
-        el->acc_cap = 0;
-        PG_TRY(dev_alloc(el->d_acc, n, st));
-        el->acc_cap = n;
+    Acceleration *acc_io = acc;  // DIRECT: the kernels read and write the caller's array
+    const Entity *state_in = state;
+    if (direct) {
+        host_prefault(state, n * sizeof(Entity), false);
+        host_prefault(acc, n * sizeof(Acceleration), true);
+    } else {
+        if (el->acc_cap < n) {
+            dev_free(el->d_acc, st);
+            el->d_acc = nullptr;
+            el->acc_cap = 0;
+            PG_TRY(dev_alloc(el->d_acc, n, st));
+            el->acc_cap = n;
+        }
+        PG_CUDA(cudaMemcpyAsync(el->bodies.aos, state, n * sizeof(Entity), cudaMemcpyHostToDevice,
+                                st));
+        PG_CUDA(cudaMemcpyAsync(el->d_acc, acc, n * sizeof(Acceleration), cudaMemcpyHostToDevice,
+                                st));
+        acc_io = el->d_acc;
+        state_in = el->bodies.aos;
     }
-    PG_CUDA(cudaMemcpyAsync(el->bodies.aos, state, n * sizeof(Entity), cudaMemcpyHostToDevice, st));
-    PG_CUDA(cudaMemcpyAsync(el->d_acc, acc, n * sizeof(Acceleration), cudaMemcpyHostToDevice, st));
-    PG_TRY(launch_unpack(el->bodies, el->bodies.aos, n, tree, st));
+    PG_TRY(launch_unpack(el->bodies, state_in, n, tree, st));
     int splits = 1;
     if (!tree) {
         if (el->plan_n != (int)n) {
@@ -67,8 +82,10 @@ static int accumulate_locked(ElementState *el, const Entity *state, size_t n, Ac
         p.com_theta = el->com_theta;
         PG_TRY(bh_accelerations(el->bh, el->bodies, p, el->partial, st));
     }
-    PG_TRY(launch_accumulate_aos(el->bodies, el->partial, splits, el->d_acc, st));
-    PG_CUDA(cudaMemcpyAsync(acc, el->d_acc, n * sizeof(Acceleration), cudaMemcpyDeviceToHost, st));
+    PG_TRY(launch_accumulate_aos(el->bodies, el->partial, splits, acc_io, st));
+    if (!direct)
+        PG_CUDA(cudaMemcpyAsync(acc, el->d_acc, n * sizeof(Acceleration), cudaMemcpyDeviceToHost,
+                                st));
     PG_CUDA(cudaStreamSynchronize(st));
     if (tree) PG_TRY(bh_check(el->bh, st));
     return PHYSIM_OK;

@@ -83,8 +83,24 @@ inline int dev_alloc(T *&p, size_t count, cudaStream_t stream)
 int bodies_reserve(DeviceBodies &b, size_t n, bool with_state, cudaStream_t stream);
 void bodies_free(DeviceBodies &b, cudaStream_t stream);
 
-// Unpacks an Entity array already on the device into the SoA arrays.
-int launch_unpack(DeviceBodies &b, const Entity *d_aos, size_t n, bool full_state,
+// True when calls on `device` hand the caller's host arrays to the kernels
+// in place (PHYSIM_HOST_ACCESS_DIRECT, or AUTO on a device with pageable
+// memory access through the host's page tables); false when they copy.
+// Fails if DIRECT is requested on a device that cannot.
+int host_direct(int device, bool *direct);
+// Before kernels touch a host array in place: maps every page of
+// [p, p + bytes) into the process (writable if `write`), without changing its
+// contents, so the GPU meets no page that was never touched.  A GPU access to
+// such a page (a freshly mmap'd output array) is a fault the host's kernel
+// serves one page at a time, an order of magnitude slower than the same
+// fault taken on the CPU.  Best effort: a range the host's kernel will not
+// populate (not host memory, an older kernel) is left to the GPU's faults.
+void host_prefault(const void *p, size_t bytes, bool write);
+
+// Unpacks an Entity array into the SoA arrays.  `aos` may be device memory
+// or, where host_direct() holds, the caller's host array: each block reads
+// its 256 entities as one contiguous run.
+int launch_unpack(DeviceBodies &b, const Entity *aos, size_t n, bool full_state,
                   cudaStream_t stream);
 // Packs the SoA state back into b.aos.
 int launch_pack(DeviceBodies &b, cudaStream_t stream);
@@ -117,9 +133,12 @@ int launch_rk4_aos_stage(const Entity *d_ent, const Entity *d_q, const Accelerat
                          double *ksum, Entity *d_out, size_t n, double dt, int stage,
                          cudaStream_t stream);
 
-// Verlet over explicit device arrays (the host-array integrator path).
-int launch_verlet_aos(const Entity *d_in, const Entity *d_prev, Entity *d_out,
-                      const Acceleration *d_acc, size_t n, double dt, bool initial,
+// Verlet over explicit Entity arrays (the host-array integrator path).  in,
+// out and acc may be host arrays where host_direct() holds; prev and keep
+// are device memory.  keep (optional) receives a copy of in, the next
+// call's previous state.
+int launch_verlet_aos(const Entity *in, const Entity *d_prev, Entity *out, Entity *keep,
+                      const Acceleration *acc, size_t n, double dt, bool initial,
                       cudaStream_t stream);
 
 // Whole-system f64 diagnostics into d_out[0..8]: mass, m*x, m*y, m*z,

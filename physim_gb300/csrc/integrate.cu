@@ -9,6 +9,18 @@
 // The same kernel combines the pair kernel's partial sums, so one launch
 // does combine + kick + drift + refresh of the f32 body copy.
 #include <string.h>
+#include <sys/mman.h>
+#include <unistd.h>
+
+#include <atomic>
+
+// madvise advice values of Linux 5.14+ (absent from older headers)
+#ifndef MADV_POPULATE_READ
+#define MADV_POPULATE_READ 22
+#endif
+#ifndef MADV_POPULATE_WRITE
+#define MADV_POPULATE_WRITE 23
+#endif
 
 #include "common.cuh"
 #include "engine.h"
@@ -21,17 +33,41 @@ constexpr int kThreads = 256;
 
 inline int blocks_for(size_t n) { return (int)((n + kThreads - 1) / kThreads); }
 
+// Copies `bytes` (a multiple of 8) between global memory -- HBM, or the
+// caller's host array reached through the host's page tables -- and shared
+// memory with every thread of the block, as consecutive 16-byte words when
+// both ends are 16-byte aligned, else 8-byte words.  An array of structs read
+// one struct per thread touches a 32-byte sector per 8-byte field; this moves
+// whole runs instead, which is what a link to host memory needs.
+__device__ __forceinline__ void block_copy(void *dst, const void *src, int bytes)
+{
+    if (((((uintptr_t)dst | (uintptr_t)src) & 15) == 0) && (bytes & 15) == 0) {
+        const int4 *s = (const int4 *)src;
+        int4 *d = (int4 *)dst;
+        for (int w = threadIdx.x; w < bytes / 16; w += blockDim.x) d[w] = s[w];
+    } else {
+        const long long *s = (const long long *)src;
+        long long *d = (long long *)dst;
+        for (int w = threadIdx.x; w < bytes / 8; w += blockDim.x) d[w] = s[w];
+    }
+}
+
 __global__ void unpack_kernel(const Entity *__restrict__ in, int n, int n_pad, float4 *body4,
                               uint8_t *fixed, double *x, double *y, double *z, double *vx,
                               double *vy, double *vz, double *m, double *radius, uint64_t *id)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ __align__(16) Entity s_in[kThreads];
+    const int base = blockIdx.x * kThreads;
+    const int count = min(kThreads, n - base);  // <= 0 for blocks of the padded tail
+    if (count > 0) block_copy(s_in, in + base, count * (int)sizeof(Entity));
+    __syncthreads();
+    const int i = base + threadIdx.x;
     if (i >= n_pad) return;
     if (i >= n) {
         body4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
-    const Entity en = in[i];
+    const Entity en = s_in[threadIdx.x];
     body4[i] = make_float4((float)en.x, (float)en.y, (float)en.z, (float)en.mass);
     fixed[i] = en.fixed ? 1 : 0;
     m[i] = en.mass;
@@ -85,20 +121,30 @@ __device__ __forceinline__ void body_acc(const double *partial, int splits, int 
     if (mass == 0.0) ax = ay = az = __longlong_as_double(0x7ff8000000000000LL);
 }
 
+// The block's accelerations are read and written back as one contiguous run;
+// a fixed body's entry is written back with the bits it was read with.
 __global__ void accumulate_aos_kernel(const double *__restrict__ mass, const uint8_t *fixed,
                                       const double *partial, int splits, int n,
                                       Acceleration *acc)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (fixed[i]) return;  // transformers.rs:139-141: fixed bodies are left untouched
-    double ax, ay, az;
-    body_acc(partial, splits, n, i, false, mass[i], ax, ay, az);
-    Acceleration a = acc[i];
-    a.x = __dadd_rn(a.x, ax);
-    a.y = __dadd_rn(a.y, ay);
-    a.z = __dadd_rn(a.z, az);
-    acc[i] = a;
+    __shared__ __align__(16) Acceleration s_acc[kThreads];
+    const int base = blockIdx.x * kThreads;
+    const int count = min(kThreads, n - base);
+    block_copy(s_acc, acc + base, count * (int)sizeof(Acceleration));
+    __syncthreads();
+    const int i = base + threadIdx.x;
+    // transformers.rs:139-141: fixed bodies are left untouched
+    if (i < n && !fixed[i]) {
+        double ax, ay, az;
+        body_acc(partial, splits, n, i, false, mass[i], ax, ay, az);
+        Acceleration a = s_acc[threadIdx.x];
+        a.x = __dadd_rn(a.x, ax);
+        a.y = __dadd_rn(a.y, ay);
+        a.z = __dadd_rn(a.z, az);
+        s_acc[threadIdx.x] = a;
+    }
+    __syncthreads();
+    block_copy(acc + base, s_acc, count * (int)sizeof(Acceleration));
 }
 
 __global__ void combine_soa_kernel(const double *__restrict__ mass, const uint8_t *fixed,
@@ -159,24 +205,53 @@ __global__ void verlet_kernel(float4 *body4, const double *mass, const uint8_t *
     body4[i] = b;
 }
 
-__global__ void verlet_aos_kernel(const Entity *in, const Entity *prev, Entity *out,
+__global__ void verlet_aos_kernel(const Entity *in, const Entity *prev, Entity *out, Entity *keep,
                                   const Acceleration *acc, int n, double dt, int initial)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    Entity en = in[i];
-    const Acceleration a = acc[i];
-    const double dt2 = __dmul_rn(dt, dt);
-    double px = 0.0, py = 0.0, pz = 0.0;
-    if (!initial) {
-        px = prev[i].x;
-        py = prev[i].y;
-        pz = prev[i].z;
+    __shared__ __align__(16) Entity s_e[kThreads];
+    __shared__ __align__(16) Acceleration s_a[kThreads];
+    const int base = blockIdx.x * kThreads;
+    const int count = min(kThreads, n - base);
+    block_copy(s_e, in + base, count * (int)sizeof(Entity));
+    block_copy(s_a, acc + base, count * (int)sizeof(Acceleration));
+    __syncthreads();
+    if (keep) block_copy(keep + base, s_e, count * (int)sizeof(Entity));
+    const int i = base + threadIdx.x;
+    double x = 0.0, y = 0.0, z = 0.0, vx = 0.0, vy = 0.0, vz = 0.0;
+    if (i < n) {
+        const Entity &en = s_e[threadIdx.x];
+        x = en.x;
+        y = en.y;
+        z = en.z;
+        vx = en.vx;
+        vy = en.vy;
+        vz = en.vz;
+        const Acceleration a = s_a[threadIdx.x];
+        const double dt2 = __dmul_rn(dt, dt);
+        double px = 0.0, py = 0.0, pz = 0.0;
+        if (!initial) {
+            px = prev[i].x;
+            py = prev[i].y;
+            pz = prev[i].z;
+        }
+        verlet_axis(x, vx, px, a.x, dt, dt2, initial);
+        verlet_axis(y, vy, py, a.y, dt, dt2, initial);
+        verlet_axis(z, vz, pz, a.z, dt, dt2, initial);
     }
-    verlet_axis(en.x, en.vx, px, a.x, dt, dt2, initial);
-    verlet_axis(en.y, en.vy, py, a.y, dt, dt2, initial);
-    verlet_axis(en.z, en.vz, pz, a.z, dt, dt2, initial);
-    out[i] = en;
+    __syncthreads();  // every read of s_e (the keep copy) is done
+    // Only the six updated fields are rewritten: every other byte of the
+    // output record, struct padding included, is the input's.
+    if (i < n) {
+        Entity &en = s_e[threadIdx.x];
+        en.x = x;
+        en.y = y;
+        en.z = z;
+        en.vx = vx;
+        en.vy = vy;
+        en.vz = vz;
+    }
+    __syncthreads();
+    block_copy(out + base, s_e, count * (int)sizeof(Entity));
 }
 
 // euler.rs:29-37: x + vx*dt + 0.5*a*dt^2 ; vx + a*dt for every body.  A fixed
@@ -358,6 +433,34 @@ void dev_free(void *p, cudaStream_t stream)
     if (p) cudaFreeAsync(p, stream);
 }
 
+namespace {
+std::atomic<uint32_t> g_host_access{PHYSIM_HOST_ACCESS_AUTO};
+std::atomic<int> g_pageable[64];  // 0 unknown, 1 no, 2 yes
+}  // namespace
+
+int host_direct(int device, bool *direct)
+{
+    *direct = false;
+    const uint32_t mode = g_host_access.load(std::memory_order_relaxed);
+    if (mode == PHYSIM_HOST_ACCESS_COPY) return PHYSIM_OK;
+    PG_CHECK(device >= 0 && device < 64, PHYSIM_ERR_ARGUMENT, "device %d out of range", device);
+    int known = g_pageable[device].load(std::memory_order_relaxed);
+    if (known == 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                                   device) != cudaSuccess)
+            v = 0;
+        known = v ? 2 : 1;
+        g_pageable[device].store(known, std::memory_order_relaxed);
+    }
+    PG_CHECK(known == 2 || mode == PHYSIM_HOST_ACCESS_AUTO, PHYSIM_ERR_ARGUMENT,
+             "host access DIRECT: device %d does not reach pageable host memory through the "
+             "host's page tables",
+             device);
+    *direct = known == 2;
+    return PHYSIM_OK;
+}
+
 void bodies_free(DeviceBodies &b, cudaStream_t stream)
 {
     void *ptrs[] = {b.body4, b.fixed, b.x,  b.y,  b.z,      b.vx, b.vy,
@@ -388,13 +491,13 @@ int bodies_reserve(DeviceBodies &b, size_t n, bool with_state, cudaStream_t stre
     return PHYSIM_OK;
 }
 
-int launch_unpack(DeviceBodies &b, const Entity *d_aos, size_t n, bool full_state,
+int launch_unpack(DeviceBodies &b, const Entity *aos, size_t n, bool full_state,
                   cudaStream_t stream)
 {
     size_t n_pad = pad_bodies(n);
     if (n_pad == 0) return PHYSIM_OK;
     unpack_kernel<<<blocks_for(n_pad), kThreads, 0, stream>>>(
-        d_aos, (int)n, (int)n_pad, b.body4, b.fixed, full_state ? b.x : nullptr, b.y, b.z, b.vx,
+        aos, (int)n, (int)n_pad, b.body4, b.fixed, full_state ? b.x : nullptr, b.y, b.z, b.vx,
         b.vy, b.vz, b.m, b.radius, b.id);
     PG_CUDA(cudaGetLastError());
     return PHYSIM_OK;
@@ -485,15 +588,41 @@ int launch_rk4_aos_stage(const Entity *d_ent, const Entity *d_q, const Accelerat
     return PHYSIM_OK;
 }
 
-int launch_verlet_aos(const Entity *d_in, const Entity *d_prev, Entity *d_out,
-                      const Acceleration *d_acc, size_t n, double dt, bool initial,
+int launch_verlet_aos(const Entity *in, const Entity *d_prev, Entity *out, Entity *keep,
+                      const Acceleration *acc, size_t n, double dt, bool initial,
                       cudaStream_t stream)
 {
     if (n == 0) return PHYSIM_OK;
-    verlet_aos_kernel<<<blocks_for(n), kThreads, 0, stream>>>(d_in, d_prev, d_out, d_acc, (int)n,
+    verlet_aos_kernel<<<blocks_for(n), kThreads, 0, stream>>>(in, d_prev, out, keep, acc, (int)n,
                                                               dt, initial ? 1 : 0);
     PG_CUDA(cudaGetLastError());
     return PHYSIM_OK;
 }
 
 }  // namespace pg
+
+void pg::host_prefault(const void *p, size_t bytes, bool write)
+{
+    if (!p || !bytes) return;
+    static const uintptr_t page = (uintptr_t)sysconf(_SC_PAGESIZE);
+    const uintptr_t lo = (uintptr_t)p & ~(page - 1);
+    const uintptr_t hi = ((uintptr_t)p + bytes + page - 1) & ~(page - 1);
+    (void)madvise((void *)lo, hi - lo, write ? MADV_POPULATE_WRITE : MADV_POPULATE_READ);
+}
+
+extern "C" int physim_gpu_set_host_access(uint32_t mode)
+{
+    PG_CHECK(mode <= PHYSIM_HOST_ACCESS_DIRECT, PHYSIM_ERR_ARGUMENT, "unknown host access mode %u",
+             mode);
+    pg::g_host_access.store(mode);
+    return PHYSIM_OK;
+}
+
+extern "C" int physim_gpu_host_access(int32_t device, uint32_t *mode)
+{
+    PG_CHECK(mode, PHYSIM_ERR_ARGUMENT, "null argument");
+    bool direct = false;
+    PG_TRY(pg::host_direct(device, &direct));
+    *mode = direct ? PHYSIM_HOST_ACCESS_DIRECT : PHYSIM_HOST_ACCESS_COPY;
+    return PHYSIM_OK;
+}

@@ -610,14 +610,26 @@ int physim_gpu_verlet_integrate(PhysimVerlet *v, const Entity *entities, Entity 
     // verlet.rs:102: a different length means the Taylor first step.
     const bool initial = !v->has_prev || v->prev_len != n;
     if (n) {
-        PG_CUDA(cudaMemcpyAsync(v->d_in, entities, n * sizeof(Entity), cudaMemcpyHostToDevice,
-                                v->stream));
-        PG_CUDA(cudaMemcpyAsync(v->d_acc, acc, n * sizeof(Acceleration), cudaMemcpyHostToDevice,
-                                v->stream));
-        PG_TRY(launch_verlet_aos(v->d_in, v->d_prev, v->d_out, v->d_acc, n, dt, initial,
-                                 v->stream));
-        PG_CUDA(cudaMemcpyAsync(new_state, v->d_out, n * sizeof(Entity), cudaMemcpyDeviceToHost,
-                                v->stream));
+        bool direct = false;
+        PG_TRY(host_direct(v->device, &direct));
+        if (direct) {
+            // the kernel reads entities and acc and writes new_state in host
+            // memory, keeping a device copy of entities in d_in
+            host_prefault(entities, n * sizeof(Entity), false);
+            host_prefault(acc, n * sizeof(Acceleration), false);
+            host_prefault(new_state, n * sizeof(Entity), true);
+            PG_TRY(launch_verlet_aos(entities, v->d_prev, new_state, v->d_in, acc, n, dt, initial,
+                                     v->stream));
+        } else {
+            PG_CUDA(cudaMemcpyAsync(v->d_in, entities, n * sizeof(Entity),
+                                    cudaMemcpyHostToDevice, v->stream));
+            PG_CUDA(cudaMemcpyAsync(v->d_acc, acc, n * sizeof(Acceleration),
+                                    cudaMemcpyHostToDevice, v->stream));
+            PG_TRY(launch_verlet_aos(v->d_in, v->d_prev, v->d_out, nullptr, v->d_acc, n, dt,
+                                     initial, v->stream));
+            PG_CUDA(cudaMemcpyAsync(new_state, v->d_out, n * sizeof(Entity),
+                                    cudaMemcpyDeviceToHost, v->stream));
+        }
     }
     PG_CUDA(cudaStreamSynchronize(v->stream));
     // previous_state = entities (verlet.rs:31,81)

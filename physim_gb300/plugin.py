@@ -111,9 +111,18 @@ class GpuVerlet:
         check(lib.physim_gpu_verlet_create(device, C.byref(h)), "physim_gpu_verlet_create")
         self.handle = h
 
-    def integrate(self, entities: np.ndarray, acc: np.ndarray, dt: float) -> np.ndarray:
+    def integrate(self, entities: np.ndarray, acc: np.ndarray, dt: float,
+                  out: np.ndarray | None = None) -> np.ndarray:
+        """The new state; written into `out` (an ENTITY array of the same
+        length, reused across steps as physim's pipeline reuses new_state,
+        pipeline.rs:104-173) when given."""
         entities, acc = as_entities(entities), as_accelerations(acc)
-        new_state = np.empty_like(entities)
+        if out is None:
+            new_state = np.empty_like(entities)
+        else:
+            if out.dtype != ENTITY or len(out) != len(entities) or not out.flags.c_contiguous:
+                raise ValueError("out must be a C-contiguous ENTITY array of the same length")
+            new_state = out
         check(lib.physim_gpu_verlet_integrate(self.handle, entities.ctypes.data,
                                               new_state.ctypes.data, len(entities),
                                               acc.ctypes.data, dt),

@@ -175,3 +175,16 @@ def test_entity_dtype_layout():
 def test_sim_config_layout():
     from physim_gb300._lib import PhysimSimConfig
     assert C.sizeof(PhysimSimConfig) == 64
+
+
+def test_host_access_setting():
+    """The host-access mode is validated and COPY needs no device query."""
+    import physim_gb300 as pg
+    from physim_gb300 import lib
+    assert lib.physim_gpu_set_host_access(3) != 0  # unknown mode
+    try:
+        pg.set_host_access("copy")
+        assert pg.host_access(0) == "copy"
+        assert lib.physim_gpu_host_access(0, None) != 0
+    finally:
+        pg.set_host_access("auto")
