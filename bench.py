@@ -13,9 +13,11 @@ N(N-1) pair interactions plus the f64 kick-drift.  Prints one JSON line.
             device that reaches pageable host memory (Grace over NVLink-C2C)
             the kernels read and write the host arrays in place ("transfer":
             "direct"); value_with_copies is the same run with cudaMemcpyAsync.
-  roofline  the pair kernel against the FP32 peak: 20 flop per pair
-            (Nyland, Harris & Prins, GPU Gems 3 ch. 31) / event time, peak =
-            SMs x 128 FP32 lanes x 2 x max SM clock.
+  roofline  the pair kernel against the FP32 peak: 20 flop per ordered pair
+            (Nyland, Harris & Prins, GPU Gems 3 ch. 31), or 27 per unordered
+            pair when the autotuner picks the symmetric kernel (each pair
+            evaluated once, both bodies updated), over the kernel's event
+            time; peak = SMs x 128 FP32 lanes x 2 x max SM clock.
   cpu_baseline  the C restatement of the reference (single thread, as physim's
             transform runs) on a bounded sample of bodies.
 
@@ -44,6 +46,10 @@ N_CUBE = 1_048_576
 E = 0.01
 DT = 1e-5
 FLOP_PER_PAIR = 20
+# one unordered pair of the symmetric kernel: 3 FADD (d), FMUL + 2 FFMA (r^2),
+# FADD + FMUL + FFMA (the argument), rsqrt, FMUL + 3 FFMA (a_i), FMUL + 3 FFMA
+# (a_j), counting an FFMA as 2 flop and the rsqrt as 1
+FLOP_PER_SYM_PAIR = 27
 FP32_LANES_PER_SM = 128
 METRIC = "Gpair-interactions/s at N=1M (direct-sum simple_astro + verlet)"
 WORKLOAD = "direct-sum N=1,048,580 (1,048,576 cube U[-0.5,0.5]^3 seed 1 + 4 stars m=1e5), e=0.01, verlet dt=1e-5"
@@ -290,13 +296,14 @@ def host_array_steps(pg, element, props, state, steps, device, mode):
     return seconds, used
 
 
-def _timed_steps(sim, stream, steps: int, flush) -> tuple[list[float], list[float]]:
+def _timed_steps(sim, stream, steps: int, flush, pair=False):
     """Per-step CUDA-event times on the simulation's stream, L2 flushed between
-    steps outside the events.  Returns (step ms, gravity-kernel ms)."""
+    steps outside the events.  Returns (step ms, gravity-kernel ms) and, with
+    `pair`, the pair kernel's ms as a third list."""
     import torch
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
-    grav = []
+    grav, pairs = [], []
     for k in range(steps):
         with torch.cuda.stream(stream):
             flush.zero_()
@@ -304,8 +311,11 @@ def _timed_steps(sim, stream, steps: int, flush) -> tuple[list[float], list[floa
             sim.step(1)
             ends[k].record(stream)
         grav.append(sim.last_step_ms()[0])
+        if pair:
+            pairs.append(sim.last_pair_ms())
     torch.cuda.synchronize()
-    return [s.elapsed_time(e) for s, e in zip(starts, ends)], grav
+    times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    return (times, grav, pairs) if pair else (times, grav)
 
 
 def measure_direct(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict:
@@ -331,7 +341,7 @@ def measure_direct(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict
     torch.cuda.synchronize()
     clocks.start()
     t_wall = time.perf_counter()
-    step_ms, grav_ms = _timed_steps(sim, stream, args.steps, flush)
+    step_ms, grav_ms, pair_ms = _timed_steps(sim, stream, args.steps, flush, pair=True)
     wall = time.perf_counter() - t_wall
     dist.barrier()
     clk = clocks.stop()
@@ -340,26 +350,37 @@ def measure_direct(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict
     launches = sim.launches_per_step * args.steps
     sim.close()
 
-    kern_ms = statistics.mean(grav_ms)
-    achieved = FLOP_PER_PAIR * pairs_step / (kern_ms / 1e3) / 1e12
+    kern_ms = statistics.mean(pair_ms)
+    if plan.get("symmetric"):
+        # each unordered pair evaluated once: 27 flop (FFMA = 2) per pair
+        kernel, flop_note = "direct_sym_kernel", FLOP_PER_SYM_PAIR
+        flops_step = FLOP_PER_SYM_PAIR * pairs_step / 2
+    else:
+        kernel, flop_note = "direct_forces_kernel", FLOP_PER_PAIR
+        flops_step = FLOP_PER_PAIR * pairs_step
+    achieved = flops_step / (kern_ms / 1e3) / 1e12
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
     peak = sms * FP32_LANES_PER_SM * 2 * sm_max * 1e6 / 1e12
     traffic = None
     tfile = ROOT / "profiles" / "direct_forces_traffic.json"
     if tfile.exists() and args.bodies == N_CUBE:
         try:
-            traffic = json.loads(tfile.read_text()).get("bytes_per_launch")
-        except ValueError:
+            traffic = json.loads(tfile.read_text()).get(kernel, {}).get("bytes_per_launch")
+        except (ValueError, AttributeError):
             traffic = None
     out = {"value": all_pairs / (total_ms / 1e3) / 1e9, "ms_per_step": total_ms / args.steps,
            "bodies": n, "pairs_per_step": pairs_step, "wall_s": wall, "gpu_launches": launches,
            "plan": plan,
-           "roofline": {"bound": "fp32", "kernel": "direct_forces_kernel", "achieved": achieved,
+           "roofline": {"bound": "fp32", "kernel": kernel, "achieved": achieved,
                         "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                         "traffic": traffic,
                         "peak_basis": f"{sms} SMs x {FP32_LANES_PER_SM} FP32 lanes x 2 x "
                                       f"{sm_max:.0f} MHz (max SM clock, measured-peaks file)",
-                        "flop_per_pair": FLOP_PER_PAIR, "kernel_ms": kern_ms}}
+                        "flop_per_pair": flop_note,
+                        "pairs_per_launch": pairs_step // 2 if plan.get("symmetric")
+                        else pairs_step,
+                        "kernel_ms": kern_ms,
+                        "reduce_ms": statistics.mean(grav_ms) - kern_ms}}
     if clk:
         out["clocks"] = clk
         if clk.get("sm_mhz"):

@@ -333,12 +333,16 @@ int physim_gpu_sim_synchronize(PhysimSim *sim);
 /* The cudaStream_t the simulation runs on. */
 void *physim_gpu_sim_stream(PhysimSim *sim);
 /* Pair-kernel plan of a simple_astro simulation: threads per block, bodies
- * per thread, j-range splits, candidates timed, time of one force pass. */
+ * per thread, j-range splits, candidates timed, whether every unordered pair
+ * is evaluated once (and in how many body tiles of 1,024), time of one force
+ * pass. */
 typedef struct PhysimDirectTuning {
     uint32_t block;
     uint32_t ipt;
     uint32_t splits;
     uint32_t candidates;
+    uint32_t symmetric;
+    uint32_t tiles;
     double force_ms;
 } PhysimDirectTuning;
 
@@ -347,6 +351,11 @@ typedef struct PhysimDirectTuning {
  * simulation starts with a heuristic plan; this makes the choice by
  * measurement.  No-op for astro/astro2.  out may be NULL. */
 int physim_gpu_sim_autotune(PhysimSim *sim, PhysimDirectTuning *out);
+/* Sets the pair-kernel plan of a simple_astro simulation: the symmetric plan
+ * (plan->symmetric != 0; compensated simulations only) or a one-pair kernel
+ * of plan->block threads, plan->ipt bodies per thread and plan->splits
+ * j-range splits.  Other fields are ignored. */
+int physim_gpu_sim_set_plan(PhysimSim *sim, const PhysimDirectTuning *plan);
 /* Number of kernel launches one step enqueues (for launch accounting). */
 int physim_gpu_sim_launches_per_step(PhysimSim *sim);
 /* Records CUDA events around the gravity kernels and the integrator of each
@@ -354,6 +363,10 @@ int physim_gpu_sim_launches_per_step(PhysimSim *sim);
  * returns the two device times in milliseconds. */
 int physim_gpu_sim_set_profiling(PhysimSim *sim, int enable);
 int physim_gpu_sim_last_step_ms(PhysimSim *sim, double *gravity_ms, double *integrate_ms);
+/* simple_astro with profiling on: device milliseconds of the last step's pair
+ * kernel alone (the gravity time less the reduction of the symmetric plan's
+ * slot sums). */
+int physim_gpu_sim_last_pair_ms(PhysimSim *sim, double *pair_ms);
 void physim_gpu_sim_destroy(PhysimSim *sim);
 
 /* The Barnes-Hut tree of a simulation's current state, copied to host arrays

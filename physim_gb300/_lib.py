@@ -99,7 +99,8 @@ class PhysimPlummerParams(C.Structure):
 
 class PhysimDirectTuning(C.Structure):
     _fields_ = [("block", C.c_uint32), ("ipt", C.c_uint32), ("splits", C.c_uint32),
-                ("candidates", C.c_uint32), ("force_ms", C.c_double)]
+                ("candidates", C.c_uint32), ("symmetric", C.c_uint32), ("tiles", C.c_uint32),
+                ("force_ms", C.c_double)]
 
 
 class PhysimEnsembleTuning(C.Structure):
@@ -137,10 +138,12 @@ def _load() -> C.CDLL:
         "physim_gpu_sim_launches_per_step": (C.c_int, [vp]),
         "physim_gpu_sim_set_profiling": (C.c_int, [vp, C.c_int]),
         "physim_gpu_sim_last_step_ms": (C.c_int, [vp, C.POINTER(dbl), C.POINTER(dbl)]),
+        "physim_gpu_sim_last_pair_ms": (C.c_int, [vp, C.POINTER(dbl)]),
         "physim_gpu_sim_destroy": (None, [vp]),
         "physim_gpu_sim_diagnostics": (C.c_int, [vp, C.POINTER(PhysimDiagnostics), C.c_int]),
         "physim_gpu_sim_tree_snapshot": (C.c_int, [vp, C.POINTER(PhysimTreeSnapshot)]),
         "physim_gpu_sim_autotune": (C.c_int, [vp, C.POINTER(PhysimDirectTuning)]),
+        "physim_gpu_sim_set_plan": (C.c_int, [vp, C.POINTER(PhysimDirectTuning)]),
         "physim_gpu_sim_init_cube": (C.c_int, [vp, C.POINTER(PhysimCubeParams)]),
         "physim_gpu_sim_init_plummer": (C.c_int, [vp, C.POINTER(PhysimPlummerParams)]),
         "physim_gpu_generate_cube": (C.c_int, [C.POINTER(PhysimCubeParams), vp, sz, i32]),

@@ -67,7 +67,7 @@ static int accumulate_locked(ElementState *el, const Entity *state, size_t n, Ac
             el->plan_n = (int)n;
         }
         splits = el->plan.splits;
-        PG_TRY(ensure_doubles(el->partial, el->partial_cap, (size_t)splits * 3 * n, st));
+        PG_TRY(ensure_doubles(el->partial, el->partial_cap, direct_partial_doubles(el->plan), st));
         PG_TRY(launch_direct(el->plan, el->bodies.body4, (float)el->e, el->partial, st));
     } else {
         PG_TRY(ensure_doubles(el->partial, el->partial_cap, 3 * n, st));

@@ -35,6 +35,11 @@ struct DirectPlan {
     int n_jtiles = 0;      // j tiles of `block` bodies
     int chunk_tiles = 0;   // j tiles per split
     bool compensated = true;
+    // Every unordered pair evaluated once (direct_sym.cu): `tiles` body tiles
+    // of 1,024, one block per tile pair; the partial sums come out as one
+    // split, after a f32 slot buffer the same allocation holds.
+    bool symmetric = false;
+    int tiles = 0;
 };
 
 // Heuristic plan that fills the GPU: picks the i-tile shape and the number of
@@ -45,10 +50,24 @@ DirectPlan make_direct_plan(int n, int block, int ipt, int splits, bool compensa
 // Enumerates the candidate plans the autotuner times for n bodies.
 int direct_candidates(int n, int device, bool compensated, DirectPlan *out, int cap);
 
+// Whether a one-pair kernel of this shape is built.
+bool direct_shape_supported(int block, int ipt);
+// The symmetric plan for n bodies (compensated sums only).
+DirectPlan make_symmetric_plan(int n);
+// Doubles the `partial` buffer of a plan must hold.
+size_t direct_partial_doubles(const DirectPlan &plan);
+
 // Launches the pair kernel.  body4: n_pad (x,y,z,m) f32 entries.  partial:
-// splits x 3 x n doubles, partial[(s*3+c)*n + i].
+// direct_partial_doubles(plan) doubles; on return partial[(s*3+c)*n + i] for
+// s < plan.splits holds the partial sums.  pairs_done (optional) is recorded
+// on `stream` right after the pair kernel, before any reduction of its
+// output (as an external event node when the stream is being captured).
 int launch_direct(const DirectPlan &plan, const float4 *body4, float e, double *partial,
-                  cudaStream_t stream);
+                  cudaStream_t stream, cudaEvent_t pairs_done = nullptr);
+int launch_direct_symmetric(const DirectPlan &plan, const float4 *body4, float e,
+                            double *partial, cudaStream_t stream, cudaEvent_t pairs_done);
+// Records `ev` on `stream`; inside a stream capture as an external event node.
+int record_event(cudaEvent_t ev, cudaStream_t stream);
 
 // ------------------------------------------------------------------------
 // Body staging, integration and accumulation (integrate.cu)

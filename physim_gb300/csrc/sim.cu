@@ -32,7 +32,8 @@ struct PhysimSim {
     // Optional per-step timing: events around the gravity kernels and the
     // integrator of the most recent step.
     bool profiling = false;
-    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    // step start, gravity done, step done, pair kernel done (simple_astro)
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // The gravity phase of a step, captured once and replayed: the
     // Barnes-Hut build is ~100 short kernels whose launch cost would
     // otherwise dominate at small N.
@@ -78,7 +79,8 @@ int sim_forces(PhysimSim *s, int *splits_out)
     const PhysimSimConfig &c = s->cfg;
     if (c.gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO) {
         *splits_out = s->plan.splits;
-        return launch_direct(s->plan, s->b.body4, (float)c.e, s->partial, s->stream);
+        return launch_direct(s->plan, s->b.body4, (float)c.e, s->partial, s->stream,
+                             s->profiling ? s->ev[3] : nullptr);
     }
     BhParams p;
     p.nchild = c.gravity == PHYSIM_GRAVITY_ASTRO2 ? 8 : 4;
@@ -187,7 +189,7 @@ int physim_gpu_sim_create(const PhysimSimConfig *cfg, size_t n, PhysimSim **out)
     size_t partial_elems = 3 * (n ? n : 1);
     if (rc == PHYSIM_OK && cfg->gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO) {
         s->plan = plan_direct((int)n, cfg->device, cfg->compensated != 0);
-        partial_elems *= (size_t)s->plan.splits;
+        partial_elems = direct_partial_doubles(s->plan);
     }
     if (rc == PHYSIM_OK && cfg->gravity != PHYSIM_GRAVITY_SIMPLE_ASTRO)
         rc = bh_reserve(s->bh, n, cfg->device, (int)cfg->leaf_size, s->stream);
@@ -342,9 +344,8 @@ int physim_gpu_sim_autotune(PhysimSim *s, PhysimDirectTuning *out)
     }
     DirectPlan cand[16];
     const int k = direct_candidates((int)s->n, s->cfg.device, s->cfg.compensated != 0, cand, 16);
-    int max_splits = 1;
-    for (int c = 0; c < k; ++c) max_splits = std::max(max_splits, cand[c].splits);
-    const size_t need = (size_t)max_splits * 3 * s->n;
+    size_t need = 3 * s->n;
+    for (int c = 0; c < k; ++c) need = std::max(need, direct_partial_doubles(cand[c]));
     if (need > s->partial_cap) {
         dev_free(s->partial, s->stream);
         s->partial = nullptr;
@@ -396,8 +397,45 @@ int physim_gpu_sim_autotune(PhysimSim *s, PhysimDirectTuning *out)
         out->ipt = (uint32_t)s->plan.ipt;
         out->splits = (uint32_t)s->plan.splits;
         out->candidates = (uint32_t)k;
+        out->symmetric = s->plan.symmetric ? 1u : 0u;
+        out->tiles = (uint32_t)s->plan.tiles;
         out->force_ms = best_ms;
     }
+    return PHYSIM_OK;
+}
+
+int physim_gpu_sim_set_plan(PhysimSim *s, const PhysimDirectTuning *plan)
+{
+    PG_CHECK(s && plan, PHYSIM_ERR_ARGUMENT, "null argument");
+    PG_CHECK(s->cfg.gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO, PHYSIM_ERR_ARGUMENT,
+             "pair-kernel plans apply to simple_astro simulations");
+    PG_CUDA(cudaSetDevice(s->cfg.device));
+    const bool comp = s->cfg.compensated != 0;
+    DirectPlan p;
+    if (plan->symmetric) {
+        PG_CHECK(comp, PHYSIM_ERR_ARGUMENT, "the symmetric plan needs compensated sums");
+        p = make_symmetric_plan((int)s->n);
+    } else {
+        PG_CHECK(direct_shape_supported((int)plan->block, (int)plan->ipt), PHYSIM_ERR_ARGUMENT,
+                 "no pair kernel with %u threads and %u bodies per thread", plan->block,
+                 plan->ipt);
+        PG_CHECK(plan->splits >= 1, PHYSIM_ERR_ARGUMENT, "splits must be >= 1");
+        p = make_direct_plan((int)s->n, (int)plan->block, (int)plan->ipt, (int)plan->splits, comp);
+    }
+    const size_t need = direct_partial_doubles(p);
+    if (need > s->partial_cap) {
+        dev_free(s->partial, s->stream);
+        s->partial = nullptr;
+        s->partial_cap = 0;
+        PG_TRY(dev_alloc(s->partial, need, s->stream));
+        s->partial_cap = need;
+    }
+    s->plan = p;
+    // the captured gravity phase used the old plan
+    if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    s->graph_exec = nullptr;
+    s->graph = nullptr;
     return PHYSIM_OK;
 }
 
@@ -408,15 +446,27 @@ int physim_gpu_sim_set_profiling(PhysimSim *s, int enable)
     if (enable && !s->ev[0])
         for (cudaEvent_t &e : s->ev) PG_CUDA(cudaEventCreate(&e));
     s->profiling = enable != 0;
-    if (s->bh) {
-        PG_TRY(bh_set_profiling(s->bh, s->profiling));
-        // the captured gravity phase must be re-captured with (or without)
-        // the traversal events
-        if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
-        if (s->graph) cudaGraphDestroy(s->graph);
-        s->graph_exec = nullptr;
-        s->graph = nullptr;
-    }
+    if (s->bh) PG_TRY(bh_set_profiling(s->bh, s->profiling));
+    // the captured gravity phase must be re-captured with (or without) the
+    // traversal and pair-kernel events
+    if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    s->graph_exec = nullptr;
+    s->graph = nullptr;
+    return PHYSIM_OK;
+}
+
+int physim_gpu_sim_last_pair_ms(PhysimSim *s, double *pair_ms)
+{
+    PG_CHECK(s && pair_ms, PHYSIM_ERR_ARGUMENT, "null argument");
+    PG_CHECK(s->profiling, PHYSIM_ERR_ARGUMENT, "profiling is off");
+    PG_CHECK(s->cfg.gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO, PHYSIM_ERR_ARGUMENT,
+             "the pair kernel is simple_astro's");
+    PG_CUDA(cudaSetDevice(s->cfg.device));
+    PG_CUDA(cudaEventSynchronize(s->ev[2]));
+    float a = 0.f;
+    PG_CUDA(cudaEventElapsedTime(&a, s->ev[0], s->ev[3]));
+    *pair_ms = a;
     return PHYSIM_OK;
 }
 
@@ -538,8 +588,10 @@ void *physim_gpu_sim_stream(PhysimSim *s) { return s ? (void *)s->stream : nullp
 int physim_gpu_sim_launches_per_step(PhysimSim *s)
 {
     if (!s) return 0;
-    const int per_eval = s->cfg.gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO ? 2
-                                                                       : bh_launches(s->bh) + 1;
+    // gravity launches + the integrator's kernel
+    const int per_eval = s->cfg.gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO
+                             ? (s->plan.symmetric ? 2 : 1) + 1
+                             : bh_launches(s->bh) + 1;
     return s->cfg.integrator == PHYSIM_INTEGRATOR_RK4 ? 4 * per_eval : per_eval;
 }
 

@@ -177,7 +177,17 @@ class Simulation:
         t = PhysimDirectTuning()
         check(lib.physim_gpu_sim_autotune(self.handle, C.byref(t)), "physim_gpu_sim_autotune")
         return {"block": t.block, "ipt": t.ipt, "splits": t.splits, "candidates": t.candidates,
-                "force_ms": t.force_ms}
+                "symmetric": bool(t.symmetric), "tiles": t.tiles, "force_ms": t.force_ms}
+
+    def set_plan(self, symmetric: bool = False, block: int = 256, ipt: int = 4,
+                 splits: int = 1) -> None:
+        """Fixes the pair-kernel plan (simple_astro): every unordered pair once
+        (`symmetric`), or a one-pair kernel of `block` threads with `ipt`
+        bodies per thread and `splits` j-range splits."""
+        from ._lib import PhysimDirectTuning
+        t = PhysimDirectTuning()
+        t.symmetric, t.block, t.ipt, t.splits = int(symmetric), block, ipt, splits
+        check(lib.physim_gpu_sim_set_plan(self.handle, C.byref(t)), "physim_gpu_sim_set_plan")
 
     def set_profiling(self, enable: bool = True) -> None:
         check(lib.physim_gpu_sim_set_profiling(self.handle, 1 if enable else 0),
@@ -189,6 +199,13 @@ class Simulation:
         check(lib.physim_gpu_sim_last_step_ms(self.handle, C.byref(g), C.byref(i)),
               "physim_gpu_sim_last_step_ms")
         return g.value, i.value
+
+    def last_pair_ms(self) -> float:
+        """Device milliseconds of the last step's pair kernel (simple_astro)."""
+        v = C.c_double()
+        check(lib.physim_gpu_sim_last_pair_ms(self.handle, C.byref(v)),
+              "physim_gpu_sim_last_pair_ms")
+        return v.value
 
     @property
     def stream(self) -> int:
