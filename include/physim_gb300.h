@@ -431,6 +431,9 @@ typedef struct PhysimEnsembleTuning {
     uint32_t ipt;          /* bodies per thread */
     uint32_t chunk_bodies; /* j bodies per work unit */
     uint32_t candidates;   /* plans timed */
+    uint32_t symmetric_from; /* members from this many bodies evaluate each
+                              * unordered pair once (0: none) */
+    uint32_t reserved;
     double force_ms;       /* time of one pair-kernel pass with the chosen plan */
 } PhysimEnsembleTuning;
 

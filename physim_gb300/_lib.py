@@ -105,7 +105,8 @@ class PhysimDirectTuning(C.Structure):
 
 class PhysimEnsembleTuning(C.Structure):
     _fields_ = [("block", C.c_uint32), ("ipt", C.c_uint32), ("chunk_bodies", C.c_uint32),
-                ("candidates", C.c_uint32), ("force_ms", C.c_double)]
+                ("candidates", C.c_uint32), ("symmetric_from", C.c_uint32),
+                ("reserved", C.c_uint32), ("force_ms", C.c_double)]
 
 
 ELEMENTS = ("astro", "astro2", "simple_astro")

@@ -11,6 +11,10 @@
 //      code as the per-simulation kernel;
 //   2. one kernel combining the partial sums and applying verlet in f64 for
 //      every member with steps left, then counting the step.
+// Members from a plan's size threshold up evaluate each unordered pair once
+// (direct_sym_tile.cuh): a second persistent kernel pulls their 1,024-body
+// tile pairs, writing per-member f32 slot sums that the verlet kernel adds
+// with TwoSum; smaller members keep the one-pair units.
 // One step is captured once (per work plan) into a CUDA graph and replayed
 // for every step.  Members can be resized in place (a finished member's slot
 // takes the next job; the work plan is rebuilt).  The autotuner times the candidate kernel shapes (threads x bodies per thread)
@@ -22,6 +26,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "direct_sym_tile.cuh"
 #include "direct_tile.cuh"
 #include "engine.h"
 
@@ -37,10 +42,18 @@ struct MemberInfo {
     int32_t splits;
     float e;
     double dt;
+    int32_t sym_tiles;    // > 0: tiles of the symmetric units, slot sums at soff
+    int32_t pad;
+    int64_t soff;         // first f32 slot sum of the member
 };
 
 struct WorkUnit {
     int32_t member, itile, split, pad;
+};
+
+// A tile pair (I, J), I <= J, of a member on the symmetric units.
+struct SymUnit {
+    int32_t member, I, J, pad;
 };
 
 template <int BLOCK, int IPT, bool COMP>
@@ -69,6 +82,31 @@ ensemble_forces_kernel(const float4 *__restrict__ body4, const MemberInfo *__res
     }
 }
 
+__global__ void __launch_bounds__(kSymThreads, 3)
+ensemble_sym_kernel(const float4 *__restrict__ body4, const MemberInfo *__restrict__ members,
+                    const SymUnit *__restrict__ units, int n_units,
+                    const unsigned long long *__restrict__ remaining, int *__restrict__ counter,
+                    float *__restrict__ slots)
+{
+    __shared__ float jacc[kSymWarps][kSymTile][3];
+    __shared__ int next;
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(counter, 1);
+        __syncthreads();
+        const int u = next;
+        if (u >= n_units) return;
+        const SymUnit w = units[u];
+        if (remaining[w.member] != 0) {
+            const MemberInfo m = members[w.member];
+            if (w.I == w.J)
+                sym_tile_pair<true>(body4 + m.off, m.n, w.I, w.J, m.e, slots + m.soff, jacc);
+            else
+                sym_tile_pair<false>(body4 + m.off, m.n, w.I, w.J, m.e, slots + m.soff, jacc);
+        }
+        __syncthreads();
+    }
+}
+
 // Combine + verlet for every member with steps left (verlet.rs:24-82; the
 // first step after an upload is the Taylor step).  slot_member[s] < 0 marks
 // padding.
@@ -78,7 +116,8 @@ __global__ void ensemble_verlet_kernel(float4 *body4, const double *__restrict__
                                        const MemberInfo *__restrict__ members,
                                        const unsigned long long *__restrict__ remaining,
                                        const unsigned long long *__restrict__ done,
-                                       const double *__restrict__ partial, int slots, double *x,
+                                       const double *__restrict__ partial,
+                                       const float *__restrict__ slot_sums, int slots, double *x,
                                        double *y, double *z, double *vx, double *vy, double *vz,
                                        double *px, double *py, double *pz)
 {
@@ -90,11 +129,28 @@ __global__ void ensemble_verlet_kernel(float4 *body4, const double *__restrict__
     const int i = s - m.off;
     double ax = 0.0, ay = 0.0, az = 0.0;
     if (!fixed[s]) {
-        for (int sp = 0; sp < m.splits; ++sp) {
-            const double *p = partial + m.poff + (size_t)sp * 3 * m.n;
-            ax += p[i];
-            ay += p[m.n + i];
-            az += p[2 * (size_t)m.n + i];
+        if (m.sym_tiles > 0) {
+            // the member's slot sums, TwoSum-compensated in slot order
+            const size_t n3 = 3 * (size_t)m.n;
+            const float *p = slot_sums + m.soff + i;
+            float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
+            for (int t = 0; t < m.sym_tiles; ++t)
+                for (int c = 0; c < 3; ++c) {
+                    float sum, err;
+                    two_sum(h[c], p[(size_t)t * n3 + (size_t)c * m.n], sum, err);
+                    h[c] = sum;
+                    l[c] += err;
+                }
+            ax = (double)h[0] + (double)l[0];
+            ay = (double)h[1] + (double)l[1];
+            az = (double)h[2] + (double)l[2];
+        } else {
+            for (int sp = 0; sp < m.splits; ++sp) {
+                const double *p = partial + m.poff + (size_t)sp * 3 * m.n;
+                ax += p[i];
+                ay += p[m.n + i];
+                az += p[2 * (size_t)m.n + i];
+            }
         }
         if (mass[s] == 0.0) ax = ay = az = __longlong_as_double(0x7ff8000000000000LL);
     }
@@ -129,7 +185,7 @@ __global__ void ensemble_count_kernel(unsigned long long *remaining, unsigned lo
                                       int count, int *counter)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k == 0) *counter = 0;  // the next step's work queue starts empty
+    if (k == 0) counter[0] = counter[1] = 0;  // the next step's work queues start empty
     if (k >= count || remaining[k] == 0) return;
     done[k] += 1;
     if (remaining[k] != ~0ull) remaining[k] -= 1;
@@ -196,6 +252,10 @@ struct Shape {
 constexpr Shape kShapes[] = {{128, 2}, {128, 4}, {256, 4}, {256, 2}, {128, 8}};
 constexpr int kChunks[] = {4096, 8192, 16384, 65536};
 constexpr int kMinChunk = 4096;  // smallest j chunk any plan uses (sizes the partial sums)
+// Default size from which members use the symmetric units, and the thresholds
+// the autotuner compares (INT32_MAX: none).
+constexpr int kEnsembleSymMin = 16384;
+constexpr int kSymMins[] = {8192, 16384, 32768, INT32_MAX};
 
 template <int BLOCK, int IPT>
 void *ens_kernel_ptr(bool comp)
@@ -243,12 +303,19 @@ struct PhysimEnsemble {
     int n_units = 0;
     size_t units_cap = 0;
     unsigned long long *remaining = nullptr, *done = nullptr;
-    int *counter = nullptr;
+    int *counter = nullptr;  // [0] one-pair units, [1] symmetric units
     double *partial = nullptr;
+    SymUnit *d_sym_units = nullptr;
+    int n_sym_units = 0;
+    size_t sym_units_cap = 0;
+    float *slot_sums = nullptr;  // f32 slot sums of the symmetric members
+    size_t slot_cap = 0;
+    int sym_grid = 0;
     Entity *staging = nullptr;
     size_t staging_cap = 0;
     // plan
     int block = 128, ipt = 4, chunk = 16384;
+    int sym_min = kEnsembleSymMin;  // members from this many bodies use the symmetric units
     int grid = 0;
     bool tuned = false;
     double tuned_ms = 0.0;
@@ -277,18 +344,31 @@ void drop_graph(PhysimEnsemble *E)
 }
 
 // Builds member tiling and the work list for (block, ipt, chunk) and uploads them.
-int plan_ensemble(PhysimEnsemble *E, int block, int ipt, int chunk)
+int plan_ensemble(PhysimEnsemble *E, int block, int ipt, int chunk, int sym_min)
 {
     const int chunk_tiles = std::max(1, chunk / block);
     std::vector<WorkUnit> units;
+    std::vector<SymUnit> sym_units;
     std::vector<long long> cost;
-    int64_t poff = 0;
+    int64_t poff = 0, soff = 0;
     for (size_t k = 0; k < E->members.size(); ++k) {
         MemberInfo &mi = E->members[k];
         mi.n_jtiles = cdiv(mi.n, block);
         mi.chunk_tiles = chunk_tiles;
         mi.splits = std::max(1, cdiv(mi.n_jtiles, chunk_tiles));
         mi.poff = poff;
+        mi.sym_tiles = 0;
+        mi.soff = soff;
+        if (mi.n >= sym_min && E->cfg.compensated != 0) {
+            // each unordered pair once: all tile pairs of the member
+            const int T = (int)(pad_bodies((size_t)mi.n) / kSymTile);
+            mi.sym_tiles = T;
+            mi.splits = 0;
+            soff += (int64_t)T * 3 * mi.n;
+            for (int J = 0; J < T; ++J)
+                for (int I = 0; I <= J; ++I) sym_units.push_back({(int32_t)k, I, J, 0});
+            continue;
+        }
         poff += (int64_t)mi.splits * 3 * mi.n;
         const int n_itiles = cdiv(mi.n, block * ipt);
         for (int it = 0; it < n_itiles; ++it)
@@ -310,25 +390,55 @@ int plan_ensemble(PhysimEnsemble *E, int block, int ipt, int chunk)
         PG_TRY(ealloc(E, E->d_units, sorted.size()));
         E->units_cap = sorted.size();
     }
-    PG_CUDA(cudaMemcpyAsync(E->d_units, sorted.data(), sorted.size() * sizeof(WorkUnit),
-                            cudaMemcpyHostToDevice, E->stream));
+    if (sym_units.size() > E->sym_units_cap) {
+        dev_free(E->d_sym_units, E->stream);
+        E->d_sym_units = nullptr;
+        PG_TRY(ealloc(E, E->d_sym_units, sym_units.size()));
+        E->sym_units_cap = sym_units.size();
+    }
+    if ((size_t)soff > E->slot_cap) {
+        dev_free(E->slot_sums, E->stream);
+        E->slot_sums = nullptr;
+        PG_TRY(ealloc(E, E->slot_sums, (size_t)soff));
+        E->slot_cap = (size_t)soff;
+    }
+    if (!sorted.empty())
+        PG_CUDA(cudaMemcpyAsync(E->d_units, sorted.data(), sorted.size() * sizeof(WorkUnit),
+                                cudaMemcpyHostToDevice, E->stream));
+    if (!sym_units.empty())
+        PG_CUDA(cudaMemcpyAsync(E->d_sym_units, sym_units.data(),
+                                sym_units.size() * sizeof(SymUnit), cudaMemcpyHostToDevice,
+                                E->stream));
     PG_CUDA(cudaMemcpyAsync(E->d_members, E->members.data(), E->members.size() * sizeof(MemberInfo),
                             cudaMemcpyHostToDevice, E->stream));
     PG_CUDA(cudaStreamSynchronize(E->stream));
     E->n_units = (int)sorted.size();
+    E->n_sym_units = (int)sym_units.size();
     E->block = block;
     E->ipt = ipt;
     E->chunk = chunk;
+    E->sym_min = sym_min;
     int per_sm = 1;
     PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &per_sm, ens_kernel(block, ipt, E->cfg.compensated != 0), block, 0));
     E->grid = std::max(1, per_sm) * device_sm_count(E->device);
+    int sym_per_sm = 1;
+    PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sym_per_sm, ensemble_sym_kernel,
+                                                          kSymThreads, 0));
+    E->sym_grid = std::max(1, sym_per_sm) * device_sm_count(E->device);
     drop_graph(E);
     return PHYSIM_OK;
 }
 
 int launch_forces(PhysimEnsemble *E)
 {
+    if (E->n_sym_units > 0) {
+        ensemble_sym_kernel<<<std::min(E->sym_grid, E->n_sym_units), kSymThreads, 0, E->stream>>>(
+            E->body4, E->d_members, E->d_sym_units, E->n_sym_units, E->remaining, E->counter + 1,
+            E->slot_sums);
+        PG_CUDA(cudaGetLastError());
+    }
+    if (E->n_units == 0) return PHYSIM_OK;
     void *fn = ens_kernel(E->block, E->ipt, E->cfg.compensated != 0);
     PG_CHECK(fn, PHYSIM_ERR_ARGUMENT, "no ensemble kernel for %d x %d", E->block, E->ipt);
     void *args[] = {(void *)&E->body4, (void *)&E->d_members, (void *)&E->d_units,
@@ -344,7 +454,7 @@ int enqueue_step(PhysimEnsemble *E)
     const int t = 256;
     ensemble_verlet_kernel<<<cdiv(E->slots, t), t, 0, E->stream>>>(
         E->body4, E->m, E->fixed, E->slot_member, E->d_members, E->remaining, E->done, E->partial,
-        E->slots, E->x, E->y, E->z, E->vx, E->vy, E->vz, E->px, E->py, E->pz);
+        E->slot_sums, E->slots, E->x, E->y, E->z, E->vx, E->vy, E->vz, E->px, E->py, E->pz);
     ensemble_count_kernel<<<cdiv((long long)E->members.size(), 256), 256, 0, E->stream>>>(
         E->remaining, E->done, (int)E->members.size(), E->counter);
     PG_CUDA(cudaGetLastError());
@@ -356,7 +466,8 @@ void free_ensemble(PhysimEnsemble *E)
     drop_graph(E);
     void *p[] = {E->body4, E->fixed, E->x,  E->y,  E->z,  E->vx, E->vy, E->vz, E->px, E->py,
                  E->pz,    E->m,     E->radius, E->id, E->slot_member, E->d_members, E->d_units,
-                 E->remaining, E->done, E->counter, E->partial, E->staging};
+                 E->remaining, E->done, E->counter, E->partial, E->staging,
+                 E->d_sym_units, E->slot_sums};
     for (void *q : p) dev_free(q, E->stream);
     if (E->stream) cudaStreamSynchronize(E->stream);
 }
@@ -433,7 +544,7 @@ int physim_gpu_ensemble_create(const PhysimSimConfig *cfg, const size_t *sizes, 
     EA(E->d_members, count);
     EA(E->remaining, count);
     EA(E->done, count);
-    EA(E->counter, 1);
+    EA(E->counter, 2);
     EA(E->partial, partial_elems);
 #undef EA
     if (rc == PHYSIM_OK) {
@@ -445,7 +556,7 @@ int physim_gpu_ensemble_create(const PhysimSimConfig *cfg, const size_t *sizes, 
         if (cudaMemsetAsync(E->body4, 0, slots * sizeof(float4), E->stream) != cudaSuccess ||
             cudaMemsetAsync(E->fixed, 1, slots, E->stream) != cudaSuccess ||
             cudaMemsetAsync(E->m, 0, slots * sizeof(double), E->stream) != cudaSuccess ||
-            cudaMemsetAsync(E->counter, 0, sizeof(int), E->stream) != cudaSuccess ||
+            cudaMemsetAsync(E->counter, 0, 2 * sizeof(int), E->stream) != cudaSuccess ||
             cudaMemcpyAsync(E->slot_member, map.data(), map.size() * sizeof(int32_t),
                             cudaMemcpyHostToDevice, E->stream) != cudaSuccess ||
             cudaMemcpyAsync(E->remaining, rem.data(), count * sizeof(unsigned long long),
@@ -457,7 +568,7 @@ int physim_gpu_ensemble_create(const PhysimSimConfig *cfg, const size_t *sizes, 
             rc = PHYSIM_ERR_CUDA;
         }
     }
-    if (rc == PHYSIM_OK) rc = plan_ensemble(E, 128, 4, 16384);
+    if (rc == PHYSIM_OK) rc = plan_ensemble(E, 128, 4, 16384, kEnsembleSymMin);
     if (rc != PHYSIM_OK) {
         free_ensemble(E);
         if (E->own_stream) cudaStreamDestroy(E->stream);
@@ -522,51 +633,56 @@ int physim_gpu_ensemble_autotune(PhysimEnsemble *E, PhysimEnsembleTuning *out)
     PG_CUDA(cudaEventCreate(&a));
     PG_CUDA(cudaEventCreate(&b));
     double best = 1e300;
-    int bb = E->block, bi = E->ipt, bc = E->chunk, tried = 0;
+    int bb = E->block, bi = E->ipt, bc = E->chunk, bs = E->sym_min, tried = 0;
     int rc = PHYSIM_OK;
-    for (const Shape &s : kShapes) {
-        for (int chunk : kChunks) {
-            rc = plan_ensemble(E, s.block, s.ipt, chunk);
-            if (rc != PHYSIM_OK) break;
-            // one untimed + two timed force evaluations (the state is not advanced)
-            float ms_total = 0.f;
-            for (int rep = 0; rep < 3 && rc == PHYSIM_OK; ++rep) {
-                if (cudaMemsetAsync(E->counter, 0, sizeof(int), E->stream) != cudaSuccess ||
-                    cudaEventRecord(a, E->stream) != cudaSuccess) {
-                    rc = PHYSIM_ERR_CUDA;
-                    break;
-                }
-                rc = launch_forces(E);
-                if (rc != PHYSIM_OK) break;
-                if (cudaEventRecord(b, E->stream) != cudaSuccess ||
-                    cudaEventSynchronize(b) != cudaSuccess) {
-                    rc = PHYSIM_ERR_CUDA;
-                    break;
-                }
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, a, b);
-                if (rep > 0) ms_total += ms;
+    // one untimed + two timed force evaluations of a plan (the state is not advanced)
+    auto time_plan = [&](int block, int ipt, int chunk, int sym_min) {
+        rc = plan_ensemble(E, block, ipt, chunk, sym_min);
+        float ms_total = 0.f;
+        for (int rep = 0; rep < 3 && rc == PHYSIM_OK; ++rep) {
+            if (cudaMemsetAsync(E->counter, 0, 2 * sizeof(int), E->stream) != cudaSuccess ||
+                cudaEventRecord(a, E->stream) != cudaSuccess) {
+                rc = PHYSIM_ERR_CUDA;
+                break;
             }
+            rc = launch_forces(E);
             if (rc != PHYSIM_OK) break;
-            ++tried;
-            const double ms = ms_total / 2.0;
-            if (ms < best) {
-                best = ms;
-                bb = s.block;
-                bi = s.ipt;
-                bc = chunk;
+            if (cudaEventRecord(b, E->stream) != cudaSuccess ||
+                cudaEventSynchronize(b) != cudaSuccess) {
+                rc = PHYSIM_ERR_CUDA;
+                break;
             }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            if (rep > 0) ms_total += ms;
         }
-        if (rc != PHYSIM_OK) break;
-    }
+        if (rc != PHYSIM_OK) return;
+        ++tried;
+        const double ms = ms_total / 2.0;
+        if (ms < best) {
+            best = ms;
+            bb = block;
+            bi = ipt;
+            bc = chunk;
+            bs = sym_min;
+        }
+    };
+    // the one-pair shapes with the default threshold, then the thresholds
+    // with the best shape
+    for (const Shape &s : kShapes)
+        for (int chunk : kChunks)
+            if (rc == PHYSIM_OK) time_plan(s.block, s.ipt, chunk, kEnsembleSymMin);
+    const int sb = bb, si = bi, sc = bc;
+    for (int sym_min : kSymMins)
+        if (rc == PHYSIM_OK && sym_min != kEnsembleSymMin) time_plan(sb, si, sc, sym_min);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     if (rc != PHYSIM_OK) {
         set_error("autotune failed: %s", last_error());
         return rc;
     }
-    PG_CUDA(cudaMemsetAsync(E->counter, 0, sizeof(int), E->stream));
-    PG_TRY(plan_ensemble(E, bb, bi, bc));
+    PG_CUDA(cudaMemsetAsync(E->counter, 0, 2 * sizeof(int), E->stream));
+    PG_TRY(plan_ensemble(E, bb, bi, bc, bs));
     E->tuned = true;
     E->tuned_ms = best;
     E->candidates = tried;
@@ -575,6 +691,7 @@ int physim_gpu_ensemble_autotune(PhysimEnsemble *E, PhysimEnsembleTuning *out)
         out->ipt = (uint32_t)bi;
         out->chunk_bodies = (uint32_t)bc;
         out->candidates = (uint32_t)tried;
+        out->symmetric_from = bs == INT32_MAX ? 0u : (uint32_t)bs;
         out->force_ms = best;
     }
     return PHYSIM_OK;
@@ -601,7 +718,7 @@ int physim_gpu_ensemble_resize_member(PhysimEnsemble *E, size_t index, size_t n)
     PG_CUDA(cudaMemcpyAsync(E->remaining + index, &zero, sizeof zero, cudaMemcpyHostToDevice,
                             E->stream));
     drop_graph(E);
-    return plan_ensemble(E, E->block, E->ipt, E->chunk);
+    return plan_ensemble(E, E->block, E->ipt, E->chunk, E->sym_min);
 }
 
 int physim_gpu_ensemble_step(PhysimEnsemble *E, uint32_t steps)
@@ -689,7 +806,11 @@ int physim_gpu_ensemble_synchronize(PhysimEnsemble *E)
 
 void *physim_gpu_ensemble_stream(PhysimEnsemble *E) { return E ? (void *)E->stream : nullptr; }
 
-int physim_gpu_ensemble_launches_per_step(PhysimEnsemble *E) { return E ? 3 : 0; }
+int physim_gpu_ensemble_launches_per_step(PhysimEnsemble *E)
+{
+    if (!E) return 0;
+    return 2 + (E->n_units > 0 ? 1 : 0) + (E->n_sym_units > 0 ? 1 : 0);
+}
 
 void physim_gpu_ensemble_destroy(PhysimEnsemble *E)
 {

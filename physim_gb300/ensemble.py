@@ -72,7 +72,8 @@ class Ensemble:
         check(lib.physim_gpu_ensemble_autotune(self.handle, C.byref(t)),
               "physim_gpu_ensemble_autotune")
         return {"block": t.block, "ipt": t.ipt, "chunk_bodies": t.chunk_bodies,
-                "candidates": t.candidates, "force_ms": t.force_ms}
+                "candidates": t.candidates, "symmetric_from": t.symmetric_from,
+                "force_ms": t.force_ms}
 
     def step(self, steps: int = 1) -> None:
         check(lib.physim_gpu_ensemble_step(self.handle, steps), "physim_gpu_ensemble_step")

@@ -144,3 +144,86 @@ def test_resized_slots_match_solo_runs():
     for s, g, k in ((big, got_big, 6), (small, got_small, 5), (other, got_other, 12)):
         err = trajectory_errors(s, g, _solo(s, k))
         assert err["pos_rel_l2"] < 1e-6 and err["vel_rel_l2"] < 1e-6, err
+
+
+def _big_members():
+    """Members on both sides of the default symmetric threshold (16,384
+    bodies), one with a fixed body."""
+    from physim_gb300 import ics
+    out = [ics.cube_with_stars(20000, seed=301), ics.plummer(1000, seed=302, a=0.1),
+           ics.plummer(40000, seed=303, a=0.1), ics.cube_with_stars(16384, seed=304),
+           ics.cube_with_stars(5000, seed=305)]
+    out[0]["fixed"][7] = 1
+    return out
+
+
+def test_symmetric_members_match_solo_runs():
+    """Members from 16,384 bodies evaluate each unordered pair once (slot
+    sums added in the verlet kernel); every member still equals its solo run
+    and the oracle."""
+    import physim_gb300 as pg
+    from test_verlet_gpu import trajectory_errors
+    members = _big_members()
+    with pg.Ensemble(members, pg.SimConfig(gravity="simple_astro", e=0.01, dt=1e-5)) as ens:
+        assert ens.launches_per_step == 4  # symmetric + one-pair pair kernels, verlet, count
+        ens.step(10)
+        got = [ens.download(k) for k in range(len(members))]
+    for k, s in enumerate(members):
+        err = trajectory_errors(s, got[k], _solo(s, 10))
+        assert err["pos_rel_l2"] < 1e-6 and err["vel_rel_l2"] < 1e-6, (k, err)
+
+
+def test_symmetric_member_matches_oracle(oracle_mod):
+    import physim_gb300 as pg
+    from test_verlet_gpu import trajectory_errors
+    members = _big_members()[:1]
+    with pg.Ensemble(members, pg.SimConfig(gravity="simple_astro", e=0.01, dt=1e-5)) as ens:
+        ens.step(3)
+        got = ens.download(0)
+    want = oracle_mod.run_pipeline(members[0], "simple_astro", 3, 1e-5, 0.01)
+    err = trajectory_errors(members[0], got, want)
+    assert err["pos_rel_l2"] < 1e-5 and err["vel_rel_l2"] < 1e-5, err
+
+
+def test_autotune_with_symmetric_members():
+    import physim_gb300 as pg
+    from test_verlet_gpu import trajectory_errors
+    members = _big_members()
+    with pg.Ensemble(members, pg.SimConfig(gravity="simple_astro", e=0.01, dt=1e-5)) as ens:
+        plan = ens.autotune()
+        ens.step(5)
+        got = [ens.download(k) for k in range(len(members))]
+    assert plan["candidates"] >= 20 and plan["symmetric_from"] in (0, 8192, 16384, 32768)
+    for k, s in enumerate(members):
+        err = trajectory_errors(s, got[k], _solo(s, 5))
+        assert err["pos_rel_l2"] < 1e-6, (k, plan, err)
+
+
+def test_resized_slot_crosses_symmetric_threshold():
+    """A slot of 40,000 bodies holds a symmetric member, then a smaller
+    symmetric one, then a one-pair one: each equals its solo run."""
+    import physim_gb300 as pg
+    from physim_gb300 import ics
+    from test_verlet_gpu import trajectory_errors
+    cfg = pg.SimConfig(gravity="simple_astro", e=0.01, dt=1e-5)
+    jobs = [ics.plummer(40000, seed=310, a=0.1), ics.cube_with_stars(18000, seed=311),
+            ics.plummer(3000, seed=312, a=0.1)]
+    other = ics.cube_with_stars(17000, seed=313)
+    ens = pg.Ensemble.slots([40000, 17000], cfg)
+    try:
+        ens.resize_member(1, len(other))
+        ens.upload(1, other)
+        ens.set_member(1, 0.01, 1e-5, 9)
+        for job in jobs:
+            ens.resize_member(0, len(job))
+            ens.upload(0, job)
+            ens.set_member(0, 0.01, 1e-5, 3)
+            ens.step(3)
+            got = ens.download(0)
+            err = trajectory_errors(job, got, _solo(job, 3))
+            assert err["pos_rel_l2"] < 1e-6 and err["vel_rel_l2"] < 1e-6, (len(job), err)
+        got_other = ens.download(1)
+    finally:
+        ens.close()
+    err = trajectory_errors(other, got_other, _solo(other, 9))
+    assert err["pos_rel_l2"] < 1e-6, err
