@@ -328,6 +328,15 @@ int physim_gpu_generate_plummer(const PhysimPlummerParams *p, Entity *out, size_
 int physim_gpu_sim_download(PhysimSim *sim, Entity *state, size_t n);
 /* Waits, then writes the accelerations of the current state (not +=). */
 int physim_gpu_sim_accelerations(PhysimSim *sim, Acceleration *acc, size_t n);
+/* Waits, then writes the reference's direct-sum accelerations in f64 of the
+ * bodies idx[0..count) of the current state to out[0..count): the pair law of
+ * astro/src/lib.rs:84-113 with every f64 operation in the reference's order,
+ * bodies at equal positions skipped, F/m_i (NaN for m_i = 0, 0 for fixed
+ * bodies), summed over all bodies in a fixed tree order.  An accuracy
+ * reference for every gravity element; f64 is slow on GB300, so sample
+ * (16,384 bodies of 1,048,580 take about 2 s).  Indices must be < n. */
+int physim_gpu_sim_accelerations_f64(PhysimSim *sim, const int64_t *idx, size_t count,
+                                     Acceleration *out);
 /* Waits for all work enqueued on the simulation's stream. */
 int physim_gpu_sim_synchronize(PhysimSim *sim);
 /* The cudaStream_t the simulation runs on. */

@@ -134,6 +134,7 @@ def _load() -> C.CDLL:
         "physim_gpu_sim_step": (C.c_int, [vp, u32]),
         "physim_gpu_sim_download": (C.c_int, [vp, vp, sz]),
         "physim_gpu_sim_accelerations": (C.c_int, [vp, vp, sz]),
+        "physim_gpu_sim_accelerations_f64": (C.c_int, [vp, vp, sz, vp]),
         "physim_gpu_sim_synchronize": (C.c_int, [vp]),
         "physim_gpu_sim_stream": (vp, [vp]),
         "physim_gpu_sim_launches_per_step": (C.c_int, [vp]),

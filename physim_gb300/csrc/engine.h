@@ -160,6 +160,12 @@ int launch_verlet_aos(const Entity *in, const Entity *d_prev, Entity *out, Entit
                       const Acceleration *acc, size_t n, double dt, bool initial,
                       cudaStream_t stream);
 
+// The reference's direct-sum accelerations in f64 (reference per-pair
+// operation order) of the bodies d_idx[0..count) of b's f64 state, into
+// d_out[0..count) (reference_f64.cu).  Indices must be in [0, b.n).
+int launch_f64_sample(const DeviceBodies &b, double e, const int64_t *d_idx, size_t count,
+                      Acceleration *d_out, cudaStream_t stream);
+
 // Whole-system f64 diagnostics into d_out[0..8]: mass, m*x, m*y, m*z,
 // m*vx, m*vy, m*vz, kinetic energy, potential energy (if `potential`).
 int launch_diagnostics(const DeviceBodies &b, double e, double *d_out, bool potential,

@@ -404,6 +404,38 @@ int physim_gpu_sim_autotune(PhysimSim *s, PhysimDirectTuning *out)
     return PHYSIM_OK;
 }
 
+int physim_gpu_sim_accelerations_f64(PhysimSim *s, const int64_t *idx, size_t count,
+                                     Acceleration *out)
+{
+    PG_CHECK(s && ((idx && out) || count == 0), PHYSIM_ERR_ARGUMENT, "null argument");
+    PG_CHECK(s->uploaded, PHYSIM_ERR_ARGUMENT, "accelerations before upload");
+    for (size_t k = 0; k < count; ++k)
+        PG_CHECK(idx[k] >= 0 && (size_t)idx[k] < s->n, PHYSIM_ERR_ARGUMENT,
+                 "sample index %lld out of range (%zu bodies)", (long long)idx[k], s->n);
+    if (count == 0) return PHYSIM_OK;
+    PG_CUDA(cudaSetDevice(s->cfg.device));
+    int64_t *d_idx = nullptr;
+    Acceleration *d_out = nullptr;
+    PG_TRY(dev_alloc(d_idx, count, s->stream));
+    int rc = dev_alloc(d_out, count, s->stream);
+    if (rc == PHYSIM_OK &&
+        cudaMemcpyAsync(d_idx, idx, count * sizeof(int64_t), cudaMemcpyHostToDevice, s->stream) !=
+            cudaSuccess) {
+        set_error("copy of the sample indices failed");
+        rc = PHYSIM_ERR_CUDA;
+    }
+    if (rc == PHYSIM_OK) rc = launch_f64_sample(s->b, s->cfg.e, d_idx, count, d_out, s->stream);
+    if (rc == PHYSIM_OK && (cudaMemcpyAsync(out, d_out, count * sizeof(Acceleration),
+                                            cudaMemcpyDeviceToHost, s->stream) != cudaSuccess ||
+                            cudaStreamSynchronize(s->stream) != cudaSuccess)) {
+        set_error("f64 sample accelerations failed");
+        rc = PHYSIM_ERR_CUDA;
+    }
+    dev_free(d_idx, s->stream);
+    dev_free(d_out, s->stream);
+    return rc;
+}
+
 int physim_gpu_sim_set_plan(PhysimSim *s, const PhysimDirectTuning *plan)
 {
     PG_CHECK(s && plan, PHYSIM_ERR_ARGUMENT, "null argument");

@@ -123,6 +123,16 @@ class Simulation:
               "physim_gpu_sim_accelerations")
         return out
 
+    def accelerations_f64(self, idx) -> np.ndarray:
+        """The reference's direct-sum accelerations in f64 of the bodies `idx`
+        of the current state (an accuracy reference for every element)."""
+        idx = np.ascontiguousarray(idx, dtype=np.int64)
+        out = np.empty(len(idx), dtype=ACCELERATION)
+        check(lib.physim_gpu_sim_accelerations_f64(self.handle, idx.ctypes.data, len(idx),
+                                                   out.ctypes.data),
+              "physim_gpu_sim_accelerations_f64")
+        return out
+
     def tree_snapshot(self) -> dict:
         """Keys, sort order and tree of the current state (astro/astro2 only)."""
         from ._lib import PhysimTreeSnapshot
