@@ -488,7 +488,10 @@ def measure_bh(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict:
             sim.step(max(args.warmup, 3))
         sim.synchronize()
         dist.barrier()
+        clocks = Clocks(device)
+        clocks.start()
         step_ms, grav_ms = _timed_steps(sim, stream, steps, flush)
+        clk = clocks.stop()
         total = dist.max(sum(step_ms))
         st = sim.bh_stats()
         results[name] = {"steps_per_s": dist.sum(float(steps)) / (total / 1e3),
@@ -498,7 +501,7 @@ def measure_bh(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict:
                          "interactions_per_step": st["interactions"],
                          "node_visits_per_step": st["node_visits"],
                          "gpu_launches": sim.launches_per_step * steps,
-                         "acc_error_vs_f64": err}
+                         "acc_error_vs_f64": err, "clocks": clk}
         sim.close()
     main = results["0.5"]
     bytes_step = sum(BH_BYTES_PER_BODY.values()) * n

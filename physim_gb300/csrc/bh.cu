@@ -1193,21 +1193,21 @@ traverse_warp_kernel(TravArgs a_in)
     int nc = 0;  // queued cells
     const float2 nqx = make_float2(-q.x, -q.x), nqy = make_float2(-q.y, -q.y);
     const float2 nqz = make_float2(-q.z, -q.z), e2 = make_float2(a.e, a.e);
-    auto flush = [&]() {
-        // bodies: entries 2k and 2k + 1 are staged interleaved as
-        // (x, x', y, y')(z, z', m, m'), so two 128-bit loads give the float2
-        // operands of two interactions, which go through packed
-        // FADD2/FMUL2/FFMA2 (an odd count is padded with a massless entry,
-        // which adds exactly zero)
-        // the next tile's bodies are loaded while the current one is evaluated
+    // Evaluates `count` queued interactions whose (x, y, z, m) load(t) gives:
+    // entries 2k and 2k + 1 are staged interleaved as (x, x', y, y')(z, z', m, m'),
+    // so two 128-bit loads give the float2 operands of two interactions, which go
+    // through packed FADD2/FMUL2/FFMA2 (an odd count is padded with a massless
+    // entry, which adds exactly zero); the next tile is loaded while the current
+    // one is evaluated.
+    auto eval_packed = [&](int count, auto load) {
         float4 nb = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (lane < nq) nb = a.sbody[queue[warp][lane]];
-        for (int j0 = 0; j0 < nq; j0 += 32) {
-            const int m = min(32, nq - j0);
+        if (lane < count) nb = load(lane);
+        for (int j0 = 0; j0 < count; j0 += 32) {
+            const int m = min(32, count - j0);
             __syncwarp();
             const float4 bj = nb;
             nb = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (j0 + 32 + lane < nq) nb = a.sbody[queue[warp][j0 + 32 + lane]];
+            if (j0 + 32 + lane < count) nb = load(j0 + 32 + lane);
             float *pl = reinterpret_cast<float *>(&tile[warp][lane & ~1]) + (lane & 1);
             pl[0] = bj.x;
             pl[2] = bj.y;
@@ -1224,24 +1224,27 @@ traverse_warp_kernel(TravArgs a_in)
             ay += sy.x + sy.y;
             az += sz.x + sz.y;
         }
-        for (int j0 = 0; j0 < nc; j0 += 32) {
-            const int m = min(32, nc - j0);
-            __syncwarp();
-            if (lane < m) {
-                const int c = -queue[warp][kGQueue - 1 - (j0 + lane)] - 1;
-                tile[warp][lane] = a.nd.com[c];
-                if (kQuad) {
+    };
+    auto flush = [&]() {
+        // leaf bodies, then accepted cells (monopoles packed like bodies;
+        // with quadrupoles one cell per lane step)
+        eval_packed(nq, [&](int t) { return a.sbody[queue[warp][t]]; });
+        if (!kQuad) {
+            eval_packed(nc, [&](int t) { return a.nd.com[-queue[warp][kGQueue - 1 - t] - 1]; });
+        } else {
+            for (int j0 = 0; j0 < nc; j0 += 32) {
+                const int m = min(32, nc - j0);
+                __syncwarp();
+                if (lane < m) {
+                    const int c = -queue[warp][kGQueue - 1 - (j0 + lane)] - 1;
+                    tile[warp][lane] = a.nd.com[c];
                     tqa[warp][lane] = a.nd.quad_a[c];
                     tqb[warp][lane] = a.nd.quad_b[c];
                 }
-            }
-            __syncwarp();
-            for (int j = 0; j < m; ++j) {
-                if (kQuad)
+                __syncwarp();
+                for (int j = 0; j < m; ++j)
                     cell_quad_acc(q.x, q.y, q.z, tile[warp][j], tqa[warp][j], tqb[warp][j], a.e,
                                   ax, ay, az);
-                else
-                    pair_acc(q.x, q.y, q.z, tile[warp][j], a.e, ax, ay, az);
             }
         }
         pairs += nq + nc;
