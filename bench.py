@@ -66,7 +66,9 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--skip-e2e", action="store_true", help="profiling runs: device path only")
-    p.add_argument("--only", default="", help="comma list of parts: direct, bh, ensemble")
+    p.add_argument("--only", default="",
+                   help="comma list of parts: direct, bh, ensemble, served, precision; tour "
+                        "(every kernel once, for launch lists)")
     p.add_argument("--precision-steps", type=int, default=200)
     p.add_argument("--precision-bodies", type=int, default=262_144)
     p.add_argument("--precision-variants", default="",
@@ -756,6 +758,71 @@ def measure_served(args, dist: Dist, device: int) -> dict:
     return out
 
 
+def measure_tour(args, dist: Dist, device: int) -> dict:
+    """Runs every kernel of the library at least once on small and mid-size
+    states (profiling runs: `--only tour` under an ncu launch list shows each
+    kernel's device time).  Returns the paths run."""
+    import physim_gb300 as pg
+    from physim_gb300 import ics, initialisers
+
+    paths = []
+    cube = ics.cube_with_stars(65536, seed=1, stars=ics.STARS_4)
+    small = ics.cube_with_stars(4096, seed=2, stars=ics.STARS_2)
+    # direct sums: each pair once + verlet; one-pair kernels with euler and rk4
+    with pg.Simulation(cube, pg.SimConfig(gravity="simple_astro", e=E, dt=DT,
+                                          device=device)) as sim:
+        sim.step(2)
+        sim.diagnostics(potential=True)
+        sim.accelerations()
+        sim.accelerations_f64(np.arange(64))
+        sim.download()
+    paths.append("simple_astro 65,536 each pair once + verlet, diagnostics, f64 sample")
+    for integ in ("euler", "rk4"):
+        with pg.Simulation(small, pg.SimConfig(gravity="simple_astro", e=E, dt=DT,
+                                               integrator=integ, device=device)) as sim:
+            sim.step(1)
+    paths.append("simple_astro 4,098 one-pair kernels + euler, rk4")
+    # Barnes-Hut: warp traversal (monopole, quadrupole), exact traversal, quadtree
+    big = ics.workload_large(262_144)
+    for cfg in (dict(gravity="astro2", theta=0.5, leaf_size=16, traversal="warp"),
+                dict(gravity="astro2", theta=0.5, leaf_size=16, traversal="warp",
+                     quadrupole=True, com_theta=0.6),
+                dict(gravity="astro2", theta=0.5, leaf_size=1, traversal="exact"),
+                dict(gravity="astro", theta=0.5, leaf_size=16, traversal="warp")):
+        with pg.Simulation(big, pg.SimConfig(e=E, dt=DT, device=device, **cfg)) as sim:
+            sim.step(2)
+        paths.append(" ".join(f"{k}={v}" for k, v in cfg.items()))
+    # host arrays: the plugin transform + verlet, in place and with copies
+    for mode in ("direct", "copy"):
+        if mode == "direct" and pg.host_access(device) != "direct":
+            continue
+        pg.set_host_access(mode)
+        el = pg.TransformElementHandler("simple_astro", {"e": E, "device": device})
+        acc = pg.accelerations(len(small))
+        el.transform(small, acc)
+        pg.GpuVerlet(device).integrate(small, acc, DT)
+        el.destroy()
+        paths.append(f"plugin simple_astro + verlet, host access {mode}")
+    pg.set_host_access("auto")
+    for kind in ("euler", "rk4"):
+        el = pg.TransformElementHandler("astro2", {"e": E, "theta": 0.5, "device": device})
+        pg.GpuIntegrator(kind, device).integrate(small, lambda st, ac: el.transform(st, ac), DT)
+        el.destroy()
+    paths.append("host-array euler, rk4 with an astro2 acc_fn")
+    # ensemble with members on both kinds of units
+    members = [ics.plummer(n, seed=n, a=0.1) for n in (300, 2048, 9000, 20000)]
+    with pg.Ensemble(members, pg.SimConfig(gravity="simple_astro", e=E, dt=DT,
+                                           device=device)) as ens:
+        ens.step(2)
+        ens.download(0)
+    paths.append("ensemble of 4 members (one-pair and each-pair-once units)")
+    # device initialisers
+    initialisers.cube({"n": 10_000, "seed": 3}, device)
+    initialisers.plummer({"n": 10_000, "seed": 4}, device)
+    paths.append("cube and plummer initialisers")
+    return {"metric": "kernel tour", "value": len(paths), "unit": "paths", "paths": paths}
+
+
 def run_ours(args, dist: Dist):
     device, sms = _device_context(dist)
     peaks = measured_peaks()
@@ -766,7 +833,11 @@ def run_ours(args, dist: Dist):
     ens = measure_ensemble(args, dist, device) if "ensemble" in parts else None
     served = measure_served(args, dist, device) if "served" in parts else None
     precision = measure_precision(args, dist, device) if "precision" in parts else None
+    tour = measure_tour(args, dist, device) if "tour" in parts else None
     if dist.rank != 0:
+        return
+    if tour and not (direct or bh or ens or served or precision):
+        print(json.dumps({**tour, "higher_is_better": True}), flush=True)
         return
     if precision and not (direct or bh or ens or served):
         print(json.dumps({"metric": "precision study (RMS relative acceleration error)",
