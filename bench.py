@@ -78,6 +78,11 @@ def parse():
                    help="admission order of the served run (the one-at-a-time baselines run "
                         "both orders)")
     p.add_argument("--serve-drain", type=float, default=30.0)
+    p.add_argument("--serve-scheduling", choices=["srpt", "all"], default="all",
+                   help="tick scheduling of the served run: shortest remaining work first "
+                        "within an in-flight budget, or every admitted unit at once")
+    p.add_argument("--serve-inflight-ms", type=float, default=30.0,
+                   help="estimated device work kept in flight under srpt scheduling")
     p.add_argument("--ens-steps", type=int, default=200)
     p.add_argument("--ens-members", type=int, default=512)
     p.add_argument("--bh-steps", type=int, default=1000)
@@ -728,7 +733,8 @@ def measure_served(args, dist: Dist, device: int) -> dict:
     until = args.serve_seconds + args.serve_drain
     jobs = served_mix(rate=50.0, seconds=args.serve_seconds, seed=5)
     served = _serve_once(jobs, GpuExecutor(device=device, tick_ms=25.0, download=True), until,
-                         admission=args.serve_admission)
+                         admission=args.serve_admission, scheduling=args.serve_scheduling,
+                         inflight_seconds=args.serve_inflight_ms / 1e3)
     plain_fifo = _serve_once(served_mix(rate=50.0, seconds=args.serve_seconds, seed=5),
                              PlainExecutor(device=device, download=True), until, max_units=1,
                              max_batch=1, admission="fifo")

@@ -120,6 +120,13 @@ class Unit:
 
     jobs: list[JobSpec]
     tick_steps: int = 0  # job-steps enqueued by the last launch_tick
+    tick_seconds: float = 0.0  # estimated device seconds of the last launched tick
+    in_flight: bool = False  # a launched tick has not completed yet
+
+    def remaining_seconds(self) -> float:
+        """Estimated device seconds of the unit's unfinished steps (used to
+        order ticks under shortest-remaining-work scheduling)."""
+        return 0.0
 
     def launch_tick(self) -> None: ...
 
@@ -253,13 +260,18 @@ class _EnsembleUnit(Unit):
         self.host_left = [j.steps for j in jobs]  # host-side count for step accounting
         self.tick_steps = 0
 
+    def remaining_seconds(self) -> float:
+        return sum(r * j.step_seconds() for r, j in zip(self.host_left, self.jobs))
+
     def launch_tick(self) -> None:
         self.ens.step(self.k)
         self.tick_steps = 0
+        self.tick_seconds = 0.0
         for i, r in enumerate(self.host_left):
             t = min(self.k, r)
             self.host_left[i] = r - t
             self.tick_steps += t
+            self.tick_seconds += t * self.jobs[i].step_seconds()
         self.tick.record()
 
     def tick_done(self) -> bool:
@@ -322,10 +334,16 @@ class _PoolUnit(Unit):
             self.slot_job[k] = j
             self.slot_left[k] = j.steps
 
+    def remaining_seconds(self) -> float:
+        return (sum(self.slot_left[k] * j.step_seconds()
+                    for k, j in enumerate(self.slot_job) if j is not None) +
+                sum(j.work_seconds() for j in self.waiting))
+
     def launch_tick(self) -> None:
         self._fill()
         active = [k for k, j in enumerate(self.slot_job) if j is not None and self.slot_left[k]]
         self.tick_steps = 0
+        self.tick_seconds = 0.0
         if active:
             est_ms = sum(self.slot_job[k].n ** 2 for k in active) / 2.0e12 * 1e3 + 0.02
             steps = int(max(1, min(max(self.slot_left[k] for k in active),
@@ -335,6 +353,7 @@ class _PoolUnit(Unit):
                 t = min(steps, self.slot_left[k])
                 self.slot_left[k] -= t
                 self.tick_steps += t
+                self.tick_seconds += t * self.slot_job[k].step_seconds()
         self.tick.record()
 
     def tick_done(self) -> bool:
@@ -383,12 +402,16 @@ class _SimUnit(Unit):
         self.reported = False
         self.tick_steps = 0
 
+    def remaining_seconds(self) -> float:
+        return self.left * self.jobs[0].step_seconds()
+
     def launch_tick(self) -> None:
         k = min(self.k_full, self.left)
         if k > 0:
             self.sim.step(k)
             self.left -= k
         self.tick_steps = k
+        self.tick_seconds = k * self.jobs[0].step_seconds()
         self.tick.record()
 
     def tick_done(self) -> bool:
@@ -416,10 +439,22 @@ class Server:
     def __init__(self, executor: Executor, hbm_budget: int = 150 << 30,
                  clock: Callable[[], float] = time.perf_counter,
                  max_units: int = 64, max_batch: int = 16, keep_states: bool = False,
-                 admission: str = "fifo"):
+                 admission: str = "fifo", scheduling: str = "all",
+                 inflight_seconds: float = 0.03):
         if admission not in ("fifo", "shortest"):
             raise ValueError(f"unknown admission policy {admission!r}")
+        if scheduling not in ("all", "srpt"):
+            raise ValueError(f"unknown scheduling policy {scheduling!r}")
         self.admission = admission
+        # "all": every admitted unit keeps one tick in flight, so all of them
+        # share the GPU.  "srpt": ticks are handed out in order of the units'
+        # estimated remaining device work, only while the estimated device
+        # work already in flight is below `inflight_seconds` (at least one
+        # tick is always in flight): a long job's next tick waits while
+        # shorter ones run, small launch-bound units still overlap, and the
+        # preemption point is the end of a tick.
+        self.scheduling = scheduling
+        self.inflight_seconds = inflight_seconds
         self.executor = executor
         self.max_batch = max_batch
         self.keep_states = keep_states
@@ -491,12 +526,9 @@ class Server:
                     self.in_use -= j.device_bytes()
                 return
             for u in units:
-                try:
-                    u.launch_tick()
-                    self.units.append(u)
-                except Exception as err:  # noqa: BLE001
-                    self._fail_unit(u, err)
-            self.max_running = max(self.max_running, len(self.units))
+                u.in_flight = False
+                self.units.append(u)
+            self._dispatch()
 
     def _fail_unit(self, u: Unit, err: BaseException) -> None:
         """A unit whose device work raised: its unfinished jobs fail, their
@@ -512,29 +544,58 @@ class Server:
         except Exception:
             pass
 
+    def _launch(self, u: Unit) -> bool:
+        try:
+            u.launch_tick()
+            u.in_flight = True
+            return True
+        except Exception as err:  # noqa: BLE001 -- isolate the failing unit
+            self._fail_unit(u, err)
+            self.units.remove(u)
+            return False
+
+    def _dispatch(self) -> None:
+        """Hands out ticks to the units that have none in flight."""
+        idle = [u for u in self.units if not u.in_flight]
+        if self.scheduling == "all":
+            for u in idle:
+                self._launch(u)
+        else:
+            busy = [u for u in self.units if u.in_flight]
+            inflight = sum(u.tick_seconds for u in busy)
+            for u in sorted(idle, key=lambda v: v.remaining_seconds()):
+                if busy and inflight >= self.inflight_seconds:
+                    break
+                if self._launch(u):
+                    busy.append(u)
+                    inflight += u.tick_seconds
+        self.max_running = max(self.max_running, sum(1 for u in self.units if u.in_flight))
+
     def _service(self, now: float) -> None:
         still = []
         for u in self.units:
             try:
-                if not u.tick_done():
-                    still.append(u)
-                    continue
-                self.steps_executed += u.tick_steps
-                u.tick_steps = 0
-                for j, state in u.finished_jobs():
-                    t = self.clock() - self.t0
-                    self.results.append(JobResult(j, self.admitted_at[j.id], t,
-                                                  state if self.keep_states else None))
-                    self.in_use -= j.device_bytes()
-                    self.steps_done += j.steps
+                if u.in_flight:
+                    if not u.tick_done():
+                        still.append(u)
+                        continue
+                    u.in_flight = False
+                    self.steps_executed += u.tick_steps
+                    u.tick_steps = 0
+                    for j, state in u.finished_jobs():
+                        t = self.clock() - self.t0
+                        self.results.append(JobResult(j, self.admitted_at[j.id], t,
+                                                      state if self.keep_states else None))
+                        self.in_use -= j.device_bytes()
+                        self.steps_done += j.steps
                 if u.alive():
-                    u.launch_tick()
                     still.append(u)
                 else:
                     u.close()
             except Exception as err:  # noqa: BLE001 -- isolate the failing unit
                 self._fail_unit(u, err)
         self.units = still
+        self._dispatch()
 
     def run(self, until: float | None = None, poll: float = 0.001,
             sample_every: float = 0.25) -> list[JobResult]:

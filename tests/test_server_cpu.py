@@ -186,3 +186,63 @@ def test_shortest_job_first_admission():
         assert [b[0] for b in ex.batches] == want, policy
     with pytest.raises(ValueError):
         Server(FakeExecutor(), admission="random")
+
+
+class TimedUnit(FakeUnit):
+    """A fake unit whose tick takes three polls and whose work is estimated
+    at 1 ms per job-step."""
+
+    def __init__(self, jobs, ex):
+        super().__init__(jobs, ex)
+        self.polls = 0
+
+    def launch_tick(self):
+        super().launch_tick()
+        self.tick_seconds = self.tick_steps * 1e-3
+        self.polls = 0
+        self.ex.launches.append(self.jobs[0].id)
+
+    def tick_done(self):
+        self.polls += 1
+        return self.polls >= 3
+
+    def remaining_seconds(self):
+        return sum(self.left.values()) * 1e-3
+
+
+class TimedExecutor(FakeExecutor):
+    def __init__(self, k=10):
+        super().__init__(k=k)
+        self.launches = []
+
+    def make_units(self, jobs):
+        return [TimedUnit([j], self) for j in jobs]
+
+
+@pytest.mark.parametrize("scheduling", ["all", "srpt"])
+def test_shortest_remaining_work_scheduling(scheduling):
+    """Under "srpt" a short job that arrives while a long one runs gets the
+    GPU at the long job's next tick boundary, and the two never have ticks in
+    flight together (each tick's estimated work fills the in-flight budget);
+    under "all" both keep a tick in flight."""
+    ex = TimedExecutor(k=10)
+    srv = Server(ex, hbm_budget=1 << 40, scheduling=scheduling, inflight_seconds=0.005,
+                 admission="shortest")
+    long_job, short_job = job(0, 1000, 400, t=0.0), job(1, 1000, 30, t=0.02)
+    srv.submit([long_job, short_job])
+    res = srv.run(until=60.0)
+    done = {r.spec.id: r.finished for r in res}
+    assert set(done) == {0, 1} and done[1] < done[0]
+    assert srv.steps_executed == 430
+    if scheduling == "srpt":
+        assert srv.max_running == 1
+        # once the short job is admitted, its 3 ticks run back to back
+        first = ex.launches.index(1)
+        assert ex.launches[first:first + 3] == [1, 1, 1]
+    else:
+        assert srv.max_running == 2
+
+
+def test_unknown_scheduling_policy():
+    with pytest.raises(ValueError):
+        Server(FakeExecutor(), scheduling="lifo")
