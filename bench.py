@@ -83,6 +83,10 @@ def parse():
                         "within an in-flight budget, or every admitted unit at once")
     p.add_argument("--serve-inflight-ms", type=float, default=30.0,
                    help="estimated device work kept in flight under srpt scheduling")
+    p.add_argument("--serve-max-units", type=int, default=8,
+                   help="most units (ensembles, simulations) admitted at one time")
+    p.add_argument("--serve-async-admission", type=int, default=1,
+                   help="build admitted jobs' units on a worker thread (1) or inline (0)")
     p.add_argument("--ens-steps", type=int, default=200)
     p.add_argument("--ens-members", type=int, default=512)
     p.add_argument("--bh-steps", type=int, default=1000)
@@ -734,7 +738,9 @@ def measure_served(args, dist: Dist, device: int) -> dict:
     jobs = served_mix(rate=50.0, seconds=args.serve_seconds, seed=5)
     served = _serve_once(jobs, GpuExecutor(device=device, tick_ms=25.0, download=True), until,
                          admission=args.serve_admission, scheduling=args.serve_scheduling,
-                         inflight_seconds=args.serve_inflight_ms / 1e3)
+                         inflight_seconds=args.serve_inflight_ms / 1e3,
+                         async_admission=bool(args.serve_async_admission),
+                         max_units=args.serve_max_units)
     plain_fifo = _serve_once(served_mix(rate=50.0, seconds=args.serve_seconds, seed=5),
                              PlainExecutor(device=device, download=True), until, max_units=1,
                              max_batch=1, admission="fifo")
@@ -746,9 +752,12 @@ def measure_served(args, dist: Dist, device: int) -> dict:
     out = {"metric": "served-mix job latency (arrival to final state on the host)",
            "admission": ("shortest job first (estimated device work)"
                          if args.serve_admission == "shortest" else "arrival order")
-                        + ", HBM budget 150 GB, at most 64 units (one ensemble per admission "
-                          "round of direct-sum jobs, one simulation per Barnes-Hut job, each on "
-                          "its own stream)",
+                        + f", HBM budget 150 GB, at most {args.serve_max_units} units (one "
+                          "ensemble per admission round of direct-sum jobs, one simulation per "
+                          "Barnes-Hut job, each on its own stream)"
+                        + (", units built on a worker thread" if args.serve_async_admission
+                           else ""),
+           "scheduling": args.serve_scheduling,
            "jobs_arrived": len(jobs), "arrival_seconds": args.serve_seconds,
            "drain_seconds": args.serve_drain, "offered_direct_pairs": offered_direct}
     out.update(served)

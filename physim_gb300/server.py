@@ -21,6 +21,7 @@ scheduling logic can be exercised without a GPU (tests use a fake executor).
 from __future__ import annotations
 
 import collections
+import concurrent.futures
 import heapq
 import math
 import threading
@@ -440,7 +441,7 @@ class Server:
                  clock: Callable[[], float] = time.perf_counter,
                  max_units: int = 64, max_batch: int = 16, keep_states: bool = False,
                  admission: str = "fifo", scheduling: str = "all",
-                 inflight_seconds: float = 0.03):
+                 inflight_seconds: float = 0.03, async_admission: bool = False):
         if admission not in ("fifo", "shortest"):
             raise ValueError(f"unknown admission policy {admission!r}")
         if scheduling not in ("all", "srpt"):
@@ -455,6 +456,12 @@ class Server:
         # preemption point is the end of a tick.
         self.scheduling = scheduling
         self.inflight_seconds = inflight_seconds
+        # async_admission: admitted jobs' units (initial states, device
+        # allocations, uploads) are built on a worker thread, so the loop
+        # that hands out ticks never waits for them
+        self._builder = (concurrent.futures.ThreadPoolExecutor(max_workers=1)
+                         if async_admission else None)
+        self._building: list[tuple[concurrent.futures.Future, list[JobSpec], int]] = []
         self.executor = executor
         self.max_batch = max_batch
         self.keep_states = keep_states
@@ -499,7 +506,7 @@ class Server:
                 sorted(self.pending, key=lambda j: (j.work_seconds(), j.arrival, j.id)))
         keep = collections.deque()
         room = self.budget - self.in_use
-        new_units = 0
+        new_units = sum(c for _, _, c in self._building)
         cost = getattr(self.executor, "unit_cost", lambda job: 1)
         while self.pending:
             j = self.pending.popleft()
@@ -517,18 +524,43 @@ class Server:
             for j in batch:
                 self.admitted_at[j.id] = now
                 self.in_use += j.device_bytes()
+            if self._builder is not None:
+                cost_new = new_units - sum(c for _, _, c in self._building)
+                self._building.append((self._builder.submit(self.executor.make_units, batch),
+                                       batch, cost_new))
+                return
             try:
                 units = self.executor.make_units(batch)
             except Exception as err:  # noqa: BLE001 -- e.g. device out of memory
-                t = self.clock() - self.t0
-                for j in batch:
-                    self.failed.append(JobResult(j, now, t, None, repr(err)))
-                    self.in_use -= j.device_bytes()
+                self._fail_batch(batch, err)
                 return
             for u in units:
                 u.in_flight = False
                 self.units.append(u)
             self._dispatch()
+
+    def _fail_batch(self, batch: list[JobSpec], err: BaseException) -> None:
+        t = self.clock() - self.t0
+        for j in batch:
+            self.failed.append(JobResult(j, self.admitted_at.get(j.id, t), t, None, repr(err)))
+            self.in_use -= j.device_bytes()
+
+    def _collect_built(self) -> None:
+        """Units whose building finished join the running set."""
+        still = []
+        for fut, batch, c in self._building:
+            if not fut.done():
+                still.append((fut, batch, c))
+                continue
+            try:
+                units = fut.result()
+            except Exception as err:  # noqa: BLE001 -- e.g. device out of memory
+                self._fail_batch(batch, err)
+                continue
+            for u in units:
+                u.in_flight = False
+                self.units.append(u)
+        self._building = still
 
     def _fail_unit(self, u: Unit, err: BaseException) -> None:
         """A unit whose device work raised: its unfinished jobs fail, their
@@ -572,6 +604,8 @@ class Server:
         self.max_running = max(self.max_running, sum(1 for u in self.units if u.in_flight))
 
     def _service(self, now: float) -> None:
+        if self._building:
+            self._collect_built()
         still = []
         for u in self.units:
             try:
@@ -613,7 +647,7 @@ class Server:
             if now >= next_sample:
                 self.queue_depth.append((now, len(self.pending), len(self.units), self.in_use))
                 next_sample = now + sample_every
-            if not self.units and not self.pending and not self.arrivals:
+            if not self.units and not self.pending and not self.arrivals and not self._building:
                 break
             time.sleep(poll)
         return self.results
@@ -621,9 +655,19 @@ class Server:
     def unfinished(self) -> int:
         done_ids = {r.spec.id for r in self.results} | {f.spec.id for f in self.failed}
         running = sum(1 for u in self.units for j in u.jobs if j.id not in done_ids)
-        return running + len(self.pending) + len(self.arrivals)
+        building = sum(len(b) for _, b, _ in self._building)
+        return running + building + len(self.pending) + len(self.arrivals)
 
     def close(self) -> None:
+        if self._builder is not None:
+            self._builder.shutdown(wait=True)
+            for fut, _, _ in self._building:
+                try:
+                    for u in fut.result():
+                        u.close()
+                except Exception:  # noqa: BLE001 -- its jobs are already unfinished
+                    pass
+            self._building = []
         for u in self.units:
             u.close()
         self.units = []

@@ -246,3 +246,32 @@ def test_shortest_remaining_work_scheduling(scheduling):
 def test_unknown_scheduling_policy():
     with pytest.raises(ValueError):
         Server(FakeExecutor(), scheduling="lifo")
+
+
+class SlowBuildExecutor(TimedExecutor):
+    """Builds units slowly (as large initial states do) and fails one job's
+    build."""
+
+    def make_units(self, jobs):
+        import time
+        time.sleep(0.02)
+        if any(j.id == 3 for j in jobs):
+            raise RuntimeError("injected build failure")
+        return super().make_units(jobs)
+
+
+@pytest.mark.parametrize("scheduling", ["all", "srpt"])
+def test_async_admission(scheduling):
+    """Units built on a worker thread: every job completes or fails once, the
+    memory budget returns to zero, and a failed build fails only its batch."""
+    ex = SlowBuildExecutor(k=10)
+    srv = Server(ex, hbm_budget=1 << 40, scheduling=scheduling, async_admission=True,
+                 max_batch=1)
+    jobs = [job(i, 1000 + i, 20 + 10 * i, t=0.005 * i) for i in range(8)]
+    srv.submit(jobs)
+    res = srv.run(until=60.0)
+    srv.close()
+    assert sorted(r.spec.id for r in res) == [0, 1, 2, 4, 5, 6, 7]
+    assert [f.spec.id for f in srv.failed] == [3]
+    assert srv.unfinished() == 0 and srv.in_use == 0
+    assert srv.steps_executed == sum(j.steps for j in jobs if j.id != 3)
