@@ -22,7 +22,12 @@ def _alone(spec):
         return sim.download()
 
 
-def test_mix_equals_alone():
+@pytest.mark.parametrize("policy", [{}, {"async_admission": True},
+                                    {"async_admission": True, "scheduling": "srpt",
+                                     "inflight_seconds": 0.01}])
+def test_mix_equals_alone(policy):
+    """Also with units built on a worker thread while others run, and with
+    shortest-remaining-work tick scheduling."""
     from physim_gb300.server import GpuExecutor, JobSpec, Server
     from test_verlet_gpu import trajectory_errors
     from physim_gb300.server import initial_state
@@ -35,12 +40,14 @@ def test_mix_equals_alone():
                         seed=510))
     jobs.append(JobSpec(arrival=0.004, id=11, n=60_000, steps=15, gravity="astro2", theta=1.0,
                         seed=511, ic="plummer"))
-    srv = Server(GpuExecutor(tick_ms=2.0), hbm_budget=8 << 30, keep_states=True)
+    srv = Server(GpuExecutor(tick_ms=2.0), hbm_budget=8 << 30, keep_states=True, **policy)
     srv.submit(jobs)
     res = srv.run(until=300.0)
+    srv.close()
     assert not srv.failed and srv.unfinished() == 0
     assert sorted(r.spec.id for r in res) == sorted(j.id for j in jobs)
-    assert srv.max_running >= 2  # units overlapping on the device
+    if policy.get("scheduling", "all") == "all":
+        assert srv.max_running >= 2  # units overlapping on the device
     for r in res:
         alone = _alone(r.spec)
         if r.spec.gravity == "astro2":
