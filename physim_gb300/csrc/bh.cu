@@ -984,6 +984,43 @@ __device__ __forceinline__ void cell_quad_acc(float qx, float qy, float qz, floa
     az = fmaf(h, sdz, fmaf(k, dz, az));
 }
 
+// Two cells' monopole + quadrupole terms for one body (nq = -position) with
+// the cells' (x, y, z, m) and second moments given as float2 planes, through
+// packed FP32 instructions; the arithmetic of each lane is that of
+// cell_quad_acc.
+__device__ __forceinline__ void cell_quad_acc2(float2 nqx, float2 nqy, float2 nqz, float2 cx,
+                                               float2 cy, float2 cz, float2 cm, float2 qax,
+                                               float2 qay, float2 qaz, float2 qaw, float2 qbx,
+                                               float2 qby, float2 qbz, float2 e2, float2 &ax,
+                                               float2 &ay, float2 &az)
+{
+    const float2 dx = add2(cx, nqx), dy = add2(cy, nqy), dz = add2(cz, nqz);
+    float2 r2 = mul2(dz, dz);
+    r2 = fma2(dy, dy, r2);
+    r2 = fma2(dx, dx, r2);
+    const float2 w = add2(r2, e2);
+    const float2 arg = fma2(r2, mul2(w, w), make_float2(kPairGuard, kPairGuard));
+    const float2 iu = make_float2(rsqrt_approx(arg.x), rsqrt_approx(arg.y));
+    const float2 s = mul2(cm, iu);
+    float2 ir = mul2(iu, w);
+    ir.x = r2.x > 1e-30f ? ir.x : 0.f;  // no quadrupole term at r = 0
+    ir.y = r2.y > 1e-30f ? ir.y : 0.f;
+    const float2 A = fma2(make_float2(3.f, 3.f), r2, e2);
+    const float2 base = mul2(mul2(ir, iu), iu);
+    const float2 h = mul2(make_float2(-A.x, -A.y), base);
+    const float2 hp =
+        mul2(base, fma2(A, fma2(mul2(make_float2(2.f, 2.f), A), mul2(iu, ir), mul2(ir, ir)),
+                        make_float2(-6.f, -6.f)));
+    const float2 sdx = fma2(qax, dx, fma2(qbx, dy, mul2(qby, dz)));
+    const float2 sdy = fma2(qbx, dx, fma2(qay, dy, mul2(qbz, dz)));
+    const float2 sdz = fma2(qby, dx, fma2(qbz, dy, mul2(qaz, dz)));
+    const float2 dsd = fma2(dx, sdx, fma2(dy, sdy, mul2(dz, sdz)));
+    const float2 k = fma2(make_float2(0.5f, 0.5f), fma2(h, qaw, mul2(hp, dsd)), s);
+    ax = fma2(h, sdx, fma2(k, dx, ax));
+    ay = fma2(h, sdy, fma2(k, dy, ay));
+    az = fma2(h, sdz, fma2(k, dz, az));
+}
+
 // The centre-of-mass guard for one body: b_max < com_theta |x - c|.
 __device__ __forceinline__ bool com_guard(const TravArgs &a, float4 geo, float4 c, float qx,
                                           float qy, float qz)
@@ -1232,19 +1269,41 @@ traverse_warp_kernel(TravArgs a_in)
         if (!kQuad) {
             eval_packed(nc, [&](int t) { return a.nd.com[-queue[warp][kGQueue - 1 - t] - 1]; });
         } else {
+            // cells with quadrupoles, two per packed instruction: centre of
+            // mass and both moment vectors staged interleaved like bodies
             for (int j0 = 0; j0 < nc; j0 += 32) {
                 const int m = min(32, nc - j0);
                 __syncwarp();
+                float4 c4 = make_float4(0.f, 0.f, 0.f, 0.f), qa = c4, qb = c4;
                 if (lane < m) {
                     const int c = -queue[warp][kGQueue - 1 - (j0 + lane)] - 1;
-                    tile[warp][lane] = a.nd.com[c];
-                    tqa[warp][lane] = a.nd.quad_a[c];
-                    tqb[warp][lane] = a.nd.quad_b[c];
+                    c4 = a.nd.com[c];
+                    qa = a.nd.quad_a[c];
+                    qb = a.nd.quad_b[c];
                 }
+                const int slot = lane & ~1, half = lane & 1;
+                float *pc = reinterpret_cast<float *>(&tile[warp][slot]) + half;
+                float *pa = reinterpret_cast<float *>(&tqa[warp][slot]) + half;
+                float *pb = reinterpret_cast<float *>(&tqb[warp][slot]) + half;
+                pc[0] = c4.x; pc[2] = c4.y; pc[4] = c4.z; pc[6] = c4.w;
+                pa[0] = qa.x; pa[2] = qa.y; pa[4] = qa.z; pa[6] = qa.w;
+                pb[0] = qb.x; pb[2] = qb.y; pb[4] = qb.z; pb[6] = qb.w;
                 __syncwarp();
-                for (int j = 0; j < m; ++j)
-                    cell_quad_acc(q.x, q.y, q.z, tile[warp][j], tqa[warp][j], tqb[warp][j], a.e,
-                                  ax, ay, az);
+                float2 sx = make_float2(0.f, 0.f), sy = sx, sz = sx;
+                for (int jj = 0; jj < (m + 1) >> 1; ++jj) {
+                    const float4 C0 = tile[warp][2 * jj], C1 = tile[warp][2 * jj + 1];
+                    const float4 A0 = tqa[warp][2 * jj], A1 = tqa[warp][2 * jj + 1];
+                    const float4 B0 = tqb[warp][2 * jj], B1 = tqb[warp][2 * jj + 1];
+                    cell_quad_acc2(nqx, nqy, nqz, make_float2(C0.x, C0.y), make_float2(C0.z, C0.w),
+                                   make_float2(C1.x, C1.y), make_float2(C1.z, C1.w),
+                                   make_float2(A0.x, A0.y), make_float2(A0.z, A0.w),
+                                   make_float2(A1.x, A1.y), make_float2(A1.z, A1.w),
+                                   make_float2(B0.x, B0.y), make_float2(B0.z, B0.w),
+                                   make_float2(B1.x, B1.y), e2, sx, sy, sz);
+                }
+                ax += sx.x + sx.y;
+                ay += sy.x + sy.y;
+                az += sz.x + sz.y;
             }
         }
         pairs += nq + nc;
