@@ -136,7 +136,7 @@ void set_callback_target(void *target);
  *
  *  init(json, len): a JSON object (not NUL-terminated).  Keys read:
  *    theta  (astro, astro2; default 1.0), e (all; absolute value; default 1.0)
- *  and, for this build only (ignored by the reference, so TOML stays valid):
+ *  and, for this library only (ignored by the reference, so TOML stays valid):
  *    leaf_size  (astro, astro2; bodies per tree leaf, 1..64; default 1 = the
  *                reference's tree)
  *    traversal  ("exact": each body uses its own reference interaction list,

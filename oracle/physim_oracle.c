@@ -694,7 +694,7 @@ int oracle_run_pipeline(Entity *state, size_t n, int element, double theta, doub
     return oracle_run_pipeline_with(state, n, element, 0, theta, e, dt, steps, threads);
 }
 
-/* Number of OpenMP threads this build would use (1 without OpenMP). */
+/* Number of OpenMP threads the oracle library uses (1 without OpenMP). */
 int oracle_max_threads(void)
 {
 #ifdef _OPENMP

@@ -105,10 +105,9 @@ def test_upload_restarts_with_taylor_step(oracle_mod):
 
 @pytest.mark.parametrize("dt", [1e-5, 3.0e-7, 1.0 / 3.0, 0.1, 2.0 ** -20])
 def test_gpu_verlet_division_bit_identical(oracle_mod, dt):
-    """The velocity (x' - x) / dt of the regular step uses an FMA-corrected
-    reciprocal with an exact-remainder check; it must round exactly as the
-    reference's division does, including zeros, tiny and huge differences
-    and non-finite values."""
+    """The velocity (x' - x) / dt of the regular step (a correctly rounded
+    f64 division on the GPU) must round exactly as the reference's division
+    does, including zeros, tiny and huge differences and non-finite values."""
     import physim_gb300 as pg
     from physim_gb300.entity import entities
     rng = np.random.default_rng(int(dt * 1e9) % 1000)
