@@ -13,14 +13,14 @@
 // kernels, so this is up to 1.53x the interactions per second.
 //
 // Schedule.  Bodies form tiles of 1,024 (the body padding unit); one block
-// evaluates one tile pair (I, J), I <= J, of the T(T+1)/2.  Its 4 warps hold
-// the 1,024 bodies of tile I in registers (8 per thread, as 4 packed FFMA2
-// pairs).  A warp takes the bodies of tile J 32 at a time, one per lane, and
+// evaluates one tile pair (I, J), I <= J, of the T(T+1)/2.  Its 2 warps hold
+// the 1,024 bodies of tile I in registers (16 per thread, as 8 packed FFMA2
+// pairs, so each rotation of the travelling bodies serves 16 pairs).  A warp takes the bodies of tile J 32 at a time, one per lane, and
 // rotates them through its lanes with shuffles: after 32 steps every lane's
 // 8 bodies have met all 32, and each travelling body's accumulated reaction
 // (a float2: the two halves of the packed pairs) is back at its home lane.
 // a_i stays in registers for the whole tile; each warp writes its a_j sums
-// for the tile to its own slice of shared memory, and the block adds the 4
+// for the tile to its own slice of shared memory, and the block adds the 2
 // slices in a fixed order.  The diagonal tile pair (I, I) evaluates all
 // ordered pairs of the tile and updates a_i only (a body meets itself with
 // d = 0, which contributes 0 through the r^2 guard).
@@ -44,8 +44,9 @@ namespace pg {
 
 namespace {
 
-// 3 blocks per SM: room for 170 registers, which the 4-step unroll uses (measured
-// 1% faster than 4 blocks of at most 128 registers)
+// 64 threads of up to 255 registers (about 250 used); measured on GB300 at
+// 1,048,580 bodies: 274.5 ms per pass, against 300.9 ms for 4 warps of 8
+// bodies per thread on the same GPU (the shuffles per pair halve)
 __global__ void __launch_bounds__(kSymThreads, 3)
 direct_sym_kernel(const float4 *__restrict__ body, int n, float e, float *__restrict__ P)
 {
@@ -82,7 +83,7 @@ __global__ void sym_reduce_kernel(const float *__restrict__ P, long long n3, int
 
 DirectPlan make_symmetric_plan(int n)
 {
-    // Three 48 KB blocks per SM need the largest shared-memory carveout.  Set
+    // Blocks of 24 KB of shared memory: the largest carveout keeps them all resident.  Set
     // here, when a plan is made (never inside a stream capture), per device.
     static std::atomic<bool> carveout_set[64];
     int device = 0;

@@ -10,9 +10,9 @@
 
 namespace pg {
 
-constexpr int kSymWarps = 4;
+constexpr int kSymWarps = 2;
 constexpr int kSymThreads = kSymWarps * 32;
-constexpr int kSymIpt = 8;                          // bodies of tile I per thread
+constexpr int kSymIpt = 16;                         // bodies of tile I per thread
 constexpr int kSymTile = kSymThreads * kSymIpt;     // 1,024
 constexpr int kSymGroups = kSymTile / 32;           // groups of 32 bodies of tile J
 static_assert(kSymTile == kBodyPad, "tiles are whole units of the body padding");
@@ -62,7 +62,7 @@ __device__ __forceinline__ void sym_tile_pair(const float4 *__restrict__ body, i
         if (g + 1 < kSymGroups) next = body[J * kSymTile + (g + 1) * 32 + lane];
         float xj = bj.x, yj = bj.y, zj = bj.z, mj = bj.w;
         float2 jx = make_float2(0.f, 0.f), jy = jx, jz = jx;
-#pragma unroll 4
+#pragma unroll 2
         for (int k = 0; k < 32; ++k) {
             const float2 xj2 = make_float2(xj, xj);
             const float2 yj2 = make_float2(yj, yj);
