@@ -56,7 +56,6 @@ constexpr int kMaxLevels = 31;
 
 constexpr int kTravWarps = 4;
 constexpr int kStack = 192;
-constexpr int kBuf = 128;
 
 // flags[0]: node capacity exceeded (tree truncated; results stay exact)
 // flags[1]: traversal stack overflow (results of the affected warp invalid)
@@ -958,36 +957,11 @@ __device__ __forceinline__ void quad_acc(float qx, float qy, float qz, float4 c,
     az = fmaf(h, sdz, fmaf(k, dz, az));
 }
 
-// Monopole + quadrupole of one accepted cell, sharing the one reciprocal
-// square root: 1/sqrt(r^2 (r^2 + e)^2) = 1/u, and 1/r = (r^2 + e)/u.
-__device__ __forceinline__ void cell_quad_acc(float qx, float qy, float qz, float4 c, float4 qa,
-                                              float4 qb, float e, float &ax, float &ay,
-                                              float &az)
-{
-    const float dx = c.x - qx, dy = c.y - qy, dz = c.z - qz;
-    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const float w = r2 + e;
-    const float iu = rsqrt_approx(fmaf(r2, w * w, kPairGuard));
-    const float s = c.w * iu;
-    const float ir = r2 > 1e-30f ? iu * w : 0.f;  // no quadrupole term at r = 0
-    const float A = fmaf(3.f, r2, e);
-    const float base = ir * iu * iu;
-    const float h = -A * base;
-    const float hp = base * fmaf(A, fmaf(2.f * A, iu * ir, ir * ir), -6.f);
-    const float sdx = fmaf(qa.x, dx, fmaf(qb.x, dy, qb.y * dz));
-    const float sdy = fmaf(qb.x, dx, fmaf(qa.y, dy, qb.z * dz));
-    const float sdz = fmaf(qb.y, dx, fmaf(qb.z, dy, qa.z * dz));
-    const float dsd = fmaf(dx, sdx, fmaf(dy, sdy, dz * sdz));
-    const float k = fmaf(0.5f, fmaf(h, qa.w, hp * dsd), s);
-    ax = fmaf(h, sdx, fmaf(k, dx, ax));
-    ay = fmaf(h, sdy, fmaf(k, dy, ay));
-    az = fmaf(h, sdz, fmaf(k, dz, az));
-}
-
-// Two cells' monopole + quadrupole terms for one body (nq = -position) with
-// the cells' (x, y, z, m) and second moments given as float2 planes, through
-// packed FP32 instructions; the arithmetic of each lane is that of
-// cell_quad_acc.
+// Monopole + quadrupole terms of two accepted cells for one body (nq =
+// -position), the cells' (x, y, z, m) and second moments given as float2
+// planes, through packed FP32 instructions.  Per lane the monopole and the
+// quadrupole share one reciprocal square root: 1/sqrt(r^2 (r^2 + e)^2) = 1/u
+// and 1/r = (r^2 + e)/u; the quadrupole term is that of quad_acc.
 __device__ __forceinline__ void cell_quad_acc2(float2 nqx, float2 nqy, float2 nqz, float2 cx,
                                                float2 cy, float2 cz, float2 cm, float2 qax,
                                                float2 qay, float2 qaz, float2 qaw, float2 qbx,

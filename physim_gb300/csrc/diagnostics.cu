@@ -57,29 +57,33 @@ __global__ void moments_kernel(const double *__restrict__ x, const double *__res
 // taken in f64 from the f64 state and rounded to FP32 (relative error 2^-24
 // of the separation itself, however close the pair); phi is evaluated in
 // FP32, summed in FP32 per 256-body tile and folded into f64 per tile.
+// f64 position and mass of one body (32-byte aligned: two 128-bit loads).
+struct alignas(32) Pos4 {
+    double x, y, z, w;
+};
+
 // 0.5 m_i * sum goes to out[8].
 __global__ void __launch_bounds__(kDiagThreads)
 potential_kernel(const double *__restrict__ x, const double *__restrict__ y,
                  const double *__restrict__ z, const double *__restrict__ m, int n, float e,
                  int chunk, double *__restrict__ out)
 {
-    __shared__ double4 tile[kDiagThreads];
+    __shared__ Pos4 tile[kDiagThreads];
     const int i = blockIdx.x * kDiagThreads + threadIdx.x;
     const int j0 = blockIdx.y * chunk, j1 = min(j0 + chunk, n);
-    const double4 bi = i < n ? make_double4(x[i], y[i], z[i], m[i]) : make_double4(0, 0, 0, 0);
+    const Pos4 bi = i < n ? Pos4{x[i], y[i], z[i], m[i]} : Pos4{0.0, 0.0, 0.0, 0.0};
     const float se = sqrtf(e);
     const float inv_se = e > 0.f ? 1.f / se : 0.f;
     double acc = 0.0;
     for (int t = j0; t < j1; t += kDiagThreads) {
         __syncthreads();
         const int j = t + threadIdx.x;
-        tile[threadIdx.x] = j < j1 ? make_double4(x[j], y[j], z[j], m[j])
-                                   : make_double4(0, 0, 0, 0);
+        tile[threadIdx.x] = j < j1 ? Pos4{x[j], y[j], z[j], m[j]} : Pos4{0.0, 0.0, 0.0, 0.0};
         __syncthreads();
         const int cnt = min(kDiagThreads, j1 - t);
         float part = 0.f;
         for (int k = 0; k < cnt; ++k) {
-            const double4 bj = tile[k];
+            const Pos4 bj = tile[k];
             const double ddx = bj.x - bi.x, ddy = bj.y - bi.y, ddz = bj.z - bi.z;
             if (ddx == 0.0 && ddy == 0.0 && ddz == 0.0) continue;  // equal centres
             const float dx = (float)ddx, dy = (float)ddy, dz = (float)ddz;
