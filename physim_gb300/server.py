@@ -36,6 +36,9 @@ import numpy as np
 BYTES_PER_BODY_DIRECT = 200
 BYTES_PER_BODY_TREE = 700
 BYTES_FIXED = 4 << 20
+# Smallest direct-sum job that may evaluate each unordered pair once (the
+# lowest size threshold the ensemble autotuner picks)
+SYMMETRIC_FROM = 8192
 
 
 @dataclass(order=True)
@@ -54,6 +57,10 @@ class JobSpec:
 
     def device_bytes(self) -> int:
         per = BYTES_PER_BODY_DIRECT if self.gravity == "simple_astro" else BYTES_PER_BODY_TREE
+        if self.gravity == "simple_astro" and self.n >= SYMMETRIC_FROM:
+            # evaluating each unordered pair once keeps an f32 slot sum per
+            # body for every 1,024-body tile
+            per += 12 * ((self.n + 1023) // 1024)
         return BYTES_FIXED + per * self.n
 
     def step_seconds(self) -> float:

@@ -83,13 +83,13 @@ def test_all_jobs_complete_once():
 
 def test_budget_is_respected_and_first_fit():
     ex = FakeExecutor(k=1)
-    per = BYTES_PER_BODY_DIRECT
-    budget = 2 * BYTES_FIXED + 2 * per * 10_000
-    srv = Server(ex, hbm_budget=budget)
-    ex.server = srv
     big = job(0, 10_000, 50)
     blocked = job(1, 15_000, 5, t=0.0001)   # does not fit beside `big`
     small = job(2, 5_000, 5, t=0.0002)      # fits: overtakes the waiting job
+    budget = big.device_bytes() + small.device_bytes() + BYTES_PER_BODY_DIRECT
+    assert big.device_bytes() + blocked.device_bytes() > budget
+    srv = Server(ex, hbm_budget=budget)
+    ex.server = srv
     srv.submit([big, blocked, small])
     srv.run(until=30.0)
     assert ex.max_in_use <= budget
