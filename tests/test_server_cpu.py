@@ -275,3 +275,15 @@ def test_async_admission(scheduling):
     assert [f.spec.id for f in srv.failed] == [3]
     assert srv.unfinished() == 0 and srv.in_use == 0
     assert srv.steps_executed == sum(j.steps for j in jobs if j.id != 3)
+
+
+def test_device_bytes_estimates():
+    """Direct-sum jobs from the symmetric size up also hold one f32 slot sum
+    per 1,024-body tile and body; Barnes-Hut jobs hold the tree workspace."""
+    from physim_gb300.server import BYTES_PER_BODY_TREE, SYMMETRIC_FROM
+    small = job(0, SYMMETRIC_FROM - 1, 10)
+    big = job(1, 32768, 10)
+    assert small.device_bytes() == BYTES_FIXED + BYTES_PER_BODY_DIRECT * small.n
+    assert big.device_bytes() == BYTES_FIXED + (BYTES_PER_BODY_DIRECT + 12 * 32) * big.n
+    tree = job(2, 100_000, 10, gravity="astro2")
+    assert tree.device_bytes() == BYTES_FIXED + BYTES_PER_BODY_TREE * tree.n
