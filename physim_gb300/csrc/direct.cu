@@ -119,9 +119,30 @@ constexpr int kSymmetricMinBodies = 20480;
 // Smallest size at which the autotuner also times the symmetric plan.
 constexpr int kSymmetricCandidateBodies = 12288;
 
+// The symmetric plan's slot buffer grows as n^2 (12 B per body and 1,024-body
+// tile: 12.9 GB at 1,048,580 bodies, 51 GB at 2M); above a quarter of the
+// device's memory the one-pair plans are used instead.
+static bool symmetric_fits(int n, int device)
+{
+    static size_t total[64] = {0};
+    if (device < 0 || device >= 64) return false;
+    if (total[device] == 0) {
+        size_t free_b = 0, total_b = 0;
+        int cur = 0;
+        if (cudaGetDevice(&cur) == cudaSuccess && cur == device &&
+            cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+            total[device] = total_b;
+        else
+            return false;
+    }
+    const DirectPlan p = make_symmetric_plan(n);
+    return direct_partial_doubles(p) * sizeof(double) <= total[device] / 4;
+}
+
 DirectPlan plan_direct(int n, int device, bool compensated)
 {
-    if (compensated && n >= kSymmetricMinBodies) return make_symmetric_plan(n);
+    if (compensated && n >= kSymmetricMinBodies && symmetric_fits(n, device))
+        return make_symmetric_plan(n);
     const int sms = device_sm_count(device);
     DirectPlan best;
     double best_score = -1.0;
@@ -177,7 +198,8 @@ int direct_candidates(int n, int device, bool compensated, DirectPlan *out, int 
             out[k++] = make_plan(n, s.block, s.ipt, best[q], compensated);
         }
     }
-    if (compensated && n >= kSymmetricCandidateBodies && k < cap) out[k++] = make_symmetric_plan(n);
+    if (compensated && n >= kSymmetricCandidateBodies && k < cap && symmetric_fits(n, device))
+        out[k++] = make_symmetric_plan(n);
     return k;
 }
 

@@ -347,6 +347,18 @@ void drop_graph(PhysimEnsemble *E)
 int plan_ensemble(PhysimEnsemble *E, int block, int ipt, int chunk, int sym_min)
 {
     const int chunk_tiles = std::max(1, chunk / block);
+    {
+        // the members' slot sums grow as n^2 (12 B per body and 1,024-body
+        // tile); above a quarter of the device's memory every member takes
+        // the one-pair units
+        size_t slot_bytes = 0, free_b = 0, total_b = 0;
+        for (const MemberInfo &mi : E->members)
+            if (mi.n >= sym_min)
+                slot_bytes += (pad_bodies((size_t)mi.n) / kSymTile) * 12 * (size_t)mi.n;
+        if (slot_bytes > 0 &&
+            (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || slot_bytes > total_b / 4))
+            sym_min = INT32_MAX;
+    }
     std::vector<WorkUnit> units;
     std::vector<SymUnit> sym_units;
     std::vector<long long> cost;
