@@ -1,0 +1,44 @@
+"""bench.py's output contract where it runs without a GPU: the reference arm
+(the CPU restatement of simple_astro timed on the host cores) prints one JSON
+line with the metric and units of the GPU arm, a cpu_baseline describing the
+run and an e2e object with no transfers; the argument parser keeps the
+documented defaults."""
+from __future__ import annotations
+
+import json
+import subprocess
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def test_reference_arm_json_line():
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
+                          "--steps", "1", "--warmup", "0", "--cpu-seconds", "0.3"],
+                         capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    import bench
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC
+    assert d["unit"] == "Gpair-interactions/s" and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 0
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1
+    assert cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+    assert d["config"]["workload"] == bench.WORKLOAD
+
+
+def test_parser_defaults(monkeypatch):
+    sys.path.insert(0, str(ROOT))
+    import bench
+    monkeypatch.setattr(sys, "argv", ["bench.py"])
+    a = bench.parse()
+    assert (a.gpus, a.impl, a.only) == (1, "ours", "")
+    assert a.warmup >= 3 and a.steps >= 1
+    assert a.serve_scheduling == "all" and a.serve_max_units == 8
+    assert a.bh_sample == 16384 and a.bh_steps == 1000
