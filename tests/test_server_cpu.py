@@ -287,3 +287,22 @@ def test_device_bytes_estimates():
     assert big.device_bytes() == BYTES_FIXED + (BYTES_PER_BODY_DIRECT + 12 * 32) * big.n
     tree = job(2, 100_000, 10, gravity="astro2")
     assert tree.device_bytes() == BYTES_FIXED + BYTES_PER_BODY_TREE * tree.n
+
+
+def test_async_admission_cutoff_while_building():
+    """A run cut off while units are still being built counts their jobs as
+    unfinished, and close() waits for the builds and closes their units."""
+    import time
+
+    class VerySlow(TimedExecutor):
+        def make_units(self, jobs):
+            time.sleep(0.3)
+            return super().make_units(jobs)
+
+    ex = VerySlow(k=10)
+    srv = Server(ex, hbm_budget=1 << 40, async_admission=True, max_batch=1)
+    srv.submit([job(i, 1000, 50) for i in range(3)])
+    res = srv.run(until=0.1)
+    assert res == [] and srv.unfinished() == 3
+    srv.close()
+    assert ex.closed >= 1  # the unit built after the cut-off was closed
