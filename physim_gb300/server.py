@@ -14,6 +14,13 @@ finishes, and overlaps the work of all admitted jobs on the GPU:
     that finished are downloaded and their memory returns to the budget,
     and waiting jobs are admitted into the freed room.
 
+Admission order is arrival order or shortest estimated device work first.
+Ticks go either to every admitted unit at once ("all") or, under "srpt",
+to the units with the least remaining estimated work while the estimated
+work in flight is below a budget.  With `async_admission` the units of
+admitted jobs (initial states, device allocations, uploads) are built on a
+worker thread, so handing out ticks never waits for them.
+
 Latency is measured per job from its arrival to the download of its final
 state.  The device work goes through the `Executor` interface so the
 scheduling logic can be exercised without a GPU (tests use a fake executor).
