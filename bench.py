@@ -292,22 +292,24 @@ def host_array_steps(pg, element, props, state, steps, device, mode):
     accelerations, the element's transform into them, the verlet update into
     the reused new_state array, which becomes the next state."""
     pg.set_host_access(mode)
-    used = pg.host_access(device)
-    el = pg.TransformElementHandler(element, props)
-    verlet = pg.GpuVerlet(device)
-    cur = state.copy()
-    nxt = np.empty_like(cur)
-    el.transform(cur, pg.accelerations(len(cur)))  # warm: allocations, module load
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        acc = np.zeros(len(cur), dtype=pg.ACCELERATION)
-        el.transform(cur, acc)
-        verlet.integrate(cur, acc, DT, out=nxt)
-        cur, nxt = nxt, cur
-    seconds = time.perf_counter() - t0
-    el.destroy()
-    verlet.close()
-    pg.set_host_access("auto")
+    try:
+        used = pg.host_access(device)
+        el = pg.TransformElementHandler(element, props)
+        verlet = pg.GpuVerlet(device)
+        cur = state.copy()
+        nxt = np.empty_like(cur)
+        el.transform(cur, pg.accelerations(len(cur)))  # warm: allocations, module load
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            acc = np.zeros(len(cur), dtype=pg.ACCELERATION)
+            el.transform(cur, acc)
+            verlet.integrate(cur, acc, DT, out=nxt)
+            cur, nxt = nxt, cur
+        seconds = time.perf_counter() - t0
+        el.destroy()
+        verlet.close()
+    finally:
+        pg.set_host_access("auto")
     return seconds, used
 
 
