@@ -810,17 +810,19 @@ def measure_tour(args, dist: Dist, device: int) -> dict:
             sim.step(2)
         paths.append(" ".join(f"{k}={v}" for k, v in cfg.items()))
     # host arrays: the plugin transform + verlet, in place and with copies
-    for mode in ("direct", "copy"):
-        if mode == "direct" and pg.host_access(device) != "direct":
-            continue
-        pg.set_host_access(mode)
-        el = pg.TransformElementHandler("simple_astro", {"e": E, "device": device})
-        acc = pg.accelerations(len(small))
-        el.transform(small, acc)
-        pg.GpuVerlet(device).integrate(small, acc, DT)
-        el.destroy()
-        paths.append(f"plugin simple_astro + verlet, host access {mode}")
-    pg.set_host_access("auto")
+    try:
+        for mode in ("direct", "copy"):
+            if mode == "direct" and pg.host_access(device) != "direct":
+                continue
+            pg.set_host_access(mode)
+            el = pg.TransformElementHandler("simple_astro", {"e": E, "device": device})
+            acc = pg.accelerations(len(small))
+            el.transform(small, acc)
+            pg.GpuVerlet(device).integrate(small, acc, DT)
+            el.destroy()
+            paths.append(f"plugin simple_astro + verlet, host access {mode}")
+    finally:
+        pg.set_host_access("auto")
     for kind in ("euler", "rk4"):
         el = pg.TransformElementHandler("astro2", {"e": E, "theta": 0.5, "device": device})
         pg.GpuIntegrator(kind, device).integrate(small, lambda st, ac: el.transform(st, ac), DT)
