@@ -22,7 +22,12 @@ N(N-1) pair interactions plus the f64 kick-drift.  Prints one JSON line.
             transform runs) on a bounded sample of bodies.
 
 --impl reference times the reference algorithm's CPU implementation (the C
-restatement, the Rust reference cannot be built here) on all host cores.
+restatement, the Rust reference cannot be built here) on all host cores: each
+step is a bounded sample of one full step (a fixed number of bodies against
+all their partners), ms_per_step is the time that sample took, and the line
+also carries a single-thread figure (physim's transform runs on one thread).
+That arm imports only numpy modules of the package and the oracle, so the
+CUDA library is never loaded into it.
 Under torchrun every rank runs an independent replica (the path has no
 exchange step); value is the sum of the ranks' pairs over the slowest rank.
 """
@@ -214,57 +219,101 @@ def measured_peaks() -> dict:
 # ---------------------------------------------------------------------------
 # CPU baseline: the C restatement on a bounded sample
 # ---------------------------------------------------------------------------
-def cpu_sample_rate(state, threads: int, target_s: float) -> dict:
+def _sample_rows(n: int, k: int, seed: int) -> np.ndarray:
+    return np.sort(np.random.default_rng(seed).choice(n, k, replace=False))
+
+
+def cpu_rows_per_second(state, threads: int, probe_s: float = 0.3) -> float:
+    """Rows (bodies x all their partners) of the f64 simple_astro restatement
+    one call on `threads` threads finishes per second, from growing probes."""
     import oracle
     n = len(state)
-    rng = np.random.default_rng(123)
-    k = 8
-    t_per = None
+    k = max(8, threads)
     while True:
-        idx = rng.choice(n, k, replace=False)
+        idx = _sample_rows(n, min(n, k), 99)
         t0 = time.perf_counter()
         oracle.simple_astro_sample(state, E, idx, threads=threads)
         dt = time.perf_counter() - t0
-        if dt > 0.5 or k >= n:
-            t_per = dt / k
-            break
-        k = min(n, k * 4)
-    k = int(min(n, max(k, target_s / max(t_per, 1e-9))))
-    idx = rng.choice(n, k, replace=False)
+        if dt > probe_s or k >= n:
+            return len(idx) / max(dt, 1e-9)
+        k *= 4
+
+
+def cpu_sample_step(state, threads: int, rows: int, seed: int) -> dict:
+    """One bounded CPU step: the reference's simple_astro accelerations
+    (f64 C restatement, transformers.rs:219-244) of `rows` bodies against
+    all n-1 partners, on `threads` threads.  Returns its seconds and pairs."""
+    import oracle
+    n = len(state)
+    idx = _sample_rows(n, rows, seed)
     t0 = time.perf_counter()
     oracle.simple_astro_sample(state, E, idx, threads=threads)
     dt = time.perf_counter() - t0
-    pairs = k * (n - 1)
-    return {"value": pairs / dt / 1e9, "unit": "Gpair-interactions/s", "cores": threads,
-            "seconds": dt,
-            "sample": f"{k} bodies x {n - 1} partners of the {n}-body workload (f64 C "
-                      f"restatement of simple_astro, transformers.rs:219-244)"}
+    return {"seconds": dt, "pairs": len(idx) * (n - 1), "rows": len(idx)}
+
+
+def cpu_sample_rate(state, threads: int, target_s: float) -> dict:
+    """The CPU baseline of our arm: one sample of about target_s seconds."""
+    n = len(state)
+    rows = int(min(n, max(threads, cpu_rows_per_second(state, threads) * target_s)))
+    r = cpu_sample_step(state, threads, rows, 123)
+    return {"value": r["pairs"] / r["seconds"] / 1e9, "unit": "Gpair-interactions/s",
+            "cores": threads, "seconds": r["seconds"],
+            "sample": f"{rows} of the {n} bodies x their {n - 1} partners, {r['seconds']:.1f} s "
+                      f"(f64 C restatement of simple_astro, transformers.rs:219-244, "
+                      f"{threads} thread{'s' if threads > 1 else ''})"}
+
+
+def bench_config(bodies: int, gpus: int) -> dict:
+    """The workload both arms report (our arm's plan details are kept outside)."""
+    return {"workload": WORKLOAD, "bodies": bodies + 4, "pairs_per_step": (bodies + 4) * (bodies + 3),
+            "parallelism": f"replicas x{gpus}" if gpus > 1 else "single GPU",
+            "l2": "flushed between timed steps (256 MiB write, outside the events)"}
+
+
+def workload_state(bodies: int):
+    from physim_gb300 import ics  # numpy only: the CUDA library stays unloaded
+    return ics.workload_large(bodies)
 
 
 def run_reference(args, dist: Dist):
+    """The reference algorithm on the host cores: each step is a bounded
+    sample of one full simple_astro step (a fixed number of bodies against
+    all their partners), timed as it runs; value = sampled pairs / seconds."""
     if dist.rank != 0:
         return
     import oracle
-    from physim_gb300 import ics
-    state = ics.workload_large(N_CUBE)
-    threads = oracle.load().oracle_max_threads()
-    per_step = max(args.cpu_seconds / 3.0, 1.0)
-    for _ in range(args.warmup):
-        cpu_sample_rate(state, threads, per_step / 4)
-    vals = [cpu_sample_rate(state, threads, per_step) for _ in range(args.steps)]
-    value = statistics.median(v["value"] for v in vals)
+    state = workload_state(args.bodies)
     n = len(state)
+    threads = oracle.load().oracle_max_threads()
+    per_step_s = max(0.5, args.cpu_seconds / 4.0)
+    rows = int(min(n, max(threads, cpu_rows_per_second(state, threads) * per_step_s)))
+    for w in range(args.warmup):
+        cpu_sample_step(state, threads, max(threads, rows // 4), 1000 + w)
+    steps = [cpu_sample_step(state, threads, rows, 2000 + k) for k in range(args.steps)]
+    seconds = sum(r["seconds"] for r in steps)
+    pairs = sum(r["pairs"] for r in steps)
+    value = pairs / seconds / 1e9
+    single = cpu_sample_rate(state, 1, max(1.0, args.cpu_seconds / 4.0))
+    sample = (f"each step: {rows} of the {n} bodies x their {n - 1} partners "
+              f"({rows / n:.2%} of one full step's {n * (n - 1):.4g} pairs), "
+              f"{args.steps} steps in {seconds:.1f} s")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Gpair-interactions/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": n * (n - 1) / (value * 1e9) * 1e3, "higher_is_better": True,
+        "ms_per_step": seconds / max(args.steps, 1) * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD,
-                   "implementation": "C restatement of physim's simple_astro (oracle/, OpenMP "
-                                     "over bodies); the Rust reference needs cargo, absent here",
-                   "per_step_sample": vals[0]["sample"]},
+        "config": bench_config(args.bodies, args.gpus),
+        "implementation": "C restatement of physim's simple_astro (oracle/, f64, OpenMP over "
+                          "bodies); the Rust reference needs cargo, absent here",
+        "sampling": {"rows_per_step": rows, "total_rows": n, "partners_per_row": n - 1,
+                     "seconds_timed": seconds, "full_step_seconds_estimate":
+                         n * (n - 1) / (value * 1e9)},
         "cpu_baseline": {"value": value, "unit": "Gpair-interactions/s", "cores": threads,
-                         "kind": "port", "sample": vals[0]["sample"]},
+                         "kind": "port", "sample": sample},
+        "single_thread": {"value": single["value"], "unit": "Gpair-interactions/s", "cores": 1,
+                          "sample": single["sample"],
+                          "note": "physim's transform runs on one thread"},
         "e2e": {"value": value, "unit": "Gpair-interactions/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -339,9 +388,7 @@ def measure_direct(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict
     import torch
 
     import physim_gb300 as pg
-    from physim_gb300 import ics
-
-    state = ics.workload_large(args.bodies)
+    state = workload_state(args.bodies)
     n = len(state)
     pairs_step = n * (n - 1)  # no fixed bodies in this workload
     stream = torch.cuda.Stream(device=device)
@@ -885,8 +932,9 @@ def run_ours(args, dist: Dist):
                    "compensated_sums": True},
     }
     if direct:
-        line["config"]["pairs_per_step"] = direct["pairs_per_step"]
-        line["config"]["pair_kernel_plan"] = direct["plan"]
+        line["config"] = bench_config(args.bodies, args.gpus)
+        line["pair_kernel_plan"] = direct["plan"]
+        line["compensated_sums"] = True
         for k in ("roofline", "e2e", "gpu_launches", "cpu_baseline", "clocks"):
             if k in direct:
                 line[k] = direct[k]

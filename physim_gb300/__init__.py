@@ -4,8 +4,9 @@ The compute lives in libphysim_gb300.so (CUDA kernels behind a C ABI, see
 include/physim_gb300.h).  This package is the Python host side: ctypes
 bindings, the physim Entity layout as a numpy dtype, a mirror of physim's
 transform-element handler and pipeline step, device-resident simulations and
-seeded initial conditions.  Importing it loads the CUDA library and fails
-loudly if the library is missing; there is no CPU fallback.
+seeded initial conditions.  The CUDA library is loaded on the first call
+that needs it (`lib.load()` loads it explicitly); that call fails loudly if
+the library is missing: there is no CPU fallback.
 """
 from ._lib import LIB_PATH, PhysimError, host_access, last_error, lib, set_host_access
 from .entity import ACCELERATION, ENTITY, accelerations, entities, entity_new

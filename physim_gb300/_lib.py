@@ -1,8 +1,10 @@
 """ctypes binding of libphysim_gb300.so (declarations in include/physim_gb300.h).
 
-Importing this module loads the CUDA library; there is no CPU fallback.  If
-the shared library has not been built the import fails with an error that
-says how to build it.
+`lib` loads the CUDA library on its first use (the first physim_gpu_* or
+plugin call), not when the package is imported, so code that only needs the
+Entity dtype or the seeded initial conditions (the oracle, the CPU baseline)
+never maps the library.  There is no CPU fallback: if the shared library has
+not been built, that first call fails with an error that says how to build it.
 """
 from __future__ import annotations
 
@@ -188,7 +190,28 @@ def _load() -> C.CDLL:
     return lib
 
 
-lib = _load()
+class _Library:
+    """The loaded libphysim_gb300.so, opened on first attribute access."""
+
+    __slots__ = ("_cdll",)
+
+    def __init__(self):
+        self._cdll = None
+
+    def load(self) -> C.CDLL:
+        if self._cdll is None:
+            self._cdll = _load()
+        return self._cdll
+
+    @property
+    def loaded(self) -> bool:
+        return self._cdll is not None
+
+    def __getattr__(self, name):
+        return getattr(self.load(), name)
+
+
+lib = _Library()
 
 
 class PhysimError(RuntimeError):

@@ -30,7 +30,26 @@ def test_reference_arm_json_line():
     assert cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
-    assert d["config"]["workload"] == bench.WORKLOAD
+    assert d["config"] == bench.bench_config(bench.N_CUBE, 1)
+    smp = d["sampling"]
+    assert smp["total_rows"] == bench.N_CUBE + 4 and 0 < smp["rows_per_step"] <= smp["total_rows"]
+    # ms_per_step is the time actually spent per sampled step, not an extrapolation
+    assert abs(d["ms_per_step"] * d["steps"] / 1e3 - smp["seconds_timed"]) < 1e-6
+    assert d["single_thread"]["cores"] == 1 and d["single_thread"]["value"] > 0
+
+
+def test_reference_arm_leaves_the_cuda_library_unloaded():
+    """The reference arm runs only the oracle: libphysim_gb300.so must not be
+    mapped into its process (importing the package's numpy-only modules does
+    not load it)."""
+    code = ("import sys, bench; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', "
+            "'--warmup', '0', '--cpu-seconds', '0.2']; bench.main(); "
+            "import physim_gb300; maps = open('/proc/self/maps').read(); "
+            "print('MAPPED', 'libphysim_gb300' in maps, physim_gb300.lib.loaded)")
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
+                         timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert "MAPPED False False" in out.stdout, out.stdout[-500:]
 
 
 def test_parser_defaults(monkeypatch):
