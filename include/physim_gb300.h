@@ -365,6 +365,17 @@ int physim_gpu_sim_autotune(PhysimSim *sim, PhysimDirectTuning *out);
  * of plan->block threads, plan->ipt bodies per thread and plan->splits
  * j-range splits.  Other fields are ignored. */
 int physim_gpu_sim_set_plan(PhysimSim *sim, const PhysimDirectTuning *plan);
+/* Largest slot buffer (bytes) the heuristic direct-sum plan of a simulation or
+ * a simple_astro element may give the each-pair-once (symmetric) plan; 0
+ * restores the default, a quarter of the device's memory.  The symmetric plan
+ * is also skipped when its buffer plus 1 GiB exceeds the device's free memory
+ * when the plan is made, and a symmetric plan whose allocation fails falls
+ * back to a one-pair plan.  Process-wide, read when a plan is made.  This
+ * builds on simple_astro (transformers.rs:219-244), which has no plans. */
+int physim_gpu_set_symmetric_cap(uint64_t bytes);
+/* The current pair-kernel plan of a simple_astro simulation (block, ipt,
+ * splits, symmetric, tiles; the other fields 0); all zero for astro/astro2. */
+int physim_gpu_sim_plan(PhysimSim *sim, PhysimDirectTuning *out);
 /* Number of kernel launches one step enqueues (for launch accounting). */
 int physim_gpu_sim_launches_per_step(PhysimSim *sim);
 /* Records CUDA events around the gravity kernels and the integrator of each

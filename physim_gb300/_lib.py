@@ -148,6 +148,8 @@ def _load() -> C.CDLL:
         "physim_gpu_sim_tree_snapshot": (C.c_int, [vp, C.POINTER(PhysimTreeSnapshot)]),
         "physim_gpu_sim_autotune": (C.c_int, [vp, C.POINTER(PhysimDirectTuning)]),
         "physim_gpu_sim_set_plan": (C.c_int, [vp, C.POINTER(PhysimDirectTuning)]),
+        "physim_gpu_sim_plan": (C.c_int, [vp, C.POINTER(PhysimDirectTuning)]),
+        "physim_gpu_set_symmetric_cap": (C.c_int, [C.c_uint64]),
         "physim_gpu_sim_init_cube": (C.c_int, [vp, C.POINTER(PhysimCubeParams)]),
         "physim_gpu_sim_init_plummer": (C.c_int, [vp, C.POINTER(PhysimPlummerParams)]),
         "physim_gpu_generate_cube": (C.c_int, [C.POINTER(PhysimCubeParams), vp, sz, i32]),
@@ -237,6 +239,12 @@ def set_host_access(mode: str) -> None:
     "direct" (kernels read and write the host arrays in place over the
     device's pageable-memory access) or "auto" (direct where supported)."""
     check(lib.physim_gpu_set_host_access(HOST_ACCESS[mode]), "physim_gpu_set_host_access")
+
+
+def set_symmetric_cap(nbytes: int) -> None:
+    """Largest slot buffer the heuristic direct-sum plans give the
+    each-pair-once plan (0: a quarter of the device's memory)."""
+    check(lib.physim_gpu_set_symmetric_cap(int(nbytes)), "physim_gpu_set_symmetric_cap")
 
 
 def host_access(device: int = 0) -> str:

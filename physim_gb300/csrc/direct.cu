@@ -19,6 +19,7 @@
 // full.  Per-body sums are compensated: each j tile is summed in plain FP32
 // and folded into a (hi, lo) pair with TwoSum once per tile.
 #include <algorithm>
+#include <atomic>
 
 #include "common.cuh"
 #include "direct_tile.cuh"
@@ -120,29 +121,31 @@ constexpr int kSymmetricMinBodies = 20480;
 constexpr int kSymmetricCandidateBodies = 12288;
 
 // The symmetric plan's slot buffer grows as n^2 (12 B per body and 1,024-body
-// tile: 12.9 GB at 1,048,580 bodies, 51 GB at 2M); above a quarter of the
-// device's memory the one-pair plans are used instead.
+// tile: 12.9 GB at 1,048,580 bodies, 51 GB at 2M).  It is planned only while
+// it stays within the cap (a quarter of the device's memory unless
+// physim_gpu_set_symmetric_cap set one) and within the device's free memory
+// at planning time less a margin for everything else; otherwise the one-pair
+// plans are used.  A plan that still fails to allocate falls back to a
+// one-pair plan at the caller (element.cu, sim.cu).
+static std::atomic<uint64_t> g_symmetric_cap{0};
+constexpr size_t kSymmetricFreeMargin = size_t(1) << 30;
+
 static bool symmetric_fits(int n, int device)
 {
-    static size_t total[64] = {0};
-    if (device < 0 || device >= 64) return false;
-    if (total[device] == 0) {
-        size_t free_b = 0, total_b = 0;
-        int cur = 0;
-        if (cudaGetDevice(&cur) == cudaSuccess && cur == device &&
-            cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
-            total[device] = total_b;
-        else
-            return false;
+    int cur = 0;
+    size_t free_b = 0, total_b = 0;
+    if (cudaGetDevice(&cur) != cudaSuccess || cur != device ||
+        cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
     }
-    const DirectPlan p = make_symmetric_plan(n);
-    return direct_partial_doubles(p) * sizeof(double) <= total[device] / 4;
+    const uint64_t cap = g_symmetric_cap.load();
+    const size_t need = direct_partial_doubles(make_symmetric_plan(n)) * sizeof(double);
+    return need <= (cap ? cap : total_b / 4) && need + kSymmetricFreeMargin <= free_b;
 }
 
-DirectPlan plan_direct(int n, int device, bool compensated)
+DirectPlan plan_direct_one_pair(int n, int device, bool compensated)
 {
-    if (compensated && n >= kSymmetricMinBodies && symmetric_fits(n, device))
-        return make_symmetric_plan(n);
     const int sms = device_sm_count(device);
     DirectPlan best;
     double best_score = -1.0;
@@ -166,6 +169,13 @@ DirectPlan plan_direct(int n, int device, bool compensated)
         }
     }
     return best;
+}
+
+DirectPlan plan_direct(int n, int device, bool compensated)
+{
+    if (compensated && n >= kSymmetricMinBodies && symmetric_fits(n, device))
+        return make_symmetric_plan(n);
+    return plan_direct_one_pair(n, device, compensated);
 }
 
 int direct_candidates(int n, int device, bool compensated, DirectPlan *out, int cap)
@@ -241,3 +251,9 @@ int launch_direct(const DirectPlan &plan, const float4 *body4, float e, double *
 }
 
 }  // namespace pg
+
+extern "C" int physim_gpu_set_symmetric_cap(uint64_t bytes)
+{
+    pg::g_symmetric_cap.store(bytes);
+    return PHYSIM_OK;
+}

@@ -66,8 +66,15 @@ static int accumulate_locked(ElementState *el, const Entity *state, size_t n, Ac
             el->plan = plan_direct((int)n, el->device, true);
             el->plan_n = (int)n;
         }
+        int rc = ensure_doubles(el->partial, el->partial_cap, direct_partial_doubles(el->plan), st);
+        if (rc == PHYSIM_ERR_MEMORY && el->plan.symmetric) {
+            // the slot buffer did not fit after all: one-pair kernels need 3n doubles
+            (void)cudaGetLastError();
+            el->plan = plan_direct_one_pair((int)n, el->device, true);
+            rc = ensure_doubles(el->partial, el->partial_cap, direct_partial_doubles(el->plan), st);
+        }
+        PG_TRY(rc);
         splits = el->plan.splits;
-        PG_TRY(ensure_doubles(el->partial, el->partial_cap, direct_partial_doubles(el->plan), st));
         PG_TRY(launch_direct(el->plan, el->bodies.body4, (float)el->e, el->partial, st));
     } else {
         PG_TRY(ensure_doubles(el->partial, el->partial_cap, 3 * n, st));

@@ -45,6 +45,9 @@ struct DirectPlan {
 // Heuristic plan that fills the GPU: picks the i-tile shape and the number of
 // j splits whose block count wastes least in the last wave.
 DirectPlan plan_direct(int n, int device, bool compensated);
+// The heuristic one-pair plan (never the symmetric one): the fallback when the
+// symmetric plan's slot buffer cannot be allocated.
+DirectPlan plan_direct_one_pair(int n, int device, bool compensated);
 // A plan with a given shape and number of j splits (clamped to 1..j tiles).
 DirectPlan make_direct_plan(int n, int block, int ipt, int splits, bool compensated);
 // Enumerates the candidate plans the autotuner times for n bodies.

@@ -194,6 +194,13 @@ int physim_gpu_sim_create(const PhysimSimConfig *cfg, size_t n, PhysimSim **out)
     if (rc == PHYSIM_OK && cfg->gravity != PHYSIM_GRAVITY_SIMPLE_ASTRO)
         rc = bh_reserve(s->bh, n, cfg->device, (int)cfg->leaf_size, s->stream);
     if (rc == PHYSIM_OK) rc = dev_alloc(s->partial, partial_elems, s->stream);
+    if (rc == PHYSIM_ERR_MEMORY && s->plan.symmetric) {
+        // the symmetric plan's slot buffer did not fit: fall back to a one-pair plan
+        (void)cudaGetLastError();
+        s->plan = plan_direct_one_pair((int)n, cfg->device, cfg->compensated != 0);
+        partial_elems = direct_partial_doubles(s->plan);
+        rc = dev_alloc(s->partial, partial_elems, s->stream);
+    }
     s->partial_cap = partial_elems;
     if (rc == PHYSIM_OK && cfg->integrator == PHYSIM_INTEGRATOR_RK4) {
         const size_t m = 6 * (n ? n : 1);
@@ -401,6 +408,19 @@ int physim_gpu_sim_autotune(PhysimSim *s, PhysimDirectTuning *out)
         out->tiles = (uint32_t)s->plan.tiles;
         out->force_ms = best_ms;
     }
+    return PHYSIM_OK;
+}
+
+int physim_gpu_sim_plan(PhysimSim *s, PhysimDirectTuning *out)
+{
+    PG_CHECK(s && out, PHYSIM_ERR_ARGUMENT, "null argument");
+    memset(out, 0, sizeof *out);
+    if (s->cfg.gravity != PHYSIM_GRAVITY_SIMPLE_ASTRO) return PHYSIM_OK;
+    out->block = (uint32_t)s->plan.block;
+    out->ipt = (uint32_t)s->plan.ipt;
+    out->splits = (uint32_t)s->plan.splits;
+    out->symmetric = s->plan.symmetric ? 1u : 0u;
+    out->tiles = (uint32_t)s->plan.tiles;
     return PHYSIM_OK;
 }
 

@@ -189,6 +189,14 @@ class Simulation:
         return {"block": t.block, "ipt": t.ipt, "splits": t.splits, "candidates": t.candidates,
                 "symmetric": bool(t.symmetric), "tiles": t.tiles, "force_ms": t.force_ms}
 
+    def plan(self) -> dict:
+        """The current pair-kernel plan (simple_astro)."""
+        from ._lib import PhysimDirectTuning
+        t = PhysimDirectTuning()
+        check(lib.physim_gpu_sim_plan(self.handle, C.byref(t)), "physim_gpu_sim_plan")
+        return {"block": t.block, "ipt": t.ipt, "splits": t.splits,
+                "symmetric": bool(t.symmetric), "tiles": t.tiles}
+
     def set_plan(self, symmetric: bool = False, block: int = 256, ipt: int = 4,
                  splits: int = 1) -> None:
         """Fixes the pair-kernel plan (simple_astro): every unordered pair once

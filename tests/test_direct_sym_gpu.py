@@ -114,3 +114,34 @@ def test_set_plan_validation():
     with pg.Simulation(s, pg.SimConfig(gravity="astro2")) as sim:
         with pytest.raises(pg.PhysimError):
             sim.set_plan(symmetric=True)
+
+
+def test_symmetric_cap_falls_back_to_one_pair_plans(oracle_mod):
+    """The heuristic plan gives 30,000 bodies the each-pair-once plan; with
+    its slot buffer capped below its size it takes a one-pair plan instead,
+    for simulations and for the simple_astro element, with the same results
+    (within the one-pair tolerance)."""
+    import physim_gb300 as pg
+    s = _state(30_000, seed=77)
+    cfg = pg.SimConfig(gravity="simple_astro", e=0.01)
+    try:
+        with pg.Simulation(s, cfg) as sim:
+            assert sim.plan()["symmetric"]
+            sym = sim.accelerations()
+        pg.set_symmetric_cap(1 << 20)
+        with pg.Simulation(s, cfg) as sim:
+            plan = sim.plan()
+            assert not plan["symmetric"] and plan["splits"] >= 1
+            one = sim.accelerations()
+        acc = pg.accelerations(len(s))
+        with pg.TransformElementHandler("simple_astro", {"e": 0.01}) as el:
+            el.transform(s, acc)
+    finally:
+        pg.set_symmetric_cap(0)
+    idx = np.arange(0, len(s), 97)
+    ref = oracle_mod.simple_astro_sample(s, 0.01, idx)
+    live = ~np.isnan(_vec(ref)).any(axis=1) & (s["fixed"][idx] == 0)
+    for got in (sym, one, acc):
+        assert rel_err(got[idx][live], ref[live]).max() < RTOL
+    keep = ~np.isnan(_vec(sym)).any(axis=1) & (s["fixed"] == 0)
+    assert rel_err(one[keep], sym[keep]).max() < 2e-6
