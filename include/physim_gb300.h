@@ -126,6 +126,13 @@ const char *register_plugin(void);
 /* Stores physim's message-bus pointer (plugin/mod.rs:234-244).  The library
  * resolves physim's `post_bus_callback` (messages.rs:201-226) at run time. */
 void set_callback_target(void *target);
+/* Routes the configuration messages to `fn` instead of physim's
+ * `post_bus_callback` (NULL restores the lookup), for hosts other than
+ * physim's binary that mirror its message bus (messages.rs:201-226); the
+ * message and its strings are valid during the call only.  physim itself
+ * never calls this. */
+typedef void (*PhysimBusFn)(void *target, const CMessage *message);
+int physim_gpu_set_bus_callback(PhysimBusFn fn);
 
 /* ----------------------------------------------------------------------- */
 /* 1a. Transform elements.  Each set replaces the symbols that             */
@@ -432,6 +439,22 @@ typedef struct PhysimDiagnostics {
 
 /* Waits for the stream; with_potential != 0 also evaluates the potential. */
 int physim_gpu_sim_diagnostics(PhysimSim *sim, PhysimDiagnostics *out, int with_potential);
+
+/* The same diagnostics of a host Entity array, for a sink that receives the
+ * pipeline's states: the computation behind physim's `energysink` element
+ * (debug/src/energysink.rs:35-99), which prints K, V and the change of E and
+ * turns its potential on when a gravity element posts ("energysink",
+ * "gravity") (energysink.rs:112-117, transformers.rs:107-111).  All sums are
+ * f64 (pair terms FP32, see physim_gpu_sim_diagnostics): V is the total over
+ * every pair (energysink.rs:86 keeps only the last pair, `=` for `+=`), with
+ * e = 0 the reference sink's -m_a m_b / r, with e > 0 the potential whose
+ * gradient is the reference's softened force.  The state is copied to the
+ * device; one call at a time per object. */
+typedef struct PhysimEnergy PhysimEnergy;
+int physim_gpu_energy_create(int32_t device, PhysimEnergy **out);
+int physim_gpu_energy_compute(PhysimEnergy *energy, const Entity *state, size_t n, double e,
+                              int with_potential, PhysimDiagnostics *out);
+void physim_gpu_energy_destroy(PhysimEnergy *energy);
 
 /* Waits for the stream, then reports the most recent Barnes-Hut traversal:
  * node visits (one per warp and node), pair interactions (per body) and,

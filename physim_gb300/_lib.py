@@ -68,6 +68,9 @@ class PhysimSimConfig(C.Structure):
                 ("com_theta", C.c_float)]
 
 
+# void (*PhysimBusFn)(void *target, const CMessage *message)
+BusFn = C.CFUNCTYPE(None, C.c_void_p, C.POINTER(CMessage))
+
 # void (*PhysimAccFn)(void *user, const Entity *state, size_t n, Acceleration *acc)
 AccFn = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p)
 
@@ -150,6 +153,11 @@ def _load() -> C.CDLL:
         "physim_gpu_sim_set_plan": (C.c_int, [vp, C.POINTER(PhysimDirectTuning)]),
         "physim_gpu_sim_plan": (C.c_int, [vp, C.POINTER(PhysimDirectTuning)]),
         "physim_gpu_set_symmetric_cap": (C.c_int, [C.c_uint64]),
+        "physim_gpu_set_bus_callback": (C.c_int, [BusFn]),
+        "physim_gpu_energy_create": (C.c_int, [i32, C.POINTER(vp)]),
+        "physim_gpu_energy_compute": (C.c_int, [vp, vp, sz, dbl, C.c_int,
+                                                C.POINTER(PhysimDiagnostics)]),
+        "physim_gpu_energy_destroy": (None, [vp]),
         "physim_gpu_sim_init_cube": (C.c_int, [vp, C.POINTER(PhysimCubeParams)]),
         "physim_gpu_sim_init_plummer": (C.c_int, [vp, C.POINTER(PhysimPlummerParams)]),
         "physim_gpu_generate_cube": (C.c_int, [C.POINTER(PhysimCubeParams), vp, sz, i32]),

@@ -884,11 +884,34 @@ struct TravArgs {
     // bounds the distance of the cell's bodies from c); 0 disables it.
     int quad;
     float com_theta;
+    // pair-law scale (PairScale in engine.h), set on the device from the root
+    // half-width X: bodies and cells enter pair_acc / quad_acc as p 2^-sk,
+    // second moments as S 2^-2sk, the easing as e 2^-2sk (es), and the sums
+    // leave multiplied by 2^-2sk; opening tests use unscaled positions
+    int sk;
+    float sc, es;
 };
 
 __device__ __forceinline__ float load_extent(const TravArgs &a)
 {
     return (float)__longlong_as_double((long long)*a.extent_bits);
+}
+
+__device__ __forceinline__ void set_pair_scale(TravArgs &a)
+{
+    a.sk = pair_scale_exp(a.extent, a.e);
+    a.sc = pow2f(-a.sk);
+    a.es = a.e * pow2f(-2 * a.sk);
+}
+
+__device__ __forceinline__ float4 scaled(float4 p, float sc)
+{
+    return make_float4(p.x * sc, p.y * sc, p.z * sc, p.w);
+}
+
+__device__ __forceinline__ float4 scaled2(float4 q, float sc2)
+{
+    return make_float4(q.x * sc2, q.y * sc2, q.z * sc2, q.w * sc2);
 }
 
 // The reference's opening rule `extent / r < theta` (octree.rs:137-144):
@@ -1046,6 +1069,8 @@ traverse_exact_kernel(TravArgs a_in)
     __shared__ StackEntry stack[kTravWarps][kStack];
     TravArgs a = a_in;
     a.extent = load_extent(a_in);
+    set_pair_scale(a);
+    const float sc2 = a.sc * a.sc;
     unsigned long long visits = 0, pairs = 0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int k0 = (blockIdx.x * kTravWarps + warp) * 32;
@@ -1054,6 +1079,7 @@ traverse_exact_kernel(TravArgs a_in)
     const bool valid = k < a.n;
     const uint32_t active = __ballot_sync(0xffffffffu, valid);
     const float4 q = valid ? a.sbody[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 qs = scaled(q, a.sc);
     float ax = 0.f, ay = 0.f, az = 0.f, hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
     int sp = 0;
     if (lane == 0) stack[warp][0] = {0, active};
@@ -1076,10 +1102,11 @@ traverse_exact_kernel(TravArgs a_in)
         const uint32_t open = top.mask & ~__ballot_sync(0xffffffffu, acc);
         ++visits;
         if (acc) {
-            const float4 cm = a.nd.com[node];
-            pair_acc(q.x, q.y, q.z, cm, a.e, ax, ay, az);
-            if (a.quad) quad_acc(q.x, q.y, q.z, cm, a.nd.quad_a[node], a.nd.quad_b[node], a.e, ax,
-                                 ay, az);
+            const float4 cm = scaled(a.nd.com[node], a.sc);
+            pair_acc(qs.x, qs.y, qs.z, cm, a.es, ax, ay, az);
+            if (a.quad)
+                quad_acc(qs.x, qs.y, qs.z, cm, scaled2(a.nd.quad_a[node], sc2),
+                         scaled2(a.nd.quad_b[node], sc2), a.es, ax, ay, az);
             ++pairs;
         }
         ++since_fold;
@@ -1088,8 +1115,8 @@ traverse_exact_kernel(TravArgs a_in)
                 const int b = a.nd.begin[node], c = a.nd.count[node];
                 const bool mine = (open >> lane) & 1u;
                 for (int j = b; j < b + c; ++j) {
-                    const float4 bj = a.sbody[j];
-                    if (mine) pair_acc(q.x, q.y, q.z, bj, a.e, ax, ay, az);
+                    const float4 bj = scaled(a.sbody[j], a.sc);
+                    if (mine) pair_acc(qs.x, qs.y, qs.z, bj, a.es, ax, ay, az);
                 }
                 if (mine) pairs += c;
                 since_fold += c;
@@ -1123,9 +1150,10 @@ traverse_exact_kernel(TravArgs a_in)
     }
     if (valid) {
         const uint32_t i = a.order[k];
-        a.partial[i] = (double)hx + (double)lx;
-        a.partial[a.n + i] = (double)hy + (double)ly;
-        a.partial[2 * (size_t)a.n + i] = (double)hz + (double)lz;
+        const double unsc = pow2d(-2 * a.sk);
+        a.partial[i] = ((double)hx + (double)lx) * unsc;
+        a.partial[a.n + i] = ((double)hy + (double)ly) * unsc;
+        a.partial[2 * (size_t)a.n + i] = ((double)hz + (double)lz) * unsc;
     }
 }
 
@@ -1170,6 +1198,8 @@ traverse_warp_kernel(TravArgs a_in)
     __shared__ float4 tqb[kQuad ? kTravWarps : 1][32];
     TravArgs a = a_in;
     a.extent = load_extent(a_in);
+    set_pair_scale(a);
+    const float sc = a.sc, sc2 = a.sc * a.sc;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int k0 = (blockIdx.x * kTravWarps + warp) * 32;
     if (k0 >= a.n) return;
@@ -1202,8 +1232,8 @@ traverse_warp_kernel(TravArgs a_in)
     // back, so each is evaluated by its own loop: plain pairs for bodies,
     // pair + quadrupole (kQuad) for cells.
     int nc = 0;  // queued cells
-    const float2 nqx = make_float2(-q.x, -q.x), nqy = make_float2(-q.y, -q.y);
-    const float2 nqz = make_float2(-q.z, -q.z), e2 = make_float2(a.e, a.e);
+    const float2 nqx = make_float2(-q.x * sc, -q.x * sc), nqy = make_float2(-q.y * sc, -q.y * sc);
+    const float2 nqz = make_float2(-q.z * sc, -q.z * sc), e2 = make_float2(a.es, a.es);
     // Evaluates `count` queued interactions whose (x, y, z, m) load(t) gives:
     // entries 2k and 2k + 1 are staged interleaved as (x, x', y, y')(z, z', m, m'),
     // so two 128-bit loads give the float2 operands of two interactions, which go
@@ -1220,9 +1250,9 @@ traverse_warp_kernel(TravArgs a_in)
             nb = make_float4(0.f, 0.f, 0.f, 0.f);
             if (j0 + 32 + lane < count) nb = load(j0 + 32 + lane);
             float *pl = reinterpret_cast<float *>(&tile[warp][lane & ~1]) + (lane & 1);
-            pl[0] = bj.x;
-            pl[2] = bj.y;
-            pl[4] = bj.z;
+            pl[0] = bj.x * sc;
+            pl[2] = bj.y * sc;
+            pl[4] = bj.z * sc;
             pl[6] = bj.w;
             __syncwarp();
             float2 sx = make_float2(0.f, 0.f), sy = sx, sz = sx;
@@ -1251,9 +1281,9 @@ traverse_warp_kernel(TravArgs a_in)
                 float4 c4 = make_float4(0.f, 0.f, 0.f, 0.f), qa = c4, qb = c4;
                 if (lane < m) {
                     const int c = -queue[warp][kGQueue - 1 - (j0 + lane)] - 1;
-                    c4 = a.nd.com[c];
-                    qa = a.nd.quad_a[c];
-                    qb = a.nd.quad_b[c];
+                    c4 = scaled(a.nd.com[c], sc);
+                    qa = scaled2(a.nd.quad_a[c], sc2);
+                    qb = scaled2(a.nd.quad_b[c], sc2);
                 }
                 const int slot = lane & ~1, half = lane & 1;
                 float *pc = reinterpret_cast<float *>(&tile[warp][slot]) + half;
@@ -1402,9 +1432,10 @@ traverse_warp_kernel(TravArgs a_in)
     }
     if (valid) {
         const uint32_t i = a.order[k];
-        a.partial[i] = (double)hx + (double)lx;
-        a.partial[a.n + i] = (double)hy + (double)ly;
-        a.partial[2 * (size_t)a.n + i] = (double)hz + (double)lz;
+        const double unsc = pow2d(-2 * a.sk);
+        a.partial[i] = ((double)hx + (double)lx) * unsc;
+        a.partial[a.n + i] = ((double)hy + (double)ly) * unsc;
+        a.partial[2 * (size_t)a.n + i] = ((double)hz + (double)lz) * unsc;
     }
 }
 
@@ -1685,6 +1716,9 @@ int bh_accelerations(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, 
     a.stats = ws->stats;
     a.quad = p.multipole == kMultipoleQuadrupole ? 1 : 0;
     a.com_theta = (float)p.com_theta;
+    a.sk = 0;  // set on the device with the extent
+    a.sc = 1.f;
+    a.es = a.e;
     PG_CUDA(cudaMemsetAsync(ws->stats, 0, 2 * sizeof(unsigned long long), st));
     const int blocks = cdiv(cdiv(n, 32), kTravWarps);
     // external records, so they also time the kernel when replayed from a graph

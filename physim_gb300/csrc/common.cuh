@@ -68,6 +68,13 @@ __device__ __forceinline__ float rsqrt_approx(float x)
     return y;
 }
 
+// 2^k as a float (|k| <= 126) and as a double (|k| <= 1022), exact.
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
+__device__ __forceinline__ double pow2d(int k)
+{
+    return __longlong_as_double((long long)(1023 + k) << 52);
+}
+
 // Knuth's TwoSum: s + err == a + b exactly.
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &err)
 {

@@ -12,6 +12,10 @@
 // exactly equal positions are skipped, as the force loop skips them.  Pair
 // separations are f64, pair terms FP32, per-body sums f64 per tile; every
 // other sum is f64.
+#include <string.h>
+
+#include <new>
+
 #include "common.cuh"
 #include "engine.h"
 
@@ -129,3 +133,71 @@ int launch_diagnostics(const DeviceBodies &b, double e, double *d_out, bool pote
 }
 
 }  // namespace pg
+
+// ---------------------------------------------------------------------------
+// Diagnostics of host Entity arrays (the energysink element's computation)
+// ---------------------------------------------------------------------------
+struct PhysimEnergy {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    pg::DeviceBodies b;
+    double *d_out = nullptr;
+};
+
+extern "C" int physim_gpu_energy_create(int32_t device, PhysimEnergy **out)
+{
+    PG_CHECK(out, PHYSIM_ERR_ARGUMENT, "null argument");
+    *out = nullptr;
+    PG_CUDA(cudaSetDevice(device));
+    PhysimEnergy *E = new (std::nothrow) PhysimEnergy();
+    PG_CHECK(E, PHYSIM_ERR_MEMORY, "out of host memory");
+    E->device = device;
+    if (cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete E;
+        pg::set_error("cudaStreamCreate failed");
+        return PHYSIM_ERR_CUDA;
+    }
+    *out = E;
+    return PHYSIM_OK;
+}
+
+extern "C" int physim_gpu_energy_compute(PhysimEnergy *E, const Entity *state, size_t n,
+                                         double e, int with_potential, PhysimDiagnostics *out)
+{
+    using namespace pg;
+    PG_CHECK(E && out && (state || n == 0), PHYSIM_ERR_ARGUMENT, "null argument");
+    PG_CHECK(n < (size_t)INT32_MAX, PHYSIM_ERR_ARGUMENT, "too many bodies: %zu", n);
+    memset(out, 0, sizeof *out);
+    if (n == 0) return PHYSIM_OK;
+    PG_CUDA(cudaSetDevice(E->device));
+    PG_TRY(bodies_reserve(E->b, n, true, E->stream));
+    if (!E->d_out) PG_TRY(dev_alloc(E->d_out, 9, E->stream));
+    PG_CUDA(cudaMemcpyAsync(E->b.aos, state, n * sizeof(Entity), cudaMemcpyHostToDevice,
+                            E->stream));
+    PG_TRY(launch_unpack(E->b, E->b.aos, n, true, E->stream));
+    PG_TRY(launch_diagnostics(E->b, fabs(e), E->d_out, with_potential != 0, E->device,
+                              E->stream));
+    double h[9];
+    PG_CUDA(cudaMemcpyAsync(h, E->d_out, sizeof h, cudaMemcpyDeviceToHost, E->stream));
+    PG_CUDA(cudaStreamSynchronize(E->stream));
+    out->mass = h[0];
+    for (int c = 0; c < 3; ++c) {
+        out->centre_of_mass[c] = h[0] != 0.0 ? h[1 + c] / h[0] : 0.0;
+        out->momentum[c] = h[4 + c];
+    }
+    out->kinetic = h[7];
+    out->potential = with_potential ? h[8] : 0.0;
+    out->energy = out->kinetic + out->potential;
+    return PHYSIM_OK;
+}
+
+extern "C" void physim_gpu_energy_destroy(PhysimEnergy *E)
+{
+    if (!E) return;
+    cudaSetDevice(E->device);
+    pg::bodies_free(E->b, E->stream);
+    pg::dev_free(E->d_out, E->stream);
+    cudaStreamSynchronize(E->stream);
+    cudaStreamDestroy(E->stream);
+    delete E;
+}

@@ -18,6 +18,8 @@
 // by the integrator kernel), which keeps the last wave of a GPU with 152 SMs
 // full.  Per-body sums are compensated: each j tile is summed in plain FP32
 // and folded into a (hi, lo) pair with TwoSum once per tile.
+#include <math.h>
+
 #include <algorithm>
 #include <atomic>
 
@@ -32,14 +34,57 @@ namespace {
 template <int BLOCK, int IPT, bool COMP>
 __global__ void __launch_bounds__(BLOCK, 2)
 direct_forces_kernel(const float4 *__restrict__ body, int n, int n_jtiles, int chunk_tiles, float e,
-                     double *__restrict__ partial)
+                     const PairScale *__restrict__ scale, double *__restrict__ partial)
 {
     __shared__ float4 tile[2][BLOCK][2];
     const int split = blockIdx.y;
     const int t0 = split * chunk_tiles;
     const int t1 = min(t0 + chunk_tiles, n_jtiles);
-    direct_tile<BLOCK, IPT, COMP>(body, n, blockIdx.x * BLOCK * IPT, t0, t1, e,
+    direct_tile<BLOCK, IPT, COMP>(body, n, blockIdx.x * BLOCK * IPT, t0, t1, e, scale->k,
                                   partial + (size_t)split * 3 * n, tile);
+}
+
+// Largest |coordinate| of body4[0, n) (f32 bit patterns order like the
+// non-negative values; NaN and infinities skipped), reduced by the last
+// block to finish into ps->k (see PairScale).
+__global__ void __launch_bounds__(256)
+pair_scale_kernel(const float4 *__restrict__ body, int n, float e, PairScale *ps)
+{
+    uint32_t m = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 b = body[i];
+        const uint32_t bx = __float_as_uint(b.x) & 0x7fffffffu;
+        const uint32_t by = __float_as_uint(b.y) & 0x7fffffffu;
+        const uint32_t bz = __float_as_uint(b.z) & 0x7fffffffu;
+        m = max(m, bx < 0x7f800000u ? bx : 0u);
+        m = max(m, by < 0x7f800000u ? by : 0u);
+        m = max(m, bz < 0x7f800000u ? bz : 0u);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ uint32_t wm[8];
+    __shared__ bool last;
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = max(m, wm[w]);
+        ps->blockmax[blockIdx.x] = m;
+        __threadfence();
+        last = atomicAdd(&ps->arrivals, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    uint32_t t = 0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+        t = max(t, __ldcg(&ps->blockmax[b]));
+    for (int o = 16; o > 0; o >>= 1) t = max(t, __shfl_xor_sync(0xffffffffu, t, o));
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) t = max(t, wm[w]);
+        ps->k = pair_scale_exp(__uint_as_float(t), e);
+        ps->arrivals = 0u;
+    }
 }
 
 struct Shape {
@@ -232,19 +277,43 @@ int record_event(cudaEvent_t ev, cudaStream_t stream)
     return PHYSIM_OK;
 }
 
-int launch_direct(const DirectPlan &plan, const float4 *body4, float e, double *partial,
-                  cudaStream_t stream, cudaEvent_t pairs_done)
+int launch_pair_scale(const float4 *body4, int n, float e, PairScale *ps, cudaStream_t stream)
+{
+    const int blocks = std::max(1, std::min(kScaleBlocks, (n + 2047) / 2048));
+    pair_scale_kernel<<<blocks, 256, 0, stream>>>(body4, n, e, ps);
+    PG_CUDA(cudaGetLastError());
+    return PHYSIM_OK;
+}
+
+float max_abs_coordinate(const Entity *state, size_t n)
+{
+    float m = 0.f;
+    for (size_t i = 0; i < n; ++i) {
+        const float c[3] = {(float)state[i].x, (float)state[i].y, (float)state[i].z};
+        for (float v : c) {
+            const float a = fabsf(v);
+            if (a <= 3.4028235e38f && a > m) m = a;  // NaN and infinities skipped
+        }
+    }
+    return m;
+}
+
+int launch_direct(const DirectPlan &plan, const float4 *body4, float e, PairScale *scale,
+                  double *partial, cudaStream_t stream, cudaEvent_t pairs_done)
 {
     if (plan.n <= 0) return PHYSIM_OK;
+    PG_CHECK(scale, PHYSIM_ERR_ARGUMENT, "no pair-scale workspace");
+    PG_TRY(launch_pair_scale(body4, plan.n, e, scale, stream));
     if (plan.symmetric)
-        return launch_direct_symmetric(plan, body4, e, partial, stream, pairs_done);
+        return launch_direct_symmetric(plan, body4, e, scale, partial, stream, pairs_done);
     dim3 grid(plan.n_itiles, plan.splits);
     void *fn = shape_kernel(plan.block, plan.ipt, plan.compensated);
     PG_CHECK(fn != nullptr, PHYSIM_ERR_ARGUMENT, "no direct-sum kernel for block %d ipt %d",
              plan.block, plan.ipt);
     int n = plan.n, njt = plan.n_jtiles, ct = plan.chunk_tiles;
+    const PairScale *sc = scale;
     void *args[] = {(void *)&body4, (void *)&n, (void *)&njt, (void *)&ct, (void *)&e,
-                    (void *)&partial};
+                    (void *)&sc, (void *)&partial};
     PG_CUDA(cudaLaunchKernel(fn, grid, dim3(plan.block), args, 0, stream));
     if (pairs_done) PG_TRY(record_event(pairs_done, stream));
     return PHYSIM_OK;

@@ -48,21 +48,23 @@ namespace {
 // 1,048,580 bodies: 274.5 ms per pass, against 300.9 ms for 4 warps of 8
 // bodies per thread on the same GPU (the shuffles per pair halve)
 __global__ void __launch_bounds__(kSymThreads, 3)
-direct_sym_kernel(const float4 *__restrict__ body, int n, float e, float *__restrict__ P)
+direct_sym_kernel(const float4 *__restrict__ body, int n, float e,
+                  const PairScale *__restrict__ scale, float *__restrict__ P)
 {
     __shared__ float jacc[kSymWarps][kSymTile][3];
     int I, J;
     unit_tiles(blockIdx.x, I, J);
+    const int sk = scale->k;
     if (I == J)
-        sym_tile_pair<true>(body, n, I, J, e, P, jacc);
+        sym_tile_pair<true>(body, n, I, J, e, sk, P, jacc);
     else
-        sym_tile_pair<false>(body, n, I, J, e, P, jacc);
+        sym_tile_pair<false>(body, n, I, J, e, sk, P, jacc);
 }
 
 // out[c*n + k] = sum over the T slots of P[t][c][k], TwoSum-compensated f32
-// in slot order, rounded once to f64.
+// in slot order, rounded once to f64 and unscaled (x 2^-2k).
 __global__ void sym_reduce_kernel(const float *__restrict__ P, long long n3, int T,
-                                  double *__restrict__ out)
+                                  const PairScale *__restrict__ scale, double *__restrict__ out)
 {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= n3) return;
@@ -76,7 +78,7 @@ __global__ void sym_reduce_kernel(const float *__restrict__ P, long long n3, int
         hi = s;
         lo += err;
     }
-    out[idx] = (double)hi + (double)lo;
+    out[idx] = ((double)hi + (double)lo) * pow2d(-2 * scale->k);
 }
 
 }  // namespace
@@ -118,7 +120,8 @@ size_t direct_partial_doubles(const DirectPlan &p)
 }
 
 int launch_direct_symmetric(const DirectPlan &plan, const float4 *body4, float e,
-                            double *partial, cudaStream_t stream, cudaEvent_t pairs_done)
+                            const PairScale *scale, double *partial, cudaStream_t stream,
+                            cudaEvent_t pairs_done)
 {
     if (plan.n <= 0) return PHYSIM_OK;
     const long long T = plan.tiles;
@@ -127,10 +130,11 @@ int launch_direct_symmetric(const DirectPlan &plan, const float4 *body4, float e
              plan.n);
     const long long n3 = 3ll * plan.n;
     float *P = (float *)(partial + n3);
-    direct_sym_kernel<<<(unsigned)units, kSymThreads, 0, stream>>>(body4, plan.n, e, P);
+    direct_sym_kernel<<<(unsigned)units, kSymThreads, 0, stream>>>(body4, plan.n, e, scale, P);
     PG_CUDA(cudaGetLastError());
     if (pairs_done) PG_TRY(record_event(pairs_done, stream));
-    sym_reduce_kernel<<<(unsigned)((n3 + 255) / 256), 256, 0, stream>>>(P, n3, (int)T, partial);
+    sym_reduce_kernel<<<(unsigned)((n3 + 255) / 256), 256, 0, stream>>>(P, n3, (int)T, scale,
+                                                                         partial);
     PG_CUDA(cudaGetLastError());
     return PHYSIM_OK;
 }

@@ -27,9 +27,11 @@ __device__ __forceinline__ void unit_tiles(long long u, int &I, int &J)
     I = (int)(u - j * (j + 1) / 2);
 }
 
+// The f32 slot sums are left scaled (a' of PairScale, positions entering as
+// p 2^-sk): the reduction multiplies by 2^-2sk in f64.
 template <bool DIAG>
 __device__ __forceinline__ void sym_tile_pair(const float4 *__restrict__ body, int n, int I,
-                                              int J, float e, float *__restrict__ P,
+                                              int J, float e, int sk, float *__restrict__ P,
                                               float (*jacc)[kSymTile][3])
 {
     constexpr int Q = kSymIpt / 2;
@@ -39,18 +41,20 @@ __device__ __forceinline__ void sym_tile_pair(const float4 *__restrict__ body, i
 
     // bodies I*1024 + p*128 + warp*32 + lane, p = 2q (x half) and 2q+1 (y half)
     const int ib = I * kSymTile + warp * 32 + lane;
+    const float sc = pow2f(-sk);  // 2^-sk, exact
     float2 nx[Q], ny[Q], nz[Q], nm[Q], ax[Q], ay[Q], az[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const float4 b0 = body[ib + (2 * q) * kSymThreads];
         const float4 b1 = body[ib + (2 * q + 1) * kSymThreads];
-        nx[q] = make_float2(-b0.x, -b1.x);
-        ny[q] = make_float2(-b0.y, -b1.y);
-        nz[q] = make_float2(-b0.z, -b1.z);
+        nx[q] = make_float2(-b0.x * sc, -b1.x * sc);
+        ny[q] = make_float2(-b0.y * sc, -b1.y * sc);
+        nz[q] = make_float2(-b0.z * sc, -b1.z * sc);
         nm[q] = make_float2(-b0.w, -b1.w);
         ax[q] = ay[q] = az[q] = make_float2(0.f, 0.f);
     }
-    const float2 e2 = make_float2(e, e);
+    const float es = e * pow2f(-2 * sk);
+    const float2 e2 = make_float2(es, es);
     const float2 g2 = make_float2(kPairGuard, kPairGuard);
     const unsigned full = 0xffffffffu;
     const int src = (lane + 1) & 31;
@@ -60,7 +64,7 @@ __device__ __forceinline__ void sym_tile_pair(const float4 *__restrict__ body, i
         const float4 bj = next;
         // the next group's body is loaded while this group is evaluated
         if (g + 1 < kSymGroups) next = body[J * kSymTile + (g + 1) * 32 + lane];
-        float xj = bj.x, yj = bj.y, zj = bj.z, mj = bj.w;
+        float xj = bj.x * sc, yj = bj.y * sc, zj = bj.z * sc, mj = bj.w;
         float2 jx = make_float2(0.f, 0.f), jy = jx, jz = jx;
 #pragma unroll 2
         for (int k = 0; k < 32; ++k) {

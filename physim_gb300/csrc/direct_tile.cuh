@@ -11,7 +11,8 @@
 // FMUL2.  j bodies are staged in shared memory as (x,x,y,y)(z,z,m,m) so one
 // 128-bit broadcast load yields the float2 operands.  Per-body sums are
 // compensated: each j tile is summed in plain FP32 and folded into a
-// (hi, lo) pair with TwoSum once per tile.
+// (hi, lo) pair with TwoSum once per tile.  Positions enter scaled by 2^-sk
+// and the sums leave scaled by 2^-2sk (PairScale in engine.h).
 #pragma once
 
 #include "common.cuh"
@@ -21,15 +22,18 @@ namespace pg {
 
 // One i tile of BLOCK*IPT bodies starting at i_base against the j tiles
 // [t0, t1) of `body` (n bodies, padded), writing this split's partial sums to
-// out[c*n + i].  `tile` is the block's shared staging buffer.
+// out[c*n + i].  `tile` is the block's shared staging buffer; sk the pair
+// scale exponent.
 template <int BLOCK, int IPT, bool COMP>
 __device__ __forceinline__ void direct_tile(const float4 *__restrict__ body, int n, int i_base,
-                                            int t0, int t1, float e, double *__restrict__ out,
-                                            float4 (*tile)[BLOCK][2])
+                                            int t0, int t1, float e, int sk,
+                                            double *__restrict__ out, float4 (*tile)[BLOCK][2])
 {
     static_assert(IPT % 2 == 0, "bodies per thread must be even (packed pairs)");
     constexpr int P = IPT / 2;
     const int tid = threadIdx.x;
+    const float sc = pow2f(-sk);     // 2^-sk, exact
+    const double unsc = pow2d(-2 * sk);  // back to unscaled accelerations
 
     float2 nx[P], ny[P], nz[P];
     float2 ax[P], ay[P], az[P];
@@ -39,22 +43,24 @@ __device__ __forceinline__ void direct_tile(const float4 *__restrict__ body, int
         // bodies i_base + tid + k*BLOCK, k = 2p, 2p+1 (rows padded, always readable)
         float4 b0 = body[i_base + tid + (2 * p) * BLOCK];
         float4 b1 = body[i_base + tid + (2 * p + 1) * BLOCK];
-        nx[p] = make_float2(-b0.x, -b1.x);
-        ny[p] = make_float2(-b0.y, -b1.y);
-        nz[p] = make_float2(-b0.z, -b1.z);
+        nx[p] = make_float2(-b0.x * sc, -b1.x * sc);
+        ny[p] = make_float2(-b0.y * sc, -b1.y * sc);
+        nz[p] = make_float2(-b0.z * sc, -b1.z * sc);
         ax[p] = ay[p] = az[p] = make_float2(0.f, 0.f);
         hx[p] = hy[p] = hz[p] = make_float2(0.f, 0.f);
         lx[p] = ly[p] = lz[p] = make_float2(0.f, 0.f);
     }
-    const float2 e2 = make_float2(e, e);
+    const float es = e * pow2f(-2 * sk);
+    const float2 e2 = make_float2(es, es);
     const float2 g2 = make_float2(kPairGuard, kPairGuard);
 
     if (t0 < t1) {
         float4 nxt = body[t0 * BLOCK + tid];
         for (int t = t0; t < t1; ++t) {
             const int buf = (t - t0) & 1;
-            tile[buf][tid][0] = make_float4(nxt.x, nxt.x, nxt.y, nxt.y);
-            tile[buf][tid][1] = make_float4(nxt.z, nxt.z, nxt.w, nxt.w);
+            const float sx = nxt.x * sc, sy = nxt.y * sc, sz = nxt.z * sc;
+            tile[buf][tid][0] = make_float4(sx, sx, sy, sy);
+            tile[buf][tid][1] = make_float4(sz, sz, nxt.w, nxt.w);
             __syncthreads();
             if (t + 1 < t1) nxt = body[(t + 1) * BLOCK + tid];
 #pragma unroll 4
@@ -114,14 +120,14 @@ __device__ __forceinline__ void direct_tile(const float4 *__restrict__ body, int
         const int i0 = i_base + tid + (2 * p) * BLOCK;
         const int i1 = i0 + BLOCK;
         if (i0 < n) {
-            px[i0] = (double)hx[p].x + (double)lx[p].x;
-            py[i0] = (double)hy[p].x + (double)ly[p].x;
-            pz[i0] = (double)hz[p].x + (double)lz[p].x;
+            px[i0] = ((double)hx[p].x + (double)lx[p].x) * unsc;
+            py[i0] = ((double)hy[p].x + (double)ly[p].x) * unsc;
+            pz[i0] = ((double)hz[p].x + (double)lz[p].x) * unsc;
         }
         if (i1 < n) {
-            px[i1] = (double)hx[p].y + (double)lx[p].y;
-            py[i1] = (double)hy[p].y + (double)ly[p].y;
-            pz[i1] = (double)hz[p].y + (double)lz[p].y;
+            px[i1] = ((double)hx[p].y + (double)lx[p].y) * unsc;
+            py[i1] = ((double)hy[p].y + (double)ly[p].y) * unsc;
+            pz[i1] = ((double)hz[p].y + (double)lz[p].y) * unsc;
         }
     }
 }

@@ -75,7 +75,8 @@ static int accumulate_locked(ElementState *el, const Entity *state, size_t n, Ac
         }
         PG_TRY(rc);
         splits = el->plan.splits;
-        PG_TRY(launch_direct(el->plan, el->bodies.body4, (float)el->e, el->partial, st));
+        PG_TRY(launch_direct(el->plan, el->bodies.body4, (float)el->e, el->bodies.scale,
+                             el->partial, st));
     } else {
         PG_TRY(ensure_doubles(el->partial, el->partial_cap, 3 * n, st));
         PG_TRY(bh_reserve(el->bh, n, el->device, el->leaf_size, st));

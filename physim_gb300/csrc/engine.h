@@ -18,10 +18,67 @@ inline size_t pad_bodies(size_t n) { return (n + kBodyPad - 1) / kBodyPad * kBod
 // Guard added to r^2 (r^2 + e)^2 before the reciprocal square root.  It makes
 // the contribution of a body at exactly the same position zero (dx = 0 times
 // a finite factor), which is the reference's "skip equal centres" rule
-// (astro/src/transformers.rs:145,230), without a per-pair branch.  It is below
-// FLT_MIN * 10, so it changes no pair whose r^2 (r^2 + e)^2 exceeds 1e-30 by
-// more than 1e-7 relative.
-constexpr float kPairGuard = 1.0e-37f;
+// (astro/src/transformers.rs:145,230), without a per-pair branch.  It is the
+// smallest normal float, so it changes no pair whose (scaled, see PairScale)
+// r^2 (r^2 + e)^2 exceeds 1.2e-31 by more than 1e-7 relative.
+constexpr float kPairGuard = 1.17549435e-38f;
+
+// ------------------------------------------------------------------------
+// Power-of-two scaling of the pair law
+// ------------------------------------------------------------------------
+// The pair kernels evaluate r^2 (r^2 + e)^2 in FP32, which spans six times
+// the exponent range of the coordinates: unscaled it overflows for
+// separations above ~2.6e6 and underflows (e = 0) below ~5e-7.  So positions
+// enter the pair arithmetic as p' = p 2^-k, with k chosen per force pass so
+// the largest |coordinate| m of the state maps into [0.5, 1), the easing as
+// e' = e 2^-2k, and the accelerations leave as a = a' 2^-2k -- every factor
+// a power of two, so no bits are lost and a state that was in range before
+// gives the same results.  k is clamped so that e' <= 2^60 (r'^2 (r'^2 +
+// e')^2 then stays finite) and |k| <= 100.  What remains: with e = 0, pairs
+// closer than ~3e-6 m lose accuracy beyond 1e-5 relative, and closer than
+// ~5e-7 m they contribute almost nothing (r'^6 underflows into the guard).
+constexpr int kScaleBlocks = 256;
+struct PairScale {
+    int32_t k;          // scale exponent of the current state
+    uint32_t arrivals;  // blocks of a running scale pass that finished (reset by the last)
+    uint32_t blockmax[kScaleBlocks];  // per-block max |coordinate| (f32 bit patterns)
+};
+
+// Exponent of the largest |coordinate| m: m = f 2^k, f in [0.5, 1) (0 for m = 0).
+__host__ __device__ inline int coord_exp(float m)
+{
+    int k = 0;
+    if (m > 0.f && m <= 3.4028235e38f) (void)frexpf(m, &k);
+    return k;
+}
+
+// The scale exponent for coordinate exponent kx and easing e: kx, raised so
+// that e 2^-2k <= 2^60, within [-100, 100].
+__host__ __device__ inline int pair_scale_from(int kx, float e)
+{
+    int k = kx;
+    if (e > 0.f && e <= 3.4028235e38f) {
+        int ke = 0;
+        (void)frexpf(e, &ke);  // e < 2^ke
+        const int kmin = (ke - 60 + 1) >> 1;  // ceil((ke - 60) / 2)
+        if (k < kmin) k = kmin;
+    }
+    return k < -100 ? -100 : (k > 100 ? 100 : k);
+}
+
+__host__ __device__ inline int pair_scale_exp(float m, float e)
+{
+    return pair_scale_from(coord_exp(m), e);
+}
+
+// Computes ps->k for the n bodies of body4 (max over |x|, |y|, |z|; NaN and
+// infinite coordinates skipped) and easing e, on `stream`: one launch whose
+// last block to finish reduces the per-block maxima.  ps->arrivals must be 0
+// before the first pass (it is left 0).
+int launch_pair_scale(const float4 *body4, int n, float e, PairScale *ps, cudaStream_t stream);
+// The same pass over the bodies of several members of an ensemble is done by
+// its integrator kernel; a host-side value for a state being uploaded:
+float max_abs_coordinate(const Entity *state, size_t n);
 
 // ------------------------------------------------------------------------
 // Direct sum (simple_astro)
@@ -65,10 +122,13 @@ size_t direct_partial_doubles(const DirectPlan &plan);
 // s < plan.splits holds the partial sums.  pairs_done (optional) is recorded
 // on `stream` right after the pair kernel, before any reduction of its
 // output (as an external event node when the stream is being captured).
-int launch_direct(const DirectPlan &plan, const float4 *body4, float e, double *partial,
-                  cudaStream_t stream, cudaEvent_t pairs_done = nullptr);
+// Before the pair kernel, launch_direct runs the scale pass of body4 into
+// `scale` (see PairScale); the partial sums come out unscaled.
+int launch_direct(const DirectPlan &plan, const float4 *body4, float e, PairScale *scale,
+                  double *partial, cudaStream_t stream, cudaEvent_t pairs_done = nullptr);
 int launch_direct_symmetric(const DirectPlan &plan, const float4 *body4, float e,
-                            double *partial, cudaStream_t stream, cudaEvent_t pairs_done);
+                            const PairScale *scale, double *partial, cudaStream_t stream,
+                            cudaEvent_t pairs_done);
 // Records `ev` on `stream`; inside a stream capture as an external event node.
 int record_event(cudaEvent_t ev, cudaStream_t stream);
 
@@ -86,6 +146,7 @@ struct DeviceBodies {
     double *radius = nullptr;
     uint64_t *id = nullptr;
     Entity *aos = nullptr;  // staging for host<->device copies
+    PairScale *scale = nullptr;  // pair-law scale of the direct-sum kernels
 };
 
 // Stream-ordered device memory (cudaMallocAsync / cudaFreeAsync on the

@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(BLOCK, 2)
 ensemble_forces_kernel(const float4 *__restrict__ body4, const MemberInfo *__restrict__ members,
                        const WorkUnit *__restrict__ units, int n_units,
                        const unsigned long long *__restrict__ remaining, int *__restrict__ counter,
-                       double *__restrict__ partial)
+                       const int32_t *__restrict__ member_kx, double *__restrict__ partial)
 {
     __shared__ float4 tile[2][BLOCK][2];
     __shared__ int next;
@@ -76,6 +76,7 @@ ensemble_forces_kernel(const float4 *__restrict__ body4, const MemberInfo *__res
             const int t0 = w.split * m.chunk_tiles;
             const int t1 = min(t0 + m.chunk_tiles, m.n_jtiles);
             direct_tile<BLOCK, IPT, COMP>(body4 + m.off, m.n, w.itile * BLOCK * IPT, t0, t1, m.e,
+                                          pair_scale_from(member_kx[w.member], m.e),
                                           partial + m.poff + (size_t)w.split * 3 * m.n, tile);
         }
         __syncthreads();
@@ -86,7 +87,7 @@ __global__ void __launch_bounds__(kSymThreads, 3)
 ensemble_sym_kernel(const float4 *__restrict__ body4, const MemberInfo *__restrict__ members,
                     const SymUnit *__restrict__ units, int n_units,
                     const unsigned long long *__restrict__ remaining, int *__restrict__ counter,
-                    float *__restrict__ slots)
+                    const int32_t *__restrict__ member_kx, float *__restrict__ slots)
 {
     __shared__ float jacc[kSymWarps][kSymTile][3];
     __shared__ int next;
@@ -98,10 +99,11 @@ ensemble_sym_kernel(const float4 *__restrict__ body4, const MemberInfo *__restri
         const SymUnit w = units[u];
         if (remaining[w.member] != 0) {
             const MemberInfo m = members[w.member];
+            const int sk = pair_scale_from(member_kx[w.member], m.e);
             if (w.I == w.J)
-                sym_tile_pair<true>(body4 + m.off, m.n, w.I, w.J, m.e, slots + m.soff, jacc);
+                sym_tile_pair<true>(body4 + m.off, m.n, w.I, w.J, m.e, sk, slots + m.soff, jacc);
             else
-                sym_tile_pair<false>(body4 + m.off, m.n, w.I, w.J, m.e, slots + m.soff, jacc);
+                sym_tile_pair<false>(body4 + m.off, m.n, w.I, w.J, m.e, sk, slots + m.soff, jacc);
         }
         __syncthreads();
     }
@@ -109,7 +111,10 @@ ensemble_sym_kernel(const float4 *__restrict__ body4, const MemberInfo *__restri
 
 // Combine + verlet for every member with steps left (verlet.rs:24-82; the
 // first step after an upload is the Taylor step).  slot_member[s] < 0 marks
-// padding.
+// padding.  Each warp also folds the largest |coordinate| of its new f32
+// positions into member_ext of its member (members are padded to whole
+// 1,024-slot tiles, so a warp's slots belong to one member); the count
+// kernel turns it into the member's next pair scale.
 __global__ void ensemble_verlet_kernel(float4 *body4, const double *__restrict__ mass,
                                        const uint8_t *__restrict__ fixed,
                                        const int32_t *__restrict__ slot_member,
@@ -119,74 +124,96 @@ __global__ void ensemble_verlet_kernel(float4 *body4, const double *__restrict__
                                        const double *__restrict__ partial,
                                        const float *__restrict__ slot_sums, int slots, double *x,
                                        double *y, double *z, double *vx, double *vy, double *vz,
-                                       double *px, double *py, double *pz)
+                                       double *px, double *py, double *pz,
+                                       const int32_t *__restrict__ member_kx,
+                                       uint32_t *__restrict__ member_ext)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= slots) return;
-    const int k = slot_member[s];
-    if (k < 0 || remaining[k] == 0) return;
-    const MemberInfo m = members[k];
-    const int i = s - m.off;
-    double ax = 0.0, ay = 0.0, az = 0.0;
-    if (!fixed[s]) {
-        if (m.sym_tiles > 0) {
-            // the member's slot sums, TwoSum-compensated in slot order
-            const size_t n3 = 3 * (size_t)m.n;
-            const float *p = slot_sums + m.soff + i;
-            float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
-            for (int t = 0; t < m.sym_tiles; ++t)
-                for (int c = 0; c < 3; ++c) {
-                    float sum, err;
-                    two_sum(h[c], p[(size_t)t * n3 + (size_t)c * m.n], sum, err);
-                    h[c] = sum;
-                    l[c] += err;
+    const int k = s < slots ? slot_member[s] : -1;
+    const bool active = k >= 0 && remaining[k] != 0;
+    uint32_t ext = 0;
+    if (active) {
+        const MemberInfo m = members[k];
+        const int i = s - m.off;
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        if (!fixed[s]) {
+            if (m.sym_tiles > 0) {
+                // the member's slot sums, TwoSum-compensated in slot order, unscaled
+                const size_t n3 = 3 * (size_t)m.n;
+                const float *p = slot_sums + m.soff + i;
+                float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
+                for (int t = 0; t < m.sym_tiles; ++t)
+                    for (int c = 0; c < 3; ++c) {
+                        float sum, err;
+                        two_sum(h[c], p[(size_t)t * n3 + (size_t)c * m.n], sum, err);
+                        h[c] = sum;
+                        l[c] += err;
+                    }
+                const double unsc = pow2d(-2 * pair_scale_from(member_kx[k], m.e));
+                ax = ((double)h[0] + (double)l[0]) * unsc;
+                ay = ((double)h[1] + (double)l[1]) * unsc;
+                az = ((double)h[2] + (double)l[2]) * unsc;
+            } else {
+                for (int sp = 0; sp < m.splits; ++sp) {
+                    const double *p = partial + m.poff + (size_t)sp * 3 * m.n;
+                    ax += p[i];
+                    ay += p[m.n + i];
+                    az += p[2 * (size_t)m.n + i];
                 }
-            ax = (double)h[0] + (double)l[0];
-            ay = (double)h[1] + (double)l[1];
-            az = (double)h[2] + (double)l[2];
-        } else {
-            for (int sp = 0; sp < m.splits; ++sp) {
-                const double *p = partial + m.poff + (size_t)sp * 3 * m.n;
-                ax += p[i];
-                ay += p[m.n + i];
-                az += p[2 * (size_t)m.n + i];
             }
+            if (mass[s] == 0.0) ax = ay = az = __longlong_as_double(0x7ff8000000000000LL);
         }
-        if (mass[s] == 0.0) ax = ay = az = __longlong_as_double(0x7ff8000000000000LL);
-    }
-    const bool initial = done[k] == 0;
-    const double dt = m.dt, dt2 = __dmul_rn(dt, dt);
-    double q[3] = {x[s], y[s], z[s]}, v[3] = {vx[s], vy[s], vz[s]}, pr[3] = {px[s], py[s], pz[s]};
-    const double a[3] = {ax, ay, az};
-    for (int c = 0; c < 3; ++c) {
-        double xn, vn;
-        if (initial) {
-            xn = __dadd_rn(__dadd_rn(q[c], __dmul_rn(v[c], dt)), __dmul_rn(__dmul_rn(0.5, a[c]), dt2));
-            vn = __dadd_rn(v[c], __dmul_rn(a[c], dt));
-        } else {
-            xn = __dadd_rn(__dsub_rn(__dmul_rn(2.0, q[c]), pr[c]), __dmul_rn(a[c], dt2));
-            vn = __ddiv_rn(__dsub_rn(xn, q[c]), dt);
+        const bool initial = done[k] == 0;
+        const double dt = m.dt, dt2 = __dmul_rn(dt, dt);
+        double q[3] = {x[s], y[s], z[s]}, v[3] = {vx[s], vy[s], vz[s]},
+               pr[3] = {px[s], py[s], pz[s]};
+        const double a[3] = {ax, ay, az};
+        for (int c = 0; c < 3; ++c) {
+            double xn, vn;
+            if (initial) {
+                xn = __dadd_rn(__dadd_rn(q[c], __dmul_rn(v[c], dt)),
+                               __dmul_rn(__dmul_rn(0.5, a[c]), dt2));
+                vn = __dadd_rn(v[c], __dmul_rn(a[c], dt));
+            } else {
+                xn = __dadd_rn(__dsub_rn(__dmul_rn(2.0, q[c]), pr[c]), __dmul_rn(a[c], dt2));
+                vn = __ddiv_rn(__dsub_rn(xn, q[c]), dt);
+            }
+            pr[c] = q[c];
+            q[c] = xn;
+            v[c] = vn;
         }
-        pr[c] = q[c];
-        q[c] = xn;
-        v[c] = vn;
+        x[s] = q[0]; y[s] = q[1]; z[s] = q[2];
+        vx[s] = v[0]; vy[s] = v[1]; vz[s] = v[2];
+        px[s] = pr[0]; py[s] = pr[1]; pz[s] = pr[2];
+        float4 b = body4[s];
+        b.x = (float)q[0];
+        b.y = (float)q[1];
+        b.z = (float)q[2];
+        body4[s] = b;
+        const uint32_t ex = __float_as_uint(b.x) & 0x7fffffffu;
+        const uint32_t ey = __float_as_uint(b.y) & 0x7fffffffu;
+        const uint32_t ez = __float_as_uint(b.z) & 0x7fffffffu;
+        ext = max(ext, ex < 0x7f800000u ? ex : 0u);  // NaN and infinities skipped
+        ext = max(ext, ey < 0x7f800000u ? ey : 0u);
+        ext = max(ext, ez < 0x7f800000u ? ez : 0u);
     }
-    x[s] = q[0]; y[s] = q[1]; z[s] = q[2];
-    vx[s] = v[0]; vy[s] = v[1]; vz[s] = v[2];
-    px[s] = pr[0]; py[s] = pr[1]; pz[s] = pr[2];
-    float4 b = body4[s];
-    b.x = (float)q[0];
-    b.y = (float)q[1];
-    b.z = (float)q[2];
-    body4[s] = b;
+    const uint32_t wext = __reduce_max_sync(0xffffffffu, ext);
+    const int wk = (int)__reduce_max_sync(0xffffffffu, (uint32_t)(k + 1)) - 1;
+    const bool any = __any_sync(0xffffffffu, active);
+    if ((threadIdx.x & 31) == 0 && any && wk >= 0 && wext != 0) atomicMax(&member_ext[wk], wext);
 }
 
 __global__ void ensemble_count_kernel(unsigned long long *remaining, unsigned long long *done,
-                                      int count, int *counter)
+                                      int count, int *counter, int32_t *member_kx,
+                                      uint32_t *member_ext)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k == 0) counter[0] = counter[1] = 0;  // the next step's work queues start empty
     if (k >= count || remaining[k] == 0) return;
+    // the pair scale of the member's new positions (kept if all sit at the origin)
+    const uint32_t ext = member_ext[k];
+    if (ext != 0u) member_kx[k] = coord_exp(__uint_as_float(ext));
+    member_ext[k] = 0u;
     done[k] += 1;
     if (remaining[k] != ~0ull) remaining[k] -= 1;
 }
@@ -304,6 +331,8 @@ struct PhysimEnsemble {
     size_t units_cap = 0;
     unsigned long long *remaining = nullptr, *done = nullptr;
     int *counter = nullptr;  // [0] one-pair units, [1] symmetric units
+    int32_t *member_kx = nullptr;    // coordinate exponent of each member's pair scale
+    uint32_t *member_ext = nullptr;  // largest |coordinate| of the new positions (f32 bits)
     double *partial = nullptr;
     SymUnit *d_sym_units = nullptr;
     int n_sym_units = 0;
@@ -447,7 +476,7 @@ int launch_forces(PhysimEnsemble *E)
     if (E->n_sym_units > 0) {
         ensemble_sym_kernel<<<std::min(E->sym_grid, E->n_sym_units), kSymThreads, 0, E->stream>>>(
             E->body4, E->d_members, E->d_sym_units, E->n_sym_units, E->remaining, E->counter + 1,
-            E->slot_sums);
+            E->member_kx, E->slot_sums);
         PG_CUDA(cudaGetLastError());
     }
     if (E->n_units == 0) return PHYSIM_OK;
@@ -455,7 +484,7 @@ int launch_forces(PhysimEnsemble *E)
     PG_CHECK(fn, PHYSIM_ERR_ARGUMENT, "no ensemble kernel for %d x %d", E->block, E->ipt);
     void *args[] = {(void *)&E->body4, (void *)&E->d_members, (void *)&E->d_units,
                     (void *)&E->n_units, (void *)&E->remaining, (void *)&E->counter,
-                    (void *)&E->partial};
+                    (void *)&E->member_kx, (void *)&E->partial};
     PG_CUDA(cudaLaunchKernel(fn, dim3(E->grid), dim3(E->block), args, 0, E->stream));
     return PHYSIM_OK;
 }
@@ -466,9 +495,10 @@ int enqueue_step(PhysimEnsemble *E)
     const int t = 256;
     ensemble_verlet_kernel<<<cdiv(E->slots, t), t, 0, E->stream>>>(
         E->body4, E->m, E->fixed, E->slot_member, E->d_members, E->remaining, E->done, E->partial,
-        E->slot_sums, E->slots, E->x, E->y, E->z, E->vx, E->vy, E->vz, E->px, E->py, E->pz);
+        E->slot_sums, E->slots, E->x, E->y, E->z, E->vx, E->vy, E->vz, E->px, E->py, E->pz,
+        E->member_kx, E->member_ext);
     ensemble_count_kernel<<<cdiv((long long)E->members.size(), 256), 256, 0, E->stream>>>(
-        E->remaining, E->done, (int)E->members.size(), E->counter);
+        E->remaining, E->done, (int)E->members.size(), E->counter, E->member_kx, E->member_ext);
     PG_CUDA(cudaGetLastError());
     return PHYSIM_OK;
 }
@@ -479,7 +509,7 @@ void free_ensemble(PhysimEnsemble *E)
     void *p[] = {E->body4, E->fixed, E->x,  E->y,  E->z,  E->vx, E->vy, E->vz, E->px, E->py,
                  E->pz,    E->m,     E->radius, E->id, E->slot_member, E->d_members, E->d_units,
                  E->remaining, E->done, E->counter, E->partial, E->staging,
-                 E->d_sym_units, E->slot_sums};
+                 E->d_sym_units, E->slot_sums, E->member_kx, E->member_ext};
     for (void *q : p) dev_free(q, E->stream);
     if (E->stream) cudaStreamSynchronize(E->stream);
 }
@@ -557,6 +587,8 @@ int physim_gpu_ensemble_create(const PhysimSimConfig *cfg, const size_t *sizes, 
     EA(E->remaining, count);
     EA(E->done, count);
     EA(E->counter, 2);
+    EA(E->member_kx, count);
+    EA(E->member_ext, count);
     EA(E->partial, partial_elems);
 #undef EA
     if (rc == PHYSIM_OK) {
@@ -569,6 +601,8 @@ int physim_gpu_ensemble_create(const PhysimSimConfig *cfg, const size_t *sizes, 
             cudaMemsetAsync(E->fixed, 1, slots, E->stream) != cudaSuccess ||
             cudaMemsetAsync(E->m, 0, slots * sizeof(double), E->stream) != cudaSuccess ||
             cudaMemsetAsync(E->counter, 0, 2 * sizeof(int), E->stream) != cudaSuccess ||
+            cudaMemsetAsync(E->member_kx, 0, count * sizeof(int32_t), E->stream) != cudaSuccess ||
+            cudaMemsetAsync(E->member_ext, 0, count * sizeof(uint32_t), E->stream) != cudaSuccess ||
             cudaMemcpyAsync(E->slot_member, map.data(), map.size() * sizeof(int32_t),
                             cudaMemcpyHostToDevice, E->stream) != cudaSuccess ||
             cudaMemcpyAsync(E->remaining, rem.data(), count * sizeof(unsigned long long),
@@ -612,6 +646,13 @@ int physim_gpu_ensemble_upload(PhysimEnsemble *E, size_t index, const Entity *st
         E->radius, E->id);
     PG_CUDA(cudaGetLastError());
     const unsigned long long zero = 0ull, all = ~0ull;
+    // pair scale of the uploaded positions (the integrator keeps it current)
+    const int32_t kx = coord_exp(max_abs_coordinate(state, n));
+    const uint32_t zero32 = 0u;
+    PG_CUDA(cudaMemcpyAsync(E->member_kx + index, &kx, sizeof kx, cudaMemcpyHostToDevice,
+                            E->stream));
+    PG_CUDA(cudaMemcpyAsync(E->member_ext + index, &zero32, sizeof zero32,
+                            cudaMemcpyHostToDevice, E->stream));
     PG_CUDA(cudaMemcpyAsync(E->done + index, &zero, sizeof zero, cudaMemcpyHostToDevice,
                             E->stream));
     PG_CUDA(cudaMemcpyAsync(E->remaining + index, &all, sizeof all, cudaMemcpyHostToDevice,

@@ -463,8 +463,8 @@ int host_direct(int device, bool *direct)
 
 void bodies_free(DeviceBodies &b, cudaStream_t stream)
 {
-    void *ptrs[] = {b.body4, b.fixed, b.x,  b.y,  b.z,      b.vx, b.vy,
-                    b.vz,    b.px,    b.py, b.pz, b.m,      b.radius, b.id, b.aos};
+    void *ptrs[] = {b.body4, b.fixed, b.x,  b.y,  b.z,      b.vx, b.vy,    b.vz,
+                    b.px,    b.py,    b.pz, b.m,  b.radius, b.id, b.aos, b.scale};
     for (void *p : ptrs) dev_free(p, stream);
     b = DeviceBodies();
 }
@@ -483,6 +483,8 @@ int bodies_reserve(DeviceBodies &b, size_t n, bool with_state, cudaStream_t stre
     PG_TRY(dev_alloc(b.fixed, need, stream));
     PG_TRY(dev_alloc(b.aos, need, stream));
     PG_TRY(dev_alloc(b.m, need, stream));
+    PG_TRY(dev_alloc(b.scale, 1, stream));
+    PG_CUDA(cudaMemsetAsync(b.scale, 0, sizeof(PairScale), stream));
     if (with_state) {
         double **d[] = {&b.x, &b.y, &b.z, &b.vx, &b.vy, &b.vz, &b.px, &b.py, &b.pz, &b.radius};
         for (double **p : d) PG_TRY(dev_alloc(*p, need, stream));

@@ -10,6 +10,8 @@
 // touched until the first transform, because physim instantiates every
 // element once with "{}" while scanning plugins (discover.rs:375-393).
 #include <dlfcn.h>
+
+#include <atomic>
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -278,20 +280,31 @@ bool parse_object(const uint8_t *text, size_t len, std::map<std::string, Value> 
 // ------------------------------------------------------------------------
 static void *g_bus_target = nullptr;
 typedef void (*PostBusFn)(void *, CMessage);
+static std::atomic<PhysimBusFn> g_bus_override{nullptr};
 
 static void post_configuration(const void *sender)
 {
     // transformers.rs:107-111,198-203,266-270: (Low, "energysink", "gravity").
     if (!g_bus_target) return;
-    PostBusFn post = (PostBusFn)dlsym(RTLD_DEFAULT, "post_bus_callback");
-    if (!post) return;
     CMessage msg;
     msg.priority = PHYSIM_PRIORITY_LOW;
     msg.topic = "energysink";
     msg.message = "gravity";
     msg.sender_id = (uintptr_t)sender;
     msg.origin = PHYSIM_ORIGIN_C;  // the host must not free these strings
+    if (PhysimBusFn own = g_bus_override.load()) {
+        own(g_bus_target, &msg);
+        return;
+    }
+    PostBusFn post = (PostBusFn)dlsym(RTLD_DEFAULT, "post_bus_callback");
+    if (!post) return;
     post(g_bus_target, msg);
+}
+
+extern "C" int physim_gpu_set_bus_callback(PhysimBusFn fn)
+{
+    g_bus_override.store(fn);
+    return PHYSIM_OK;
 }
 
 // ------------------------------------------------------------------------

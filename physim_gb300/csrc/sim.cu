@@ -79,7 +79,7 @@ int sim_forces(PhysimSim *s, int *splits_out)
     const PhysimSimConfig &c = s->cfg;
     if (c.gravity == PHYSIM_GRAVITY_SIMPLE_ASTRO) {
         *splits_out = s->plan.splits;
-        return launch_direct(s->plan, s->b.body4, (float)c.e, s->partial, s->stream,
+        return launch_direct(s->plan, s->b.body4, (float)c.e, s->b.scale, s->partial, s->stream,
                              s->profiling ? s->ev[3] : nullptr);
     }
     BhParams p;
@@ -372,7 +372,8 @@ int physim_gpu_sim_autotune(PhysimSim *s, PhysimDirectTuning *out)
         for (int rep = 0; rep < 3 && rc == PHYSIM_OK; ++rep) {
             if (cudaEventRecord(a, s->stream) != cudaSuccess) rc = PHYSIM_ERR_CUDA;
             if (rc == PHYSIM_OK)
-                rc = launch_direct(cand[c], s->b.body4, (float)s->cfg.e, s->partial, s->stream);
+                rc = launch_direct(cand[c], s->b.body4, (float)s->cfg.e, s->b.scale, s->partial,
+                                   s->stream);
             if (rc == PHYSIM_OK && (cudaEventRecord(b, s->stream) != cudaSuccess ||
                                     cudaEventSynchronize(b) != cudaSuccess))
                 rc = PHYSIM_ERR_CUDA;

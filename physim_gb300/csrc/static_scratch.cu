@@ -26,7 +26,8 @@ constexpr size_t kStaticPad = (kStaticMaxBodies + kBodyPad - 1) / kBodyPad * kBo
 constexpr size_t kOffBody4 = 0;
 constexpr size_t kOffMass = align256(kOffBody4 + kStaticPad * sizeof(float4));
 constexpr size_t kOffFixed = align256(kOffMass + kStaticPad * sizeof(double));
-constexpr size_t kOffPartial = align256(kOffFixed + kStaticPad);
+constexpr size_t kOffScale = align256(kOffFixed + kStaticPad);
+constexpr size_t kOffPartial = align256(kOffScale + sizeof(PairScale));
 constexpr size_t kStaticBytes =
     align256(kOffPartial + (size_t)kStaticMaxSplits * 3 * kStaticMaxBodies * sizeof(double));
 
@@ -84,10 +85,14 @@ extern "C" int physim_gpu_simple_astro_accumulate_static(const Entity *state, si
     view.m = (double *)(base + kOffMass);
     view.fixed = (uint8_t *)(base + kOffFixed);
     double *partial = (double *)(base + kOffPartial);
+    PairScale *scale = (PairScale *)(base + kOffScale);
 
     // The f32 copy is rewritten for all padded slots (zero mass past n), and
-    // every partial sum is overwritten by the pair kernel: no scratch needs
-    // clearing from an earlier call.
+    // every partial sum is overwritten by the pair kernel.  The scale pass's
+    // arrival count must start at zero: it is left at zero by every completed
+    // pass, and cleared here as well (a memset, not an allocation), so a call
+    // after an interrupted one still starts clean.
+    PG_CUDA(cudaMemsetAsync(&scale->arrivals, 0, sizeof(uint32_t), st));
     PG_TRY(launch_unpack(view, state, n, false, st));
     const int sms = device_sm_count(device);
     const int block = 128, ipt = 4;
@@ -97,7 +102,7 @@ extern "C" int physim_gpu_simple_astro_accumulate_static(const Entity *state, si
     const DirectPlan plan = make_direct_plan((int)n, block, ipt, splits, true);
     PG_CHECK(plan.splits <= kStaticMaxSplits, PHYSIM_ERR_ARGUMENT, "internal: %d splits",
              plan.splits);
-    PG_TRY(launch_direct(plan, view.body4, (float)fabs(e), partial, st));
+    PG_TRY(launch_direct(plan, view.body4, (float)fabs(e), scale, partial, st));
     PG_TRY(launch_accumulate_aos(view, partial, plan.splits, acc, st));
     return PHYSIM_OK;
 }

@@ -103,6 +103,49 @@ class TransformElementHandler:
         self.destroy()
 
 
+class MessageBus:
+    """Host-side mirror of physim's message bus (physim-core/src/messages.rs:
+    201-271) for the configuration messages the gravity elements post
+    (transformers.rs:107-111,198-203,266-270).  While installed (a `with`
+    block) the library hands those messages here through
+    physim_gpu_set_bus_callback instead of physim's `post_bus_callback`;
+    `deliver` then calls `recv_message(topic, message, priority, sender)` of
+    every client, as physim's message thread does (pipeline.rs:113-127)."""
+
+    # the bus pointer handed to set_callback_target (physim passes its
+    # Arc<Mutex<MessageBus>>; the library only hands it back); it stays set
+    # after the block, as set_callback_target rejects NULL (c_plugin/plugin.c)
+    _TARGET = C.c_int(0)
+
+    def __init__(self):
+        self.messages: list[tuple[int, str, str, int, int]] = []
+        self._pending: list[tuple[int, str, str, int, int]] = []
+        self._cb = _lib.BusFn(self._post)
+
+    def _post(self, target, msg) -> None:
+        m = msg.contents
+        rec = (m.priority, m.topic.decode(), m.message.decode(), m.sender_id or 0, m.origin)
+        self.messages.append(rec)
+        self._pending.append(rec)
+
+    def deliver(self, clients: Iterable) -> int:
+        """Delivers the pending messages, highest priority first; returns how many."""
+        pending = sorted(self._pending, key=lambda r: -r[0])
+        self._pending.clear()
+        for prio, topic, message, sender, _ in pending:
+            for c in clients:
+                c.recv_message(topic, message, priority=prio, sender=sender)
+        return len(pending)
+
+    def __enter__(self):
+        lib.set_callback_target(C.addressof(MessageBus._TARGET))
+        check(lib.physim_gpu_set_bus_callback(self._cb), "physim_gpu_set_bus_callback")
+        return self
+
+    def __exit__(self, *exc):
+        lib.physim_gpu_set_bus_callback(_lib.BusFn())
+
+
 class GpuVerlet:
     """The verlet integrator (integrators/src/verlet.rs) over host arrays, on the GPU."""
 
@@ -197,13 +240,17 @@ class GpuIntegrator:
 class Pipeline:
     """pipeline.rs:137-173 restated: per step the integrator is handed
     `transform_fn` (every transform in order adding into the accelerations
-    it is given) and produces the new state."""
+    it is given) and produces the new state.  `run` first lets the elements
+    post their configuration messages and delivers them (to the transforms
+    and the sinks), then hands each sink the initial state and every new
+    state (pipeline.rs:128-181)."""
 
     def __init__(self, transforms: Iterable[TransformElementHandler],
-                 integrator: GpuVerlet | GpuIntegrator, dt: float):
+                 integrator: GpuVerlet | GpuIntegrator, dt: float, sinks: Iterable = ()):
         self.transforms = list(transforms)
         self.integrator = integrator
         self.dt = dt
+        self.sinks = list(sinks)
 
     def transform_fn(self, state: np.ndarray, acc: np.ndarray) -> None:
         for t in self.transforms:
@@ -216,7 +263,20 @@ class Pipeline:
         self.transform_fn(state, acc)
         return self.integrator.integrate(state, acc, self.dt)
 
+    def configure(self) -> MessageBus:
+        """post_configuration_messages of every transform, delivered."""
+        with MessageBus() as bus:
+            for t in self.transforms:
+                t.post_configuration_messages()
+        bus.deliver([*self.transforms, *self.sinks])
+        return bus
+
     def run(self, state: np.ndarray, iterations: int) -> np.ndarray:
+        self.configure()
+        for sink in self.sinks:
+            sink.render(state)
         for _ in range(iterations):
             state = self.step(state)
+            for sink in self.sinks:
+                sink.render(state)
         return state

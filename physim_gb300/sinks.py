@@ -1,4 +1,5 @@
-"""The `csvsink` render element (utilities/src/csvsink.rs) as a host-side writer.
+"""Render elements as host-side sinks: `csvsink` (utilities/src/csvsink.rs)
+and `energysink` (debug/src/energysink.rs).
 
 physim hands a renderer the initial state and the state after every step
 (physim-core/src/pipeline.rs:130-181); csvsink writes state k when
@@ -9,7 +10,9 @@ exponent notation: 1 -> "1", 1e-7 -> "0.0000001", -0.0 -> "-0").
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
+import sys
 from decimal import Decimal
 
 import numpy as np
@@ -55,6 +58,83 @@ class CsvSink:
     def close(self) -> None:
         if self._fh and not self._fh.closed:
             self._fh.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class EnergySink:
+    """physim's `energysink` (debug/src/energysink.rs) with its energy on the GPU.
+
+    Every state it receives is reduced to the kinetic energy K and, once a
+    gravity element has posted ("energysink", "gravity") (energysink.rs:
+    112-117), the potential energy V, both in f64 on the device
+    (physim_gpu_energy_compute); every `print_n`-th state prints the
+    reference's line `{i:>5} :: K = .. :: V = .. :: E = .. :: Delta E ..`
+    (energysink.rs:38-58; Delta E = E of the first state - E).  Two
+    differences from the reference, both its bugs: V sums every pair (the
+    reference assigns `=` where it means `+=`, energysink.rs:86, so it keeps
+    the last pair only), and the first line's E is K + V (the reference
+    prints V there).  With the default e = 0 the pair potential is the
+    reference sink's -m_a m_b / r; with `e` > 0 it is the potential whose
+    gradient is the softened force of the gravity elements.  `records` keeps
+    (iteration, K, V, E, Delta E) of every state."""
+
+    def __init__(self, print_n: int = 1, e: float = 0.0, device: int = 0, out=None):
+        from ._lib import check, lib
+        self.print_n = max(1, int(print_n))
+        self.e = abs(float(e))
+        self.calc_gpe = False
+        self.iteration = 0
+        self.initial_energy = None
+        self.records: list[tuple[int, float, float, float, float]] = []
+        self.out = out if out is not None else sys.stdout
+        h = C.c_void_p()
+        check(lib.physim_gpu_energy_create(device, C.byref(h)), "physim_gpu_energy_create")
+        self.handle = h
+
+    def recv_message(self, topic: str, message: str, priority: int = 2, sender: int = 0) -> None:
+        if topic == "energysink" and message == "gravity":
+            self.calc_gpe = True
+
+    def energy(self, state: np.ndarray) -> tuple[float, float]:
+        """(potential, kinetic) of one state."""
+        from ._lib import PhysimDiagnostics, check, lib
+        from .entity import as_entities
+        state = as_entities(state)
+        d = PhysimDiagnostics()
+        check(lib.physim_gpu_energy_compute(self.handle, state.ctypes.data, len(state), self.e,
+                                            1 if self.calc_gpe else 0, C.byref(d)),
+              "physim_gpu_energy_compute")
+        return (d.potential if self.calc_gpe else 0.0), d.kinetic
+
+    def render(self, state: np.ndarray) -> None:
+        potential, kinetic = self.energy(state)
+        energy = kinetic + potential
+        if self.initial_energy is None:
+            self.initial_energy = energy
+        delta = self.initial_energy - energy
+        k = self.iteration
+        self.iteration += 1
+        self.records.append((k, kinetic, potential, energy, delta))
+        if k == 0 or k % self.print_n == 0:
+            self.out.write(f"{k:>5} :: K = {kinetic:.6f} :: V = {potential:.6f} :: "
+                           f"E = {energy:.6f} :: Delta E {delta:.6f}\n")
+
+    def close(self) -> None:
+        from ._lib import lib
+        if self.handle:
+            lib.physim_gpu_energy_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
     def __enter__(self):
         return self
