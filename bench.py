@@ -96,6 +96,9 @@ def parse():
     p.add_argument("--ens-members", type=int, default=512)
     p.add_argument("--bh-steps", type=int, default=1000)
     p.add_argument("--bh-e2e-steps", type=int, default=5)
+    p.add_argument("--bh-default-steps", type=int, default=3,
+                   help="pipeline steps of the drop-in default astro2 (leaf 1, exact traversal) "
+                        "through the plugin on host arrays, per theta")
     p.add_argument("--bh-sample", type=int, default=16384,
                    help="bodies whose accelerations are checked against the f64 reference law")
     p.add_argument("--bodies", type=int, default=N_CUBE,
@@ -595,6 +598,18 @@ def measure_bh(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict:
                       "value_with_copies": rate["copy"],
                       "path": "astro2_transform (leaf_size 16, warp) + physim_gpu_verlet_integrate "
                               "on host Entity arrays"}
+        # what unchanged TOML runs: `astro2 theta=.. e=..` with no other
+        # properties (leaf 1, exact traversal: the reference's interaction
+        # lists, transformers.rs:162-180), e.g. energysink.toml:37-39
+        out["e2e_default"] = {}
+        for theta in (0.5, 1.0):
+            t, used = host_array_steps(pg, "astro2", {"theta": theta, "e": E, "device": device},
+                                       state, args.bh_default_steps, device, "auto")
+            out["e2e_default"][str(theta)] = {
+                "value": dist.sum(float(args.bh_default_steps)) / dist.max(t), "unit": "steps/s",
+                "steps": args.bh_default_steps, "transfer": used,
+                "path": f"astro2_transform {{theta: {theta}, e: {E}}} (leaf 1, exact traversal) "
+                        "+ physim_gpu_verlet_integrate on host Entity arrays"}
     if dist.rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_bh_step_time(state, 0.5, args.cpu_seconds)
     return out

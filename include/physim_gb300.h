@@ -517,11 +517,15 @@ void physim_gpu_ensemble_destroy(PhysimEnsemble *ens);
  * passes device-accessible arrays, state[n] (read) and acc[n] (acc[i] += a_i
  * for every non-fixed body, as simple_astro_transform does), and the work is
  * enqueued on `stream` (a cudaStream_t; NULL: the legacy default stream).
+ * Pageable host arrays are rejected with PHYSIM_ERR_ARGUMENT on a device
+ * without pageable memory access, and device arrays of another device.
  * Scratch lives in one static device array of about 7.9 MiB that every GPU
  * loading the library holds until exit; at most 65,536 bodies (larger n is
  * rejected with PHYSIM_ERR_ARGUMENT).  The first call on a device looks up
- * that array's device address, so make it before any stream capture.  All
- * calls share the array: calls that overlap on the GPU race. */
+ * that array's device address and keeps it for the life of the process, so
+ * make it before any stream capture, and do not call this entry point after
+ * a cudaDeviceReset of a device it was used on.  All calls share the array:
+ * calls that overlap on the GPU race. */
 int physim_gpu_simple_astro_accumulate_static(const Entity *state, size_t n, double e,
                                               Acceleration *acc, void *stream);
 

@@ -36,7 +36,10 @@ constexpr size_t kStaticBytes =
 __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
 
 // Device address of g_static_scratch per device ordinal, looked up once with
-// that device current (the host-side symbol is not a device address).
+// that device current (the host-side symbol is not a device address).  The
+// cache lives as long as the process: after a cudaDeviceReset the module is
+// loaded again and the array may sit elsewhere, so this entry point must not
+// be used after a reset of a device it was called on.
 std::mutex g_scratch_lock;
 unsigned char *g_scratch_addr[64] = {nullptr};
 
@@ -74,6 +77,30 @@ extern "C" int physim_gpu_simple_astro_accumulate_static(const Entity *state, si
     if (n == 0) return PHYSIM_OK;
     int device = 0;
     PG_CUDA(cudaGetDevice(&device));
+    // The arrays are read and written by kernels: host memory the GPU cannot
+    // reach would fault there, so it is rejected here (pageable host memory
+    // is reachable on a device with pageable memory access, as GB300's
+    // NVLink-C2C host is).
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess)
+        pageable = 0;
+    const void *arrays[2] = {state, acc};
+    for (const void *ptr : arrays) {
+        cudaPointerAttributes attr;
+        const cudaError_t err = cudaPointerGetAttributes(&attr, ptr);
+        if (err != cudaSuccess) {
+            (void)cudaGetLastError();
+            set_error("cudaPointerGetAttributes(%p) failed: %s", ptr, cudaGetErrorString(err));
+            return PHYSIM_ERR_ARGUMENT;
+        }
+        PG_CHECK(attr.type != cudaMemoryTypeUnregistered || pageable, PHYSIM_ERR_ARGUMENT,
+                 "%p is pageable host memory, which device %d cannot access: pass device, "
+                 "managed or registered host memory",
+                 ptr, device);
+        PG_CHECK(attr.type != cudaMemoryTypeDevice || attr.device == device, PHYSIM_ERR_ARGUMENT,
+                 "%p is memory of device %d, not of the current device %d", ptr, attr.device,
+                 device);
+    }
     unsigned char *base = nullptr;
     PG_TRY(scratch_address(device, &base));
     cudaStream_t st = (cudaStream_t)stream;
