@@ -885,11 +885,12 @@ struct TravArgs {
     int quad;
     float com_theta;
     // pair-law scale (PairScale in engine.h), set on the device from the root
-    // half-width X: bodies and cells enter pair_acc / quad_acc as p 2^-sk,
-    // second moments as S 2^-2sk, the easing as e 2^-2sk (es), and the sums
-    // leave multiplied by 2^-2sk; opening tests use unscaled positions
-    int sk;
-    float sc, es;
+    // half-width X and the total mass M (the largest cell): bodies and cells
+    // enter pair_acc / quad_acc at p 2^-sk with mass m 2^-skm, second moments
+    // as S 2^-(2sk + skm), the easing as e 2^-2sk (es), and the sums leave
+    // multiplied by 2^(skm - 2sk); opening tests use unscaled positions
+    int sk, skm;
+    float sc, msc, es;
 };
 
 __device__ __forceinline__ float load_extent(const TravArgs &a)
@@ -900,18 +901,22 @@ __device__ __forceinline__ float load_extent(const TravArgs &a)
 __device__ __forceinline__ void set_pair_scale(TravArgs &a)
 {
     a.sk = pair_scale_exp(a.extent, a.e);
+    a.skm = mass_scale_exp(a.n > 0 ? a.nd.com[0].w : 0.f);  // root: the total mass
     a.sc = pow2f(-a.sk);
+    a.msc = pow2f(-a.skm);
     a.es = a.e * pow2f(-2 * a.sk);
 }
 
-__device__ __forceinline__ float4 scaled(float4 p, float sc)
+// (x, y, z, m) scaled by sc and msc
+__device__ __forceinline__ float4 scaled(float4 p, float sc, float msc)
 {
-    return make_float4(p.x * sc, p.y * sc, p.z * sc, p.w);
+    return make_float4(p.x * sc, p.y * sc, p.z * sc, p.w * msc);
 }
 
-__device__ __forceinline__ float4 scaled2(float4 q, float sc2)
+// second moments scaled by f = sc^2 msc
+__device__ __forceinline__ float4 scaled2(float4 q, float f)
 {
-    return make_float4(q.x * sc2, q.y * sc2, q.z * sc2, q.w * sc2);
+    return make_float4(q.x * f, q.y * f, q.z * f, q.w * f);
 }
 
 // The reference's opening rule `extent / r < theta` (octree.rs:137-144):
@@ -1070,7 +1075,7 @@ traverse_exact_kernel(TravArgs a_in)
     TravArgs a = a_in;
     a.extent = load_extent(a_in);
     set_pair_scale(a);
-    const float sc2 = a.sc * a.sc;
+    const float sc2 = a.sc * a.sc * a.msc;
     unsigned long long visits = 0, pairs = 0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int k0 = (blockIdx.x * kTravWarps + warp) * 32;
@@ -1079,7 +1084,7 @@ traverse_exact_kernel(TravArgs a_in)
     const bool valid = k < a.n;
     const uint32_t active = __ballot_sync(0xffffffffu, valid);
     const float4 q = valid ? a.sbody[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 qs = scaled(q, a.sc);
+    const float4 qs = scaled(q, a.sc, a.msc);
     float ax = 0.f, ay = 0.f, az = 0.f, hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
     int sp = 0;
     if (lane == 0) stack[warp][0] = {0, active};
@@ -1102,7 +1107,7 @@ traverse_exact_kernel(TravArgs a_in)
         const uint32_t open = top.mask & ~__ballot_sync(0xffffffffu, acc);
         ++visits;
         if (acc) {
-            const float4 cm = scaled(a.nd.com[node], a.sc);
+            const float4 cm = scaled(a.nd.com[node], a.sc, a.msc);
             pair_acc(qs.x, qs.y, qs.z, cm, a.es, ax, ay, az);
             if (a.quad)
                 quad_acc(qs.x, qs.y, qs.z, cm, scaled2(a.nd.quad_a[node], sc2),
@@ -1115,7 +1120,7 @@ traverse_exact_kernel(TravArgs a_in)
                 const int b = a.nd.begin[node], c = a.nd.count[node];
                 const bool mine = (open >> lane) & 1u;
                 for (int j = b; j < b + c; ++j) {
-                    const float4 bj = scaled(a.sbody[j], a.sc);
+                    const float4 bj = scaled(a.sbody[j], a.sc, a.msc);
                     if (mine) pair_acc(qs.x, qs.y, qs.z, bj, a.es, ax, ay, az);
                 }
                 if (mine) pairs += c;
@@ -1150,7 +1155,7 @@ traverse_exact_kernel(TravArgs a_in)
     }
     if (valid) {
         const uint32_t i = a.order[k];
-        const double unsc = pow2d(-2 * a.sk);
+        const double unsc = pow2d(a.skm - 2 * a.sk);
         a.partial[i] = ((double)hx + (double)lx) * unsc;
         a.partial[a.n + i] = ((double)hy + (double)ly) * unsc;
         a.partial[2 * (size_t)a.n + i] = ((double)hz + (double)lz) * unsc;
@@ -1199,7 +1204,7 @@ traverse_warp_kernel(TravArgs a_in)
     TravArgs a = a_in;
     a.extent = load_extent(a_in);
     set_pair_scale(a);
-    const float sc = a.sc, sc2 = a.sc * a.sc;
+    const float sc = a.sc, msc = a.msc, sc2 = a.sc * a.sc * a.msc;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int k0 = (blockIdx.x * kTravWarps + warp) * 32;
     if (k0 >= a.n) return;
@@ -1253,7 +1258,7 @@ traverse_warp_kernel(TravArgs a_in)
             pl[0] = bj.x * sc;
             pl[2] = bj.y * sc;
             pl[4] = bj.z * sc;
-            pl[6] = bj.w;
+            pl[6] = bj.w * msc;
             __syncwarp();
             float2 sx = make_float2(0.f, 0.f), sy = sx, sz = sx;
             for (int jj = 0; jj < (m + 1) >> 1; ++jj) {
@@ -1281,7 +1286,7 @@ traverse_warp_kernel(TravArgs a_in)
                 float4 c4 = make_float4(0.f, 0.f, 0.f, 0.f), qa = c4, qb = c4;
                 if (lane < m) {
                     const int c = -queue[warp][kGQueue - 1 - (j0 + lane)] - 1;
-                    c4 = scaled(a.nd.com[c], sc);
+                    c4 = scaled(a.nd.com[c], sc, msc);
                     qa = scaled2(a.nd.quad_a[c], sc2);
                     qb = scaled2(a.nd.quad_b[c], sc2);
                 }
@@ -1432,7 +1437,7 @@ traverse_warp_kernel(TravArgs a_in)
     }
     if (valid) {
         const uint32_t i = a.order[k];
-        const double unsc = pow2d(-2 * a.sk);
+        const double unsc = pow2d(a.skm - 2 * a.sk);
         a.partial[i] = ((double)hx + (double)lx) * unsc;
         a.partial[a.n + i] = ((double)hy + (double)ly) * unsc;
         a.partial[2 * (size_t)a.n + i] = ((double)hz + (double)lz) * unsc;
@@ -1716,8 +1721,8 @@ int bh_accelerations(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, 
     a.stats = ws->stats;
     a.quad = p.multipole == kMultipoleQuadrupole ? 1 : 0;
     a.com_theta = (float)p.com_theta;
-    a.sk = 0;  // set on the device with the extent
-    a.sc = 1.f;
+    a.sk = a.skm = 0;  // set on the device (extent, total mass)
+    a.sc = a.msc = 1.f;
     a.es = a.e;
     PG_CUDA(cudaMemsetAsync(ws->stats, 0, 2 * sizeof(unsigned long long), st));
     const int blocks = cdiv(cdiv(n, 32), kTravWarps);

@@ -41,48 +41,72 @@ direct_forces_kernel(const float4 *__restrict__ body, int n, int n_jtiles, int c
     const int t0 = split * chunk_tiles;
     const int t1 = min(t0 + chunk_tiles, n_jtiles);
     direct_tile<BLOCK, IPT, COMP>(body, n, blockIdx.x * BLOCK * IPT, t0, t1, e, scale->k,
-                                  partial + (size_t)split * 3 * n, tile);
+                                  scale->km, partial + (size_t)split * 3 * n, tile);
 }
 
-// Largest |coordinate| of body4[0, n) (f32 bit patterns order like the
-// non-negative values; NaN and infinities skipped), reduced by the last
-// block to finish into ps->k (see PairScale).
+// Largest |coordinate| and |mass| of body4[0, n) (f32 bit patterns order
+// like the non-negative values; NaN and infinities skipped), reduced by the
+// last block to finish into ps->k and ps->km (see PairScale).
+__device__ __forceinline__ uint32_t finite_abs_bits(float v)
+{
+    const uint32_t b = __float_as_uint(v) & 0x7fffffffu;
+    return b < 0x7f800000u ? b : 0u;
+}
+
 __global__ void __launch_bounds__(256)
 pair_scale_kernel(const float4 *__restrict__ body, int n, float e, PairScale *ps)
 {
-    uint32_t m = 0;
+    uint32_t m = 0, w = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 b = body[i];
-        const uint32_t bx = __float_as_uint(b.x) & 0x7fffffffu;
-        const uint32_t by = __float_as_uint(b.y) & 0x7fffffffu;
-        const uint32_t bz = __float_as_uint(b.z) & 0x7fffffffu;
-        m = max(m, bx < 0x7f800000u ? bx : 0u);
-        m = max(m, by < 0x7f800000u ? by : 0u);
-        m = max(m, bz < 0x7f800000u ? bz : 0u);
+        m = max(m, max(finite_abs_bits(b.x), max(finite_abs_bits(b.y), finite_abs_bits(b.z))));
+        w = max(w, finite_abs_bits(b.w));
     }
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    __shared__ uint32_t wm[8];
+    for (int o = 16; o > 0; o >>= 1) {
+        m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        w = max(w, __shfl_xor_sync(0xffffffffu, w, o));
+    }
+    __shared__ uint32_t wm[8], ww[8];
     __shared__ bool last;
-    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    if ((threadIdx.x & 31) == 0) {
+        wm[threadIdx.x >> 5] = m;
+        ww[threadIdx.x >> 5] = w;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = max(m, wm[w]);
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+            m = max(m, wm[k]);
+            w = max(w, ww[k]);
+        }
         ps->blockmax[blockIdx.x] = m;
+        ps->blockmass[blockIdx.x] = w;
         __threadfence();
         last = atomicAdd(&ps->arrivals, 1u) == gridDim.x - 1;
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
-    uint32_t t = 0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+    uint32_t t = 0, tw = 0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
         t = max(t, __ldcg(&ps->blockmax[b]));
-    for (int o = 16; o > 0; o >>= 1) t = max(t, __shfl_xor_sync(0xffffffffu, t, o));
-    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = t;
+        tw = max(tw, __ldcg(&ps->blockmass[b]));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        t = max(t, __shfl_xor_sync(0xffffffffu, t, o));
+        tw = max(tw, __shfl_xor_sync(0xffffffffu, tw, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        wm[threadIdx.x >> 5] = t;
+        ww[threadIdx.x >> 5] = tw;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) t = max(t, wm[w]);
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+            t = max(t, wm[k]);
+            tw = max(tw, ww[k]);
+        }
         ps->k = pair_scale_exp(__uint_as_float(t), e);
+        ps->km = mass_scale_exp(__uint_as_float(tw));
         ps->arrivals = 0u;
     }
 }
@@ -283,6 +307,16 @@ int launch_pair_scale(const float4 *body4, int n, float e, PairScale *ps, cudaSt
     pair_scale_kernel<<<blocks, 256, 0, stream>>>(body4, n, e, ps);
     PG_CUDA(cudaGetLastError());
     return PHYSIM_OK;
+}
+
+float max_abs_mass(const Entity *state, size_t n)
+{
+    float m = 0.f;
+    for (size_t i = 0; i < n; ++i) {
+        const float a = fabsf((float)state[i].mass);
+        if (a <= 3.4028235e38f && a > m) m = a;  // NaN and infinities skipped
+    }
+    return m;
 }
 
 float max_abs_coordinate(const Entity *state, size_t n)

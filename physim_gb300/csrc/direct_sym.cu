@@ -54,15 +54,15 @@ direct_sym_kernel(const float4 *__restrict__ body, int n, float e,
     __shared__ float jacc[kSymWarps][kSymTile][3];
     int I, J;
     unit_tiles(blockIdx.x, I, J);
-    const int sk = scale->k;
+    const int sk = scale->k, skm = scale->km;
     if (I == J)
-        sym_tile_pair<true>(body, n, I, J, e, sk, P, jacc);
+        sym_tile_pair<true>(body, n, I, J, e, sk, skm, P, jacc);
     else
-        sym_tile_pair<false>(body, n, I, J, e, sk, P, jacc);
+        sym_tile_pair<false>(body, n, I, J, e, sk, skm, P, jacc);
 }
 
 // out[c*n + k] = sum over the T slots of P[t][c][k], TwoSum-compensated f32
-// in slot order, rounded once to f64 and unscaled (x 2^-2k).
+// in slot order, rounded once to f64 and unscaled (x 2^(km - 2k)).
 __global__ void sym_reduce_kernel(const float *__restrict__ P, long long n3, int T,
                                   const PairScale *__restrict__ scale, double *__restrict__ out)
 {
@@ -78,7 +78,7 @@ __global__ void sym_reduce_kernel(const float *__restrict__ P, long long n3, int
         hi = s;
         lo += err;
     }
-    out[idx] = ((double)hi + (double)lo) * pow2d(-2 * scale->k);
+    out[idx] = ((double)hi + (double)lo) * pow2d(scale->km - 2 * scale->k);
 }
 
 }  // namespace

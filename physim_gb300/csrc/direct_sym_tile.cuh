@@ -27,12 +27,13 @@ __device__ __forceinline__ void unit_tiles(long long u, int &I, int &J)
     I = (int)(u - j * (j + 1) / 2);
 }
 
-// The f32 slot sums are left scaled (a' of PairScale, positions entering as
-// p 2^-sk): the reduction multiplies by 2^-2sk in f64.
+// The f32 slot sums are left scaled (a' of PairScale: positions entering as
+// p 2^-sk, masses as m 2^-skm): the reduction multiplies by 2^(skm - 2sk) in
+// f64.
 template <bool DIAG>
 __device__ __forceinline__ void sym_tile_pair(const float4 *__restrict__ body, int n, int I,
-                                              int J, float e, int sk, float *__restrict__ P,
-                                              float (*jacc)[kSymTile][3])
+                                              int J, float e, int sk, int skm,
+                                              float *__restrict__ P, float (*jacc)[kSymTile][3])
 {
     constexpr int Q = kSymIpt / 2;
     const int lane = threadIdx.x & 31;
@@ -42,6 +43,7 @@ __device__ __forceinline__ void sym_tile_pair(const float4 *__restrict__ body, i
     // bodies I*1024 + p*128 + warp*32 + lane, p = 2q (x half) and 2q+1 (y half)
     const int ib = I * kSymTile + warp * 32 + lane;
     const float sc = pow2f(-sk);  // 2^-sk, exact
+    const float msc = pow2f(-skm);
     float2 nx[Q], ny[Q], nz[Q], nm[Q], ax[Q], ay[Q], az[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -50,7 +52,7 @@ __device__ __forceinline__ void sym_tile_pair(const float4 *__restrict__ body, i
         nx[q] = make_float2(-b0.x * sc, -b1.x * sc);
         ny[q] = make_float2(-b0.y * sc, -b1.y * sc);
         nz[q] = make_float2(-b0.z * sc, -b1.z * sc);
-        nm[q] = make_float2(-b0.w, -b1.w);
+        nm[q] = make_float2(-b0.w * msc, -b1.w * msc);
         ax[q] = ay[q] = az[q] = make_float2(0.f, 0.f);
     }
     const float es = e * pow2f(-2 * sk);
@@ -64,7 +66,7 @@ __device__ __forceinline__ void sym_tile_pair(const float4 *__restrict__ body, i
         const float4 bj = next;
         // the next group's body is loaded while this group is evaluated
         if (g + 1 < kSymGroups) next = body[J * kSymTile + (g + 1) * 32 + lane];
-        float xj = bj.x * sc, yj = bj.y * sc, zj = bj.z * sc, mj = bj.w;
+        float xj = bj.x * sc, yj = bj.y * sc, zj = bj.z * sc, mj = bj.w * msc;
         float2 jx = make_float2(0.f, 0.f), jy = jx, jz = jx;
 #pragma unroll 2
         for (int k = 0; k < 32; ++k) {

@@ -11,8 +11,9 @@
 // FMUL2.  j bodies are staged in shared memory as (x,x,y,y)(z,z,m,m) so one
 // 128-bit broadcast load yields the float2 operands.  Per-body sums are
 // compensated: each j tile is summed in plain FP32 and folded into a
-// (hi, lo) pair with TwoSum once per tile.  Positions enter scaled by 2^-sk
-// and the sums leave scaled by 2^-2sk (PairScale in engine.h).
+// (hi, lo) pair with TwoSum once per tile.  Positions enter scaled by 2^-sk,
+// masses by 2^-skm, and the sums leave multiplied by 2^(skm - 2sk)
+// (PairScale in engine.h).
 #pragma once
 
 #include "common.cuh"
@@ -22,18 +23,19 @@ namespace pg {
 
 // One i tile of BLOCK*IPT bodies starting at i_base against the j tiles
 // [t0, t1) of `body` (n bodies, padded), writing this split's partial sums to
-// out[c*n + i].  `tile` is the block's shared staging buffer; sk the pair
-// scale exponent.
+// out[c*n + i].  `tile` is the block's shared staging buffer; sk and skm the
+// pair scale exponents.
 template <int BLOCK, int IPT, bool COMP>
 __device__ __forceinline__ void direct_tile(const float4 *__restrict__ body, int n, int i_base,
-                                            int t0, int t1, float e, int sk,
+                                            int t0, int t1, float e, int sk, int skm,
                                             double *__restrict__ out, float4 (*tile)[BLOCK][2])
 {
     static_assert(IPT % 2 == 0, "bodies per thread must be even (packed pairs)");
     constexpr int P = IPT / 2;
     const int tid = threadIdx.x;
-    const float sc = pow2f(-sk);     // 2^-sk, exact
-    const double unsc = pow2d(-2 * sk);  // back to unscaled accelerations
+    const float sc = pow2f(-sk);      // 2^-sk, exact
+    const float msc = pow2f(-skm);    // 2^-skm
+    const double unsc = pow2d(skm - 2 * sk);  // back to unscaled accelerations
 
     float2 nx[P], ny[P], nz[P];
     float2 ax[P], ay[P], az[P];
@@ -60,7 +62,8 @@ __device__ __forceinline__ void direct_tile(const float4 *__restrict__ body, int
             const int buf = (t - t0) & 1;
             const float sx = nxt.x * sc, sy = nxt.y * sc, sz = nxt.z * sc;
             tile[buf][tid][0] = make_float4(sx, sx, sy, sy);
-            tile[buf][tid][1] = make_float4(sz, sz, nxt.w, nxt.w);
+            const float sm = nxt.w * msc;
+            tile[buf][tid][1] = make_float4(sz, sz, sm, sm);
             __syncthreads();
             if (t + 1 < t1) nxt = body[(t + 1) * BLOCK + tid];
 #pragma unroll 4

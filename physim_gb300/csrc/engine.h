@@ -28,20 +28,27 @@ constexpr float kPairGuard = 1.17549435e-38f;
 // ------------------------------------------------------------------------
 // The pair kernels evaluate r^2 (r^2 + e)^2 in FP32, which spans six times
 // the exponent range of the coordinates: unscaled it overflows for
-// separations above ~2.6e6 and underflows (e = 0) below ~5e-7.  So positions
+// separations above ~2.6e6 and underflows (e = 0) below ~5e-7.  A pair at
+// one position (a body with itself, coincident bodies) contributes
+// 0 * m / sqrt(guard), which needs m / sqrt(guard) finite.  So positions
 // enter the pair arithmetic as p' = p 2^-k, with k chosen per force pass so
-// the largest |coordinate| m of the state maps into [0.5, 1), the easing as
-// e' = e 2^-2k, and the accelerations leave as a = a' 2^-2k -- every factor
-// a power of two, so no bits are lost and a state that was in range before
-// gives the same results.  k is clamped so that e' <= 2^60 (r'^2 (r'^2 +
-// e')^2 then stays finite) and |k| <= 100.  What remains: with e = 0, pairs
-// closer than ~3e-6 m lose accuracy beyond 1e-5 relative, and closer than
-// ~5e-7 m they contribute almost nothing (r'^6 underflows into the guard).
+// the largest |coordinate| of the state maps into [0.5, 1), masses as
+// m' = m 2^-km, the largest mass into [0.5, 1) (for Barnes-Hut: the total
+// mass, the largest cell), the easing as e' = e 2^-2k, and the accelerations
+// leave as a = a' 2^(km - 2k) -- every factor a power of two, so no bits are
+// lost and a state that was in range before gives the same results.  k is
+// clamped so that e' <= 2^60 (r'^2 (r'^2 + e')^2 then stays finite), k and km
+// to [-100, 100].  What remains: with e = 0, pairs closer than ~3e-6 of the
+// largest |coordinate| lose accuracy beyond 1e-5 relative, and closer than
+// ~5e-7 of it they contribute almost nothing (r'^6 underflows into the guard).
 constexpr int kScaleBlocks = 256;
 struct PairScale {
-    int32_t k;          // scale exponent of the current state
+    int32_t k;          // coordinate scale exponent of the current state
+    int32_t km;         // mass scale exponent
     uint32_t arrivals;  // blocks of a running scale pass that finished (reset by the last)
-    uint32_t blockmax[kScaleBlocks];  // per-block max |coordinate| (f32 bit patterns)
+    uint32_t pad;
+    uint32_t blockmax[kScaleBlocks];   // per-block max |coordinate| (f32 bit patterns)
+    uint32_t blockmass[kScaleBlocks];  // per-block max |mass|
 };
 
 // Exponent of the largest |coordinate| m: m = f 2^k, f in [0.5, 1) (0 for m = 0).
@@ -71,14 +78,22 @@ __host__ __device__ inline int pair_scale_exp(float m, float e)
     return pair_scale_from(coord_exp(m), e);
 }
 
-// Computes ps->k for the n bodies of body4 (max over |x|, |y|, |z|; NaN and
-// infinite coordinates skipped) and easing e, on `stream`: one launch whose
-// last block to finish reduces the per-block maxima.  ps->arrivals must be 0
-// before the first pass (it is left 0).
+// Mass scale exponent for the largest |mass| m, within [-100, 100].
+__host__ __device__ inline int mass_scale_exp(float m)
+{
+    const int k = coord_exp(m);
+    return k < -100 ? -100 : (k > 100 ? 100 : k);
+}
+
+// Computes ps->k and ps->km for the n bodies of body4 (max over |x|, |y|,
+// |z| and over |m|; NaN and infinite values skipped) and easing e, on
+// `stream`: one launch whose last block to finish reduces the per-block
+// maxima.  ps->arrivals must be 0 before the first pass (it is left 0).
 int launch_pair_scale(const float4 *body4, int n, float e, PairScale *ps, cudaStream_t stream);
-// The same pass over the bodies of several members of an ensemble is done by
-// its integrator kernel; a host-side value for a state being uploaded:
+// The coordinate pass over the members of an ensemble is done by its
+// integrator kernel; host-side values for a state being uploaded:
 float max_abs_coordinate(const Entity *state, size_t n);
+float max_abs_mass(const Entity *state, size_t n);
 
 // ------------------------------------------------------------------------
 // Direct sum (simple_astro)

@@ -61,7 +61,8 @@ __global__ void __launch_bounds__(BLOCK, 2)
 ensemble_forces_kernel(const float4 *__restrict__ body4, const MemberInfo *__restrict__ members,
                        const WorkUnit *__restrict__ units, int n_units,
                        const unsigned long long *__restrict__ remaining, int *__restrict__ counter,
-                       const int32_t *__restrict__ member_kx, double *__restrict__ partial)
+                       const int32_t *__restrict__ member_kx, const int32_t *__restrict__ member_km,
+                       double *__restrict__ partial)
 {
     __shared__ float4 tile[2][BLOCK][2];
     __shared__ int next;
@@ -77,6 +78,7 @@ ensemble_forces_kernel(const float4 *__restrict__ body4, const MemberInfo *__res
             const int t1 = min(t0 + m.chunk_tiles, m.n_jtiles);
             direct_tile<BLOCK, IPT, COMP>(body4 + m.off, m.n, w.itile * BLOCK * IPT, t0, t1, m.e,
                                           pair_scale_from(member_kx[w.member], m.e),
+                                          member_km[w.member],
                                           partial + m.poff + (size_t)w.split * 3 * m.n, tile);
         }
         __syncthreads();
@@ -87,7 +89,8 @@ __global__ void __launch_bounds__(kSymThreads, 3)
 ensemble_sym_kernel(const float4 *__restrict__ body4, const MemberInfo *__restrict__ members,
                     const SymUnit *__restrict__ units, int n_units,
                     const unsigned long long *__restrict__ remaining, int *__restrict__ counter,
-                    const int32_t *__restrict__ member_kx, float *__restrict__ slots)
+                    const int32_t *__restrict__ member_kx, const int32_t *__restrict__ member_km,
+                    float *__restrict__ slots)
 {
     __shared__ float jacc[kSymWarps][kSymTile][3];
     __shared__ int next;
@@ -99,11 +102,13 @@ ensemble_sym_kernel(const float4 *__restrict__ body4, const MemberInfo *__restri
         const SymUnit w = units[u];
         if (remaining[w.member] != 0) {
             const MemberInfo m = members[w.member];
-            const int sk = pair_scale_from(member_kx[w.member], m.e);
+            const int sk = pair_scale_from(member_kx[w.member], m.e), skm = member_km[w.member];
             if (w.I == w.J)
-                sym_tile_pair<true>(body4 + m.off, m.n, w.I, w.J, m.e, sk, slots + m.soff, jacc);
+                sym_tile_pair<true>(body4 + m.off, m.n, w.I, w.J, m.e, sk, skm, slots + m.soff,
+                                    jacc);
             else
-                sym_tile_pair<false>(body4 + m.off, m.n, w.I, w.J, m.e, sk, slots + m.soff, jacc);
+                sym_tile_pair<false>(body4 + m.off, m.n, w.I, w.J, m.e, sk, skm, slots + m.soff,
+                                     jacc);
         }
         __syncthreads();
     }
@@ -126,6 +131,7 @@ __global__ void ensemble_verlet_kernel(float4 *body4, const double *__restrict__
                                        double *y, double *z, double *vx, double *vy, double *vz,
                                        double *px, double *py, double *pz,
                                        const int32_t *__restrict__ member_kx,
+                                       const int32_t *__restrict__ member_km,
                                        uint32_t *__restrict__ member_ext)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -149,7 +155,8 @@ __global__ void ensemble_verlet_kernel(float4 *body4, const double *__restrict__
                         h[c] = sum;
                         l[c] += err;
                     }
-                const double unsc = pow2d(-2 * pair_scale_from(member_kx[k], m.e));
+                const double unsc =
+                    pow2d(member_km[k] - 2 * pair_scale_from(member_kx[k], m.e));
                 ax = ((double)h[0] + (double)l[0]) * unsc;
                 ay = ((double)h[1] + (double)l[1]) * unsc;
                 az = ((double)h[2] + (double)l[2]) * unsc;
@@ -332,6 +339,7 @@ struct PhysimEnsemble {
     unsigned long long *remaining = nullptr, *done = nullptr;
     int *counter = nullptr;  // [0] one-pair units, [1] symmetric units
     int32_t *member_kx = nullptr;    // coordinate exponent of each member's pair scale
+    int32_t *member_km = nullptr;    // mass scale exponent of each member
     uint32_t *member_ext = nullptr;  // largest |coordinate| of the new positions (f32 bits)
     double *partial = nullptr;
     SymUnit *d_sym_units = nullptr;
@@ -476,7 +484,7 @@ int launch_forces(PhysimEnsemble *E)
     if (E->n_sym_units > 0) {
         ensemble_sym_kernel<<<std::min(E->sym_grid, E->n_sym_units), kSymThreads, 0, E->stream>>>(
             E->body4, E->d_members, E->d_sym_units, E->n_sym_units, E->remaining, E->counter + 1,
-            E->member_kx, E->slot_sums);
+            E->member_kx, E->member_km, E->slot_sums);
         PG_CUDA(cudaGetLastError());
     }
     if (E->n_units == 0) return PHYSIM_OK;
@@ -484,7 +492,7 @@ int launch_forces(PhysimEnsemble *E)
     PG_CHECK(fn, PHYSIM_ERR_ARGUMENT, "no ensemble kernel for %d x %d", E->block, E->ipt);
     void *args[] = {(void *)&E->body4, (void *)&E->d_members, (void *)&E->d_units,
                     (void *)&E->n_units, (void *)&E->remaining, (void *)&E->counter,
-                    (void *)&E->member_kx, (void *)&E->partial};
+                    (void *)&E->member_kx, (void *)&E->member_km, (void *)&E->partial};
     PG_CUDA(cudaLaunchKernel(fn, dim3(E->grid), dim3(E->block), args, 0, E->stream));
     return PHYSIM_OK;
 }
@@ -496,7 +504,7 @@ int enqueue_step(PhysimEnsemble *E)
     ensemble_verlet_kernel<<<cdiv(E->slots, t), t, 0, E->stream>>>(
         E->body4, E->m, E->fixed, E->slot_member, E->d_members, E->remaining, E->done, E->partial,
         E->slot_sums, E->slots, E->x, E->y, E->z, E->vx, E->vy, E->vz, E->px, E->py, E->pz,
-        E->member_kx, E->member_ext);
+        E->member_kx, E->member_km, E->member_ext);
     ensemble_count_kernel<<<cdiv((long long)E->members.size(), 256), 256, 0, E->stream>>>(
         E->remaining, E->done, (int)E->members.size(), E->counter, E->member_kx, E->member_ext);
     PG_CUDA(cudaGetLastError());
@@ -509,7 +517,7 @@ void free_ensemble(PhysimEnsemble *E)
     void *p[] = {E->body4, E->fixed, E->x,  E->y,  E->z,  E->vx, E->vy, E->vz, E->px, E->py,
                  E->pz,    E->m,     E->radius, E->id, E->slot_member, E->d_members, E->d_units,
                  E->remaining, E->done, E->counter, E->partial, E->staging,
-                 E->d_sym_units, E->slot_sums, E->member_kx, E->member_ext};
+                 E->d_sym_units, E->slot_sums, E->member_kx, E->member_km, E->member_ext};
     for (void *q : p) dev_free(q, E->stream);
     if (E->stream) cudaStreamSynchronize(E->stream);
 }
@@ -588,6 +596,7 @@ int physim_gpu_ensemble_create(const PhysimSimConfig *cfg, const size_t *sizes, 
     EA(E->done, count);
     EA(E->counter, 2);
     EA(E->member_kx, count);
+    EA(E->member_km, count);
     EA(E->member_ext, count);
     EA(E->partial, partial_elems);
 #undef EA
@@ -602,6 +611,7 @@ int physim_gpu_ensemble_create(const PhysimSimConfig *cfg, const size_t *sizes, 
             cudaMemsetAsync(E->m, 0, slots * sizeof(double), E->stream) != cudaSuccess ||
             cudaMemsetAsync(E->counter, 0, 2 * sizeof(int), E->stream) != cudaSuccess ||
             cudaMemsetAsync(E->member_kx, 0, count * sizeof(int32_t), E->stream) != cudaSuccess ||
+            cudaMemsetAsync(E->member_km, 0, count * sizeof(int32_t), E->stream) != cudaSuccess ||
             cudaMemsetAsync(E->member_ext, 0, count * sizeof(uint32_t), E->stream) != cudaSuccess ||
             cudaMemcpyAsync(E->slot_member, map.data(), map.size() * sizeof(int32_t),
                             cudaMemcpyHostToDevice, E->stream) != cudaSuccess ||
@@ -648,8 +658,11 @@ int physim_gpu_ensemble_upload(PhysimEnsemble *E, size_t index, const Entity *st
     const unsigned long long zero = 0ull, all = ~0ull;
     // pair scale of the uploaded positions (the integrator keeps it current)
     const int32_t kx = coord_exp(max_abs_coordinate(state, n));
+    const int32_t km = mass_scale_exp(max_abs_mass(state, n));  // masses do not change
     const uint32_t zero32 = 0u;
     PG_CUDA(cudaMemcpyAsync(E->member_kx + index, &kx, sizeof kx, cudaMemcpyHostToDevice,
+                            E->stream));
+    PG_CUDA(cudaMemcpyAsync(E->member_km + index, &km, sizeof km, cudaMemcpyHostToDevice,
                             E->stream));
     PG_CUDA(cudaMemcpyAsync(E->member_ext + index, &zero32, sizeof zero32,
                             cudaMemcpyHostToDevice, E->stream));
