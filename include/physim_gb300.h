@@ -380,6 +380,19 @@ int physim_gpu_sim_set_plan(PhysimSim *sim, const PhysimDirectTuning *plan);
  * back to a one-pair plan.  Process-wide, read when a plan is made.  This
  * builds on simple_astro (transformers.rs:219-244), which has no plans. */
 int physim_gpu_set_symmetric_cap(uint64_t bytes);
+/* Barnes-Hut builds wait on other thread blocks only in the radix sort's
+ * decoupled look-back; every such wait gives up after `polls` polls that saw
+ * no progress (0 restores the default, 2^20), raising an error flag: later
+ * kernels of the build and the traversal then return at once and the next
+ * synchronising call (physim_gpu_sim_synchronize / _download, the transform)
+ * reports PHYSIM_ERR_TIMEOUT.  Process-wide, read when a build is enqueued or
+ * captured.  No reference counterpart (the reference builds its tree on one
+ * CPU thread, octree.rs:27-128). */
+int physim_gpu_set_wait_limit(uint32_t polls);
+/* Test hook for the path above: tile `tile` (>= 0; -1 turns it off) of each
+ * radix pass sees no predecessor word, so its wait always runs out.
+ * Process-wide, read when a build is enqueued or captured. */
+int physim_gpu_test_stall_sort(int32_t tile);
 /* The current pair-kernel plan of a simple_astro simulation (block, ipt,
  * splits, symmetric, tiles; the other fields 0); all zero for astro/astro2. */
 int physim_gpu_sim_plan(PhysimSim *sim, PhysimDirectTuning *out);
@@ -408,7 +421,9 @@ typedef struct PhysimTreeSnapshot {
     int32_t *node_child;   /* [cap] index of the first child, -1 for a leaf */
     uint8_t *node_nchild;  /* [cap] number of children */
     uint8_t *node_level;   /* [cap] depth below the root */
-    double *node_centre;   /* [4*m] planes cx, cy, cz, half-width; m = min(n_nodes, cap) */
+    double *node_centre;   /* [4*m] planes cx, cy, cz, half-width; m = min(n_nodes, cap);
+                              f64 centres are kept with the exact traversal only (the warp
+                              traversal keeps f32 geometry: the planes are then not written) */
     float *node_com;       /* [4*cap] centre of mass x, y, z and mass, per node */
     float *node_quad;      /* [8*m] second moments about the centre of mass (quadrupole
                             * builds): m x (Sxx, Syy, Szz, trace), then m x (Sxy, Sxz, Syz, 0) */

@@ -32,6 +32,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "common.cuh"
 #include "engine.h"
@@ -51,7 +52,6 @@ constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr int kSortWarps = kSortThreads / 32;
 
-constexpr int kBuildThreads = 256;
 constexpr int kMaxLevels = 31;
 
 constexpr int kTravWarps = 4;
@@ -67,17 +67,17 @@ constexpr int kFlagSort = 2;
 // Radix sort of the 63-bit (62-bit) keys: 8 passes of 8-bit digits.
 constexpr int kSortPasses = 8;
 // Look-back spin limit per digit (each spin is one L2 load, ~0.5 us worst
-// case), far above any wait of a running predecessor tile.
+// case), far above any wait of a running predecessor tile; the default of
+// physim_gpu_set_wait_limit.
 constexpr int kLookbackSpins = 1 << 20;
 // Predecessor tiles a look-back reads per round trip.
 constexpr int kLookbackWindow = 8;
 
 struct LevelInfo {
-    int32_t begin[kMaxLevels + 2];
-    int32_t count[kMaxLevels + 2];
-    int32_t total;                      // nodes in the tree
-    uint32_t tile_ctr[kMaxLevels + 1];  // node tiles claimed per level (reset per build)
-    uint32_t epoch;                     // builds so far (tags the look-back words)
+    int32_t begin[kMaxLevels + 2];  // first node of each level
+    int32_t count[kMaxLevels + 2];  // nodes of each level
+    int32_t total;                  // nodes in the tree
+    int32_t max_level;              // deepest level built (below D only if capacity ran out)
 };
 
 __host__ __device__ inline int tree_levels(int nchild) { return nchild == 8 ? 21 : 31; }
@@ -276,16 +276,23 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *w
 // prefix, and epoch counts (sort, pass) pairs; words of earlier passes and
 // sorts carry older epochs and read as not ready, so the status array needs
 // no clearing.  A wait that exceeds
-// kLookbackSpins sets flags[kFlagSort] and gives up (the order is then
-// invalid and the host reports an error).
+// the wait limit (kLookbackSpins unless physim_gpu_set_wait_limit set one)
+// sets flags[kFlagSort] and gives up: the tile still scatters, at positions no
+// higher than the right ones (its prefix is a partial sum), so every write
+// stays in bounds; every later kernel of the build and the traversal see the
+// flag and return at once, so nothing reads the invalid order or an unbuilt
+// tree, and the host reports PHYSIM_ERR_TIMEOUT.  stall_tile >= 0
+// (physim_gpu_test_stall_sort) makes that tile's look-back see no
+// predecessor word, so the limit is reached for sure.
 __global__ void __launch_bounds__(kSortThreads)
 radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
                   uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int n,
                   int pass, const uint32_t *__restrict__ ghist, uint32_t *__restrict__ tile_ctr,
                   unsigned long long *__restrict__ status, const uint32_t *__restrict__ epoch_ptr,
-                  uint32_t *__restrict__ flags)
+                  uint32_t *__restrict__ flags, int spin_limit, int stall_tile)
 {
     static_assert(kSortThreads >= kRadixBuckets, "one thread per digit");
+    if (*(volatile const uint32_t *)&flags[kFlagSort] != 0u) return;  // an earlier wait failed
     __shared__ uint32_t h[kSortWarps][kRadixBuckets];
     __shared__ uint32_t digit_off[kRadixBuckets];
     __shared__ uint32_t ws[33];
@@ -352,11 +359,12 @@ radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restri
             // are loaded together, then summed up to the first inclusive prefix
             int t = tile - 1;
             int spins = 0;
+            const bool stall = tile == stall_tile;
             for (;;) {
                 unsigned long long w[kLookbackWindow];
 #pragma unroll
                 for (int j = 0; j < kLookbackWindow; ++j)
-                    w[j] = t - j >= 0 ? st[(size_t)(t - j) * kRadixBuckets + d] : 0ull;
+                    w[j] = t - j >= 0 && !stall ? st[(size_t)(t - j) * kRadixBuckets + d] : 0ull;
                 int used = 0;
                 bool done = false;
 #pragma unroll
@@ -373,7 +381,7 @@ radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restri
                 }
                 if (done) break;
                 t -= used;
-                if (used == 0 && ++spins > kLookbackSpins) {
+                if (used == 0 && ++spins > spin_limit) {
                     atomicOr(&flags[kFlagSort], 1u);
                     break;
                 }
@@ -395,26 +403,7 @@ radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restri
 }
 
 // ---------------------------------------------------------------------------
-// gather of sorted bodies
-// ---------------------------------------------------------------------------
-__global__ void gather_kernel(const uint32_t *__restrict__ order, int n,
-                              const float4 *__restrict__ body4, const double *__restrict__ x,
-                              const double *__restrict__ y, const double *__restrict__ z,
-                              const double *__restrict__ m, float4 *__restrict__ sbody,
-                              double *__restrict__ spos, double *__restrict__ smass)
-{
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const uint32_t i = order[k];
-    sbody[k] = body4[i];
-    spos[k] = x[i];
-    spos[n + k] = y[i];
-    spos[2 * (size_t)n + k] = z[i];
-    smass[k] = m[i];
-}
-
-// ---------------------------------------------------------------------------
-// 4. tree build
+// node arrays
 // ---------------------------------------------------------------------------
 struct NodeArrays {
     int32_t *begin, *count, *child;
@@ -432,282 +421,387 @@ struct NodeArrays {
     int cap;
 };
 
-__global__ void root_kernel(NodeArrays nd, LevelInfo *lv, int n,
-                            const unsigned long long *__restrict__ extent_bits)
+// ---------------------------------------------------------------------------
+// 4. tree build (flat: a few launches for all levels)
+// ---------------------------------------------------------------------------
+// The tree is the reference's non-path-compressed one over the sorted keys: a
+// node at level l is a maximal run of bodies sharing the first l digits of
+// their keys, and it exists iff l = 0 or the run one level up (its parent)
+// splits, i.e. holds more than leaf_size bodies whose keys are not all equal,
+// at a level below D.  Node numbering is breadth first: levels one after the
+// other, each in key order, so a node's children are contiguous and in
+// octant order, as a level-by-level serial build lays them out.
+//
+// With L(i) the number of leading digits keys[i-1] and keys[i] share, a run
+// at level l starts at body i iff i = 0 or L(i) < l, and everything about
+// the runs starting at i follows from L near i:
+//   * the run at level l starting at i has more than `leaf` bodies iff
+//     L(i+1..i+leaf) are all >= l (those bodies exist);
+//   * it is not uniform iff the first body after i with a different key,
+//     u(i), has L(u(i)) >= l;
+//   * so it splits iff l <= c(i) = min(m(i), L(u(i)), D - 1), m(i) the
+//     minimum of L over the next leaf boundaries;
+//   * a run at level l > L(i) + 1 starting at i exists iff its parent (the
+//     run at l - 1 starting at i) splits, i.e. l <= c(i) + 1;
+//   * the run at level L(i) + 1 exists iff the run at level L(i) containing
+//     i - 1 and i (not uniform: those keys differ) has more than leaf
+//     bodies, which a scan of L over leaf boundaries either side decides.
+// Each body's existing runs form a bit mask over levels; a node's index is
+// the start of its level plus the count of set bits of that level before its
+// body (block counts, one scan over blocks, warp ballots within a block).
+// The deepest run a body starts is a leaf; its end (the next boundary below
+// its level) is read off the same shared tile of L.
+
+constexpr int kTreeBlock = 1024;   // bodies per block of the mask and node kernels
+constexpr int kTreeHalo = 72;      // boundaries read either side (> the largest leaf + 1)
+constexpr int kMaxLeaf = 64;
+constexpr uint8_t kLongLeaf = 255;  // leaf count marker: longer than the shared tile reaches
+
+__device__ __forceinline__ bool sort_failed(const uint32_t *flags)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const double X = __longlong_as_double((long long)*extent_bits);
-    for (int d = 0; d < kMaxLevels + 2; ++d) {
-        lv->begin[d] = 0;
-        lv->count[d] = 0;
-    }
-    for (int d = 0; d < kMaxLevels + 1; ++d) lv->tile_ctr[d] = 0;
-    lv->epoch += 1u;
-    lv->total = n > 0 ? 1 : 0;
-    lv->count[0] = n > 0 ? 1 : 0;
-    lv->begin[1] = 1;
-    nd.begin[0] = 0;
-    nd.count[0] = n;
-    nd.parent[0] = -1;
-    nd.child[0] = -1;
-    nd.nchild[0] = 0;
-    nd.level[0] = 0;
-    nd.c64[0] = 0.0;
-    nd.c64[nd.cap] = 0.0;
-    nd.c64[2 * (size_t)nd.cap] = 0.0;
-    nd.c64[3 * (size_t)nd.cap] = X;
-    nd.geo[0] = make_float4(0.f, 0.f, 0.f, (float)X);
-    nd.meta[0] = make_int4(0, -1, 0, n);
+    return *(volatile const uint32_t *)&flags[kFlagSort] != 0u;
 }
 
-// The top levels hold few, large nodes whose child ranges would take long
-// binary searches.  For levels < K, child ranges come from a table of cell
-// starts at level K instead: top[p] = first sorted index whose level-K
-// prefix is >= p (so empty cells point at the next cell), top[cells] = n.
-// K grows with the body count (more top levels are then large): the table
-// has nchild^K cells, K = ceil(log_nchild n) within [5, 7] for the octree
-// (at most 2M cells) and [7, 10] for the quadtree (at most 1M cells).
-inline int top_levels(int nchild, long long n)
+// L(k) for k >= 1 (the number of leading digits keys[k-1] and keys[k] share,
+// D for equal keys), and the sorted f32 bodies.
+__global__ void boundary_kernel(const uint64_t *__restrict__ keys,
+                                const uint32_t *__restrict__ order, int n, int nchild,
+                                const float4 *__restrict__ body4, float4 *__restrict__ sbody,
+                                uint8_t *__restrict__ lcp, const uint32_t *__restrict__ flags)
 {
-    int k = 0;
-    for (long long c = 1; c < n; c *= nchild) ++k;
-    return nchild == 8 ? std::min(std::max(k, 5), 7) : std::min(std::max(k, 7), 10);
-}
-
-__global__ void top_mark_kernel(const uint64_t *__restrict__ keys, int n, int shift,
-                                int32_t *__restrict__ top)
-{
+    if (sort_failed(flags)) return;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const uint64_t p = keys[k] >> shift;
-    if (k == 0 || (keys[k - 1] >> shift) != p) top[p] = k;
+    const int D = tree_levels(nchild), B = level_bits(nchild);
+    sbody[k] = body4[order[k]];
+    int L = 0;
+    if (k > 0) {
+        const uint64_t x = keys[k - 1] ^ keys[k];
+        // keys use the low B * D bits: 64 - B * D leading bits are always 0
+        L = x == 0 ? D : (__clzll((long long)x) - (64 - B * D)) / B;
+    }
+    lcp[k] = (uint8_t)L;
 }
 
-// Suffix minimum over the marks (-1 = empty cell) fills empty cells with the
-// start of the next non-empty one.  Two passes over blocks of 1024 cells
-// (cells is a power of two >= 1024): per-block minima, then per-block
-// suffix minima plus the minimum of all later blocks.
-__device__ __forceinline__ int32_t mark_value(int32_t v, int n) { return v >= 0 ? v : n; }
-
-__global__ void __launch_bounds__(1024) top_blockmin_kernel(const int32_t *__restrict__ top, int n,
-                                                            int32_t *__restrict__ blockmin)
+// First index j in [lo, n) with keys[j] != keys[i] (keys sorted), or n.
+__device__ __forceinline__ int next_key_change(const uint64_t *__restrict__ keys, int i, int lo,
+                                               int n)
 {
-    __shared__ int32_t wm[32];
-    int32_t m = mark_value(top[blockIdx.x * 1024 + threadIdx.x], n);
-    for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    const uint64_t ki = keys[i];
+    int hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (keys[mid] == ki)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// Level masks of the bodies (bit l: a node at level l starts at this body),
+// per-block counts of every level (blk_cnt[l * nblk + block]) and the body
+// count of the leaf starting at each body (the deepest run it starts; 0: no
+// node starts here, kLongLeaf: longer than the shared tile reaches); also
+// zeroes the child counters.
+__global__ void __launch_bounds__(kTreeBlock)
+mask_kernel(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ lcp, int n,
+            int nchild, int leaf, uint32_t *__restrict__ mask, uint32_t *__restrict__ blk_cnt,
+            int nblk, uint8_t *__restrict__ leafcnt, uint32_t *__restrict__ nchild32, int cap,
+            const uint32_t *__restrict__ flags)
+{
+    if (sort_failed(flags)) return;
+    __shared__ int8_t sL[kTreeBlock + 2 * kTreeHalo];
+    __shared__ uint32_t cnt[32];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cap; k += gridDim.x * blockDim.x)
+        nchild32[k] = 0u;
+    const int D = tree_levels(nchild);
+    const int base = blockIdx.x * kTreeBlock;
+    // boundaries base - halo .. base + block + halo; -1 marks "no boundary
+    // beyond here" (index 0 starts every run, indices >= n end them)
+    for (int t = threadIdx.x; t < kTreeBlock + 2 * kTreeHalo; t += blockDim.x) {
+        const int j = base - kTreeHalo + t;
+        sL[t] = (j >= 1 && j < n) ? (int8_t)lcp[j] : (int8_t)-1;
+    }
+    if (threadIdx.x < 32) cnt[threadIdx.x] = 0u;
+    __syncthreads();
+    const int i = base + threadIdx.x;
+    uint32_t m = 0u;
+    if (i < n) {
+        const int s = threadIdx.x + kTreeHalo;  // i's slot in sL
+        const int Li = i == 0 ? -1 : sL[s];
+        // m(i): min of L over the next leaf boundaries, -1 if fewer remain
+        int mi = -1;
+        if (i + leaf <= n - 1) {
+            mi = D;
+            for (int q = 1; q <= leaf; ++q) mi = min(mi, (int)sL[s + q]);
+        }
+        // u(i): the next body with another key; L(u(i)), -1 if none
+        int Lu = -1;
+        {
+            int j = i + 1, t = s + 1;
+            while (j < n && t < kTreeBlock + 2 * kTreeHalo && sL[t] == D) {
+                ++j;
+                ++t;
+            }
+            if (j < n && t >= kTreeBlock + 2 * kTreeHalo) j = next_key_change(keys, i, j, n);
+            if (j < n) Lu = lcp[j];
+        }
+        const int c = min(min(mi, Lu), D - 1);
+        if (i == 0) {
+            m = 1u;  // the root
+            for (int l = 1; l <= c + 1; ++l) m |= 1u << l;
+        } else if (Li < D) {
+            // the run at level Li containing i - 1 and i: more than leaf bodies?
+            int lft = 0, rgt = 0;
+            for (int q = 1; q <= leaf && sL[s - q] >= Li; ++q) ++lft;
+            for (int q = 1; q <= leaf && sL[s + q] >= Li; ++q) ++rgt;
+            if (lft + rgt + 2 > leaf) {
+                m |= 1u << (Li + 1);
+                for (int l = Li + 2; l <= c + 1; ++l) m |= 1u << l;
+            }
+        }
+        mask[i] = m;
+        // the leaf starting here (the deepest run; unless the capacity stops
+        // the tree above it) runs to the next boundary below its level
+        uint8_t lc = 0;
+        if (m != 0u) {
+            const int lf = 31 - __clz(m);
+            int t = s + 1, e = i + 1;
+            while (e < n && t < kTreeBlock + 2 * kTreeHalo && sL[t] >= lf) {
+                ++e;
+                ++t;
+            }
+            lc = (e < n && t >= kTreeBlock + 2 * kTreeHalo) || e - i >= (int)kLongLeaf
+                     ? kLongLeaf
+                     : (uint8_t)(e - i);
+        }
+        leafcnt[i] = lc;
+    }
+    for (int l = 0; l <= D; ++l) {
+        const uint32_t b = __ballot_sync(0xffffffffu, (m >> l) & 1u);
+        if ((threadIdx.x & 31) == 0 && b) atomicAdd(&cnt[l], (uint32_t)__popc(b));
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) blk_cnt[(size_t)threadIdx.x * nblk + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// One block: per level, the exclusive scan of the block counts (blk_off,
+// same layout as blk_cnt) and the level's first node.  Warp l scans row l,
+// 32 blocks per step.  If the nodes do not fit the node arrays, the tree
+// stops at the deepest level that fits (its nodes become leaves: results
+// stay exact, slower) and flags[kFlagNodes] is raised.
+__global__ void __launch_bounds__(1024)
+level_scan_kernel(const uint32_t *__restrict__ blk_cnt, int nblk, int nchild,
+                  uint32_t *__restrict__ blk_off, LevelInfo *lv, int cap,
+                  uint32_t *__restrict__ flags)
+{
+    if (sort_failed(flags)) return;
+    __shared__ uint32_t total_of[32];
+    const int D = tree_levels(nchild);
+    const int l = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t *row = blk_cnt + (size_t)l * nblk;
+    uint32_t *orow = blk_off + (size_t)l * nblk;
+    uint32_t carry = 0;
+    constexpr int kAhead = 4;  // row chunks loaded before they are scanned
+    for (int c0 = 0; c0 < nblk; c0 += 32 * kAhead) {
+        uint32_t v[kAhead];
+#pragma unroll
+        for (int u = 0; u < kAhead; ++u) {
+            const int b = c0 + u * 32 + lane;
+            v[u] = b < nblk ? row[b] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kAhead; ++u) {
+            uint32_t incl = v[u];
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int b = c0 + u * 32 + lane;
+            if (b < nblk) orow[b] = carry + incl - v[u];
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+    }
+    if (lane == 0) total_of[l] = carry;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long at = 0;
+        int max_level = D;
+        for (int q = 0; q <= D; ++q) {
+            const long long c = total_of[q];
+            if (at + c > cap) {
+                max_level = q - 1;
+                atomicOr(&flags[kFlagNodes], 1u);
+                break;
+            }
+            at += c;
+        }
+        at = 0;
+        for (int q = 0; q < kMaxLevels + 2; ++q) {
+            const int c = q <= max_level ? (int)total_of[q] : 0;
+            lv->begin[q] = (int32_t)at;
+            lv->count[q] = c;
+            at += c;
+        }
+        lv->total = (int32_t)at;
+        lv->max_level = max_level;
+    }
+}
+
+// Node records: per body, one node per set bit of its mask.  Leaves get
+// their body count here; an internal node's count, its child count and its
+// traversal metadata are completed by the moment pass (children counted into
+// nchild32 here); the centres by centre_kernel.
+__global__ void __launch_bounds__(kTreeBlock)
+node_kernel(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ leafcnt,
+            const uint32_t *__restrict__ mask, const uint32_t *__restrict__ blk_off, int nblk,
+            int n, int nchild, NodeArrays nd, const LevelInfo *__restrict__ lv,
+            uint32_t *__restrict__ nchild32, const uint32_t *__restrict__ flags)
+{
+    if (sort_failed(flags)) return;
+    __shared__ uint32_t sbal[kTreeBlock / 32][32];  // per warp and level: lanes with that bit
+    __shared__ uint32_t woff[kTreeBlock / 32][32];  // ... and the level's nodes before the warp
+    __shared__ int32_t lbeg[kMaxLevels + 2];
+    const int D = tree_levels(nchild), B = level_bits(nchild);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * kTreeBlock + threadIdx.x;
+    const uint32_t m = i < n ? mask[i] : 0u;
+    for (int l = 0; l < 32; ++l) {
+        const uint32_t b = __ballot_sync(0xffffffffu, (m >> l) & 1u);
+        if (lane == 0) {
+            sbal[warp][l] = b;
+            woff[warp][l] = (uint32_t)__popc(b);
+        }
+    }
+    if (threadIdx.x < kMaxLevels + 2) lbeg[threadIdx.x] = lv->begin[threadIdx.x];
     __syncthreads();
     if (threadIdx.x < 32) {
-        m = wm[threadIdx.x];
-        for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (threadIdx.x == 0) blockmin[blockIdx.x] = m;
+        uint32_t run = blk_off[(size_t)threadIdx.x * nblk + blockIdx.x];
+        for (int w = 0; w < kTreeBlock / 32; ++w) {
+            const uint32_t v = woff[w][threadIdx.x];
+            woff[w][threadIdx.x] = run;
+            run += v;
+        }
     }
-}
-
-__global__ void __launch_bounds__(1024) top_fill_kernel(int32_t *__restrict__ top, int cells, int n,
-                                                        const int32_t *__restrict__ blockmin)
-{
-    __shared__ int32_t wm[32];
-    __shared__ int32_t later;
-    const int nb = cells / 1024;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (warp == 0) {
-        int32_t m = n;
-        for (int b = (int)blockIdx.x + 1 + lane; b < nb; b += 32) m = min(m, blockmin[b]);
-        for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (lane == 0) later = m;
-    }
-    const int p = blockIdx.x * 1024 + threadIdx.x;
-    int32_t v = mark_value(top[p], n);
-    // inclusive suffix min within the warp
-    for (int o = 1; o < 32; o <<= 1) {
-        const int32_t t = __shfl_down_sync(0xffffffffu, v, o);
-        if (lane + o < 32) v = min(v, t);
-    }
-    if (lane == 0) wm[warp] = v;  // minimum of the whole warp
     __syncthreads();
-    int32_t r = later;
-    for (int w = warp + 1; w < 32; ++w) r = min(r, wm[w]);
-    top[p] = min(v, r);
-    if (blockIdx.x == 0 && threadIdx.x == 0) top[cells] = n;
-}
-
-// Child ranges of a node at `level` covering [b, e): bounds[c] = first sorted
-// index in [b, e) whose digit at `shift` is >= c; bounds[nchild] = e.
-__device__ __forceinline__ void child_bounds(const uint64_t *__restrict__ keys, int b, int e,
-                                             int shift, int nchild, int *bounds,
-                                             const int32_t *__restrict__ top, int level, int D,
-                                             int bits, int K)
-{
-    if (level < K) {
-        const uint64_t prefix = keys[b] >> (bits * (D - level));
-        for (int c = 0; c < nchild; ++c)
-            bounds[c] = top[((prefix << bits) | (uint64_t)c) << (bits * (K - level - 1))];
-        bounds[0] = b;
-        bounds[nchild] = e;
-        return;
-    }
-    const uint32_t mask = nchild - 1;
-    bounds[0] = b;
-    for (int c = 1; c < nchild; ++c) {
-        int lo = bounds[c - 1], hi = e;
-        while (lo < hi) {
-            int mid = (lo + hi) >> 1;
-            if (((uint32_t)(keys[mid] >> shift) & mask) < (uint32_t)c)
-                lo = mid + 1;
-            else
-                hi = mid;
+    if (m == 0u) return;
+    const int max_level = lv->max_level;
+    const uint32_t lt = (1u << lane) - 1u, le = lt | (1u << lane);
+    const int top = min(31 - __clz(m), max_level);
+    for (int l = __ffs(m) - 1; l <= top; ++l) {
+        if (!((m >> l) & 1u)) continue;
+        const int x = lbeg[l] + (int)woff[warp][l] + __popc(sbal[warp][l] & lt);
+        int parent = -1;
+        if (l > 0) {
+            // the last node of level l - 1 starting at or before body i
+            parent = lbeg[l - 1] + (int)woff[warp][l - 1] + __popc(sbal[warp][l - 1] & le) - 1;
+            atomicAdd(&nchild32[parent], 1u);
         }
-        bounds[c] = lo;
-    }
-    bounds[nchild] = e;
-}
-
-__device__ __forceinline__ bool node_splits(const uint64_t *__restrict__ keys, int b, int cnt,
-                                            int leaf, int level, int D)
-{
-    return level < D && cnt > leaf && keys[b] != keys[b + cnt - 1];
-}
-
-
-// One level of the build in one launch: the level's nodes are cut into tiles
-// of kBuildThreads, claimed in launch order from an atomic counter; each
-// block counts its tile's children, publishes the tile's total, walks back
-// over the preceding tiles' words to its exclusive prefix (decoupled
-// look-back, as in the radix passes; the tile holding an earlier word is
-// held by a block that is already running), then writes its nodes' children
-// at that offset.  Children therefore follow their parents' order, so the
-// next level is laid out exactly as a serial build would lay it out.  A tile
-// whose children would overflow the node arrays leaves its nodes unsplit
-// (results stay exact, flags[kFlagNodes]); the tiles before it keep theirs.
-// Status words are (tag << 32 | tile total), tag = (epoch * 32 + level) * 4 +
-// flag, flag 1 = tile total, 2 = inclusive prefix; words of other levels and
-// builds read as not ready.
-__global__ void __launch_bounds__(kBuildThreads)
-level_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, LevelInfo *lv, int level, int leaf,
-             int nchild, const int32_t *__restrict__ top, int K,
-             unsigned long long *__restrict__ status, uint32_t *__restrict__ flags)
-{
-    const int D = tree_levels(nchild), bits = level_bits(nchild);
-    const int cnt = lv->count[level];
-    if (cnt == 0) return;  // the tree is complete
-    const int first = lv->begin[level];
-    const int child_base = first + cnt;
-    const int ntiles = (cnt + kBuildThreads - 1) / kBuildThreads;
-    const unsigned long long tag =
-        ((unsigned long long)(lv->epoch & 0x03ffffffu) * 32ull + (unsigned)level) * 4ull;
-    volatile unsigned long long *st = status;
-    __shared__ uint32_t ws[33];
-    __shared__ int s_tile;
-    __shared__ int32_t s_excl;
-    if (blockIdx.x == 0 && threadIdx.x == 0) lv->begin[level + 1] = child_base;
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = (int)atomicAdd(&lv->tile_ctr[level], 1u);
-        __syncthreads();
-        const int tile = s_tile;
-        if (tile >= ntiles) break;
-        const int k = tile * kBuildThreads + threadIdx.x;
-        const int node = first + k;
-        int bounds[9];
-        uint32_t nc = 0;
-        bool split = false;
-        if (k < cnt) {
-            const int b = nd.begin[node], c = nd.count[node];
-            split = node_splits(keys, b, c, leaf, level, D);
-            if (split) {
-                child_bounds(keys, b, b + c, bits * (D - level - 1), nchild, bounds, top, level, D,
-                             bits, K);
-                for (int q = 0; q < nchild; ++q) nc += bounds[q + 1] > bounds[q];
-            }
-        }
-        uint32_t T;
-        const uint32_t local = block_exclusive_scan(nc, ws, T);
-        if (threadIdx.x < 32) {
-            // warp-wide look-back: lane l reads the word of tile t - l, so
-            // 32 predecessors cost one round trip
-            const int lane = threadIdx.x;
-            uint32_t excl = 0;
-            if (tile == 0) {
-                if (lane == 0) st[0] = ((tag + 2ull) << 32) | T;
-            } else {
-                if (lane == 0) st[tile] = ((tag + 1ull) << 32) | T;
-                int t = tile - 1, spins = 0;
-                for (;;) {
-                    const unsigned long long w = t - lane >= 0 ? st[t - lane] : 0ull;
-                    const unsigned long long wt = w >> 32;
-                    const uint32_t incl = __ballot_sync(0xffffffffu, wt == tag + 2ull);
-                    const uint32_t ready = __ballot_sync(0xffffffffu, wt == tag + 1ull) | incl;
-                    // lanes up to and including the first inclusive word, if all ready
-                    const int stop = incl ? __ffs(incl) - 1 : 31;
-                    const uint32_t need = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
-                    if ((ready & need) == need) {
-                        uint32_t v = lane <= stop ? (uint32_t)w : 0u;
-                        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                        excl += v;
-                        if (incl) break;
-                        t -= 32;  // t - 31 > 0 here: tile 0's word is inclusive
-                        continue;
-                    }
-                    if (++spins > kLookbackSpins) {
-                        if (lane == 0) atomicOr(&flags[kFlagSort], 1u);
-                        break;
-                    }
+        const bool splits = l + 1 <= max_level && ((m >> (l + 1)) & 1u);
+        const int first_child =
+            splits ? lbeg[l + 1] + (int)woff[warp][l + 1] + __popc(sbal[warp][l + 1] & lt) : -1;
+        nd.begin[x] = i;
+        nd.level[x] = (uint8_t)l;
+        nd.parent[x] = parent;
+        nd.child[x] = first_child;
+        if (!splits) {
+            // a leaf: its bodies run to the next boundary below level l
+            int cnt = leafcnt[i];
+            if (cnt == kLongLeaf || l != 31 - __clz(m)) {
+                // a long run (equal keys, or a node the capacity kept from
+                // splitting): the end of its level-l key prefix
+                const int sh = B * (D - l);
+                const uint64_t p = keys[i] >> sh;
+                int lo = i + 1, hi = n;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if ((keys[mid] >> sh) == p)
+                        lo = mid + 1;
+                    else
+                        hi = mid;
                 }
-                if (lane == 0) st[tile] = ((tag + 2ull) << 32) | (excl + T);
+                cnt = lo - i;
             }
-            if (lane == 0) s_excl = (int32_t)excl;
+            nd.count[x] = cnt;
+            nd.nchild[x] = 0;
+            nd.meta[x] = make_int4(x, -1, i, cnt);
         }
-        __syncthreads();
-        const int32_t P = s_excl;
-        const bool fits = (long long)child_base + P + T <= (long long)nd.cap;
-        if (k < cnt) {
-            if (split && fits) {
-                const int fc = child_base + P + (int)local;
-                nd.child[node] = fc;
-                nd.nchild[node] = (uint8_t)nc;
-                nd.meta[node] = make_int4(node | ((int)nc << 28), fc, nd.begin[node],
-                                          nd.count[node]);
-                const size_t cap = nd.cap;
-                const double pcx = nd.c64[node], pcy = nd.c64[cap + node];
-                const double pcz = nd.c64[2 * cap + node], pext = nd.c64[3 * cap + node];
-                const double h = __dmul_rn(pext, 0.5);  // pext / 2, exact
-                int w = 0;
-                for (int q = 0; q < nchild; ++q) {
-                    if (bounds[q + 1] <= bounds[q]) continue;
-                    const int ci = fc + w++;
-                    nd.parent[ci] = node;
-                    nd.begin[ci] = bounds[q];
-                    nd.count[ci] = bounds[q + 1] - bounds[q];
-                    nd.child[ci] = -1;
-                    nd.nchild[ci] = 0;
-                    nd.level[ci] = (uint8_t)(level + 1);
-                    const double cx = (q & 1) ? __dadd_rn(pcx, h) : __dsub_rn(pcx, h);
-                    const double cy = (q & 2) ? __dadd_rn(pcy, h) : __dsub_rn(pcy, h);
-                    const double cz =
-                        nchild == 8 ? ((q & 4) ? __dadd_rn(pcz, h) : __dsub_rn(pcz, h)) : pcz;
-                    nd.c64[ci] = cx;
-                    nd.c64[cap + ci] = cy;
-                    nd.c64[2 * cap + ci] = cz;
-                    nd.c64[3 * cap + ci] = h;
-                    // f32 geometry and leaf metadata; the metadata is rewritten
-                    // if the child splits at the next level
-                    nd.geo[ci] = make_float4((float)cx, (float)cy, (float)cz, (float)h);
-                    nd.meta[ci] = make_int4(ci, -1, bounds[q], bounds[q + 1] - bounds[q]);
-                }
-            } else {
-                nd.child[node] = -1;
-                nd.nchild[node] = 0;
+    }
+}
+
+// Geometric centres and half-widths of the nodes.  For the exact traversal
+// (exact != 0) the f64 centres follow the reference's arithmetic from the
+// root down (child = parent +- half-width / 2 per level, octree.rs:167-215,
+// quadtree.rs:167-194; the traversal re-decides near-threshold openings with
+// them): thread x follows the digits of its node's first key.  The warp
+// traversal needs only the f32 geometry: X (2q + 1 - 2^l) / 2^l from the
+// cell index q, one f64 product per axis rounded to f32 (within an f32 ulp
+// of the f64 chain's value; the traversal's margins allow 3).  Node-parallel,
+// so consecutive threads hold nodes of one level (equal chain lengths).
+__device__ __forceinline__ uint32_t compact3(uint64_t x)
+{
+    x &= 0x1249249249249249ull;
+    x = (x ^ (x >> 2)) & 0x10c30c30c30c30c3ull;
+    x = (x ^ (x >> 4)) & 0x100f00f00f00f00full;
+    x = (x ^ (x >> 8)) & 0x1f0000ff0000ffull;
+    x = (x ^ (x >> 16)) & 0x1f00000000ffffull;
+    x = (x ^ (x >> 32)) & 0x1fffffull;
+    return (uint32_t)x;
+}
+
+__device__ __forceinline__ uint32_t compact2(uint64_t x)
+{
+    x &= 0x5555555555555555ull;
+    x = (x | (x >> 1)) & 0x3333333333333333ull;
+    x = (x | (x >> 2)) & 0x0f0f0f0f0f0f0f0full;
+    x = (x | (x >> 4)) & 0x00ff00ff00ff00ffull;
+    x = (x | (x >> 8)) & 0x0000ffff0000ffffull;
+    x = (x | (x >> 16)) & 0x00000000ffffffffull;
+    return (uint32_t)x;
+}
+
+__global__ void centre_kernel(const uint64_t *__restrict__ keys, NodeArrays nd,
+                              const LevelInfo *__restrict__ lv, int nchild, int exact,
+                              const unsigned long long *__restrict__ extent_bits,
+                              const uint32_t *__restrict__ flags)
+{
+    if (sort_failed(flags)) return;
+    const int total = lv->total;
+    const int D = tree_levels(nchild), B = level_bits(nchild);
+    const uint32_t dmask = (uint32_t)nchild - 1u;
+    const double X = __longlong_as_double((long long)*extent_bits);
+    const size_t cap = nd.cap;
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < total; x += gridDim.x * blockDim.x) {
+        const int l = nd.level[x];
+        const uint64_t key = keys[nd.begin[x]];
+        if (exact) {
+            double cx = 0.0, cy = 0.0, cz = 0.0, ext = X;
+            for (int j = 1; j <= l; ++j) {
+                const uint32_t q = (uint32_t)(key >> (B * (D - j))) & dmask;
+                const double h = __dmul_rn(ext, 0.5);  // ext / 2, exact
+                cx = (q & 1) ? __dadd_rn(cx, h) : __dsub_rn(cx, h);
+                cy = (q & 2) ? __dadd_rn(cy, h) : __dsub_rn(cy, h);
+                if (nchild == 8) cz = (q & 4) ? __dadd_rn(cz, h) : __dsub_rn(cz, h);
+                ext = h;
             }
+            nd.c64[x] = cx;
+            nd.c64[cap + x] = cy;
+            nd.c64[2 * cap + x] = cz;
+            nd.c64[3 * cap + x] = ext;
+            nd.geo[x] = make_float4((float)cx, (float)cy, (float)cz, (float)ext);
+        } else {
+            const uint64_t pre = l == 0 ? 0ull : key >> (B * (D - l));
+            const double h = X * pow2d(-l);  // the half-width, exact
+            const long long span = 1ll << l;
+            const uint32_t qx = nchild == 8 ? compact3(pre) : compact2(pre);
+            const uint32_t qy = nchild == 8 ? compact3(pre >> 1) : compact2(pre >> 1);
+            const float gx = (float)(h * (double)(2ll * qx + 1 - span));
+            const float gy = (float)(h * (double)(2ll * qy + 1 - span));
+            const float gz =
+                nchild == 8 ? (float)(h * (double)(2ll * compact3(pre >> 2) + 1 - span)) : 0.f;
+            nd.geo[x] = make_float4(gx, gy, gz, (float)h);
         }
-        if (threadIdx.x == 0 && T > 0) {
-            if (fits) {
-                atomicMax(&lv->count[level + 1], P + (int32_t)T);
-                atomicMax(&lv->total, child_base + P + (int32_t)T);
-            } else {
-                atomicOr(&flags[kFlagNodes], 1u);
-            }
-        }
-        __syncthreads();
     }
 }
 
@@ -715,23 +809,19 @@ level_kernel(const uint64_t *__restrict__ keys, NodeArrays nd, LevelInfo *lv, in
 // 5. moments: mass, centre of mass and (optionally) second moments of every
 //    cell, bottom up in one launch
 // ---------------------------------------------------------------------------
-// Each leaf sums its own bodies: mass and mass-weighted positions in f64,
-// kept as double-float (hi + lo f32) pairs.  A parent is finished by the
-// thread of its last child to arrive (atomic count of arrivals after a fence;
-// nothing waits), which adds the children's pairs in child order -- so
-// results do not depend on the arrival order -- and continues upwards.  This
-// upward walk is divergent (one thread per finished node), so it uses f32
-// arithmetic only: GB300 issues f64 instructions at a small fraction of its
-// f32 rate, and a divergent f64 instruction costs as much as a full one.
-// The f32 centre of mass c = S / M is the double-float quotient rounded
-// once, within one rounding of the exact value (the reference computes it in
-// f64; its precision matters where a cell's centre of mass lies very close
-// to a body that interacts with it, e.g. a quadtree cell holding a heavy body
-// that a body far above it in z accepts).  A leaf whose bodies all sit at one
-// position keeps that exact position, so a body there cancels against it as
-// the reference's equal-centre skip does; a massless cell sits at its
-// geometric centre.  Second moments (kQuad) are f32, combined with the
-// parallel-axis rule S = sum_c [S_c + M_c (c_c - c)(c_c - c)^T].
+// Each leaf sums its own bodies: mass and mass-weighted positions as
+// double-float (hi + lo f32) pairs, each product m x taken exactly (TwoProduct
+// by FMA) -- FP32 arithmetic only, as GB300 issues f64 instructions at a small
+// fraction of its f32 rate.  A parent is finished by the thread of its last
+// child to arrive (atomic count of arrivals after a fence; nothing waits),
+// which adds the children's pairs in child order -- so results do not depend
+// on the arrival order -- and continues upwards; it also completes the
+// parent's body count, child count and traversal metadata.  The f32 centre
+// of mass c = S / M is the double-float quotient rounded once.  A leaf whose
+// bodies all sit at one position keeps that exact position, so a body there
+// cancels against it as the reference's equal-centre skip does; a massless
+// cell sits at its geometric centre.  Second moments (quad) are f32,
+// combined with the parallel-axis rule S = sum_c [S_c + M_c (c_c - c)(c_c - c)^T].
 __device__ __forceinline__ void store_quad(const NodeArrays &nd, int i, const float s[6])
 {
     nd.quad_a[i] = make_float4(s[0], s[1], s[2], s[0] + s[1] + s[2]);
@@ -746,13 +836,6 @@ __device__ __forceinline__ void df_add(float &ah, float &al, float bh, float bl)
     e += al + bl;
     ah = s + e;
     al = e - (ah - s);
-}
-
-// The f64 value v as a double-float pair.
-__device__ __forceinline__ void df_from(double v, float &h, float &l)
-{
-    h = __double2float_rn(v);
-    l = __double2float_rn(__dsub_rn(v, (double)h));
 }
 
 // f32 rounding of (sh + sl) / (mh + ml): an f32 quotient corrected once with
@@ -773,31 +856,35 @@ __device__ __forceinline__ float4 df_com(const float4 h, const float4 l, float4 
                        df_div(h.w, l.w, h.x, l.x), h.x + l.x);
 }
 
-__global__ void moments_kernel(NodeArrays nd, const LevelInfo *__restrict__ lv,
-                               const float4 *__restrict__ sbody, const double *__restrict__ spos,
-                               const double *__restrict__ smass, int n, int quad)
+// m * p added exactly-rounded into the double-float (hi, lo)
+__device__ __forceinline__ void df_add_prod(float &hi, float &lo, float m, float p)
 {
+    const float pr = m * p;
+    const float pe = fmaf(m, p, -pr);
+    df_add(hi, lo, pr, pe);
+}
+
+__global__ void moments_kernel(NodeArrays nd, const LevelInfo *__restrict__ lv,
+                               const float4 *__restrict__ sbody, int quad,
+                               const uint32_t *__restrict__ nchild32,
+                               const uint32_t *__restrict__ flags)
+{
+    if (sort_failed(flags)) return;
     const int total = lv->total;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
         if (nd.child[i] >= 0) continue;
         const int b = nd.begin[i], e = b + nd.count[i];
         const float4 p0 = sbody[b];
-        double m0 = 0.0, m1 = 0.0, m2 = 0.0, m3 = 0.0;
+        float4 h = make_float4(0.f, 0.f, 0.f, 0.f), l = h;
         bool same = true;
         for (int j = b; j < e; ++j) {
-            const double m = smass[j];
-            m0 += m;
-            m1 = fma(m, spos[j], m1);
-            m2 = fma(m, spos[n + j], m2);
-            m3 = fma(m, spos[2 * (size_t)n + j], m3);
             const float4 p = sbody[j];
+            df_add(h.x, l.x, p.w, 0.f);
+            df_add_prod(h.y, l.y, p.w, p.x);
+            df_add_prod(h.z, l.z, p.w, p.y);
+            df_add_prod(h.w, l.w, p.w, p.z);
             same = same && p.x == p0.x && p.y == p0.y && p.z == p0.z;
         }
-        float4 h, l;
-        df_from(m0, h.x, l.x);
-        df_from(m1, h.y, l.y);
-        df_from(m2, h.z, l.z);
-        df_from(m3, h.w, l.w);
         nd.msum_hi[i] = h;
         nd.msum_lo[i] = l;
         const float4 com = same ? make_float4(p0.x, p0.y, p0.z, h.x + l.x)
@@ -822,22 +909,28 @@ __global__ void moments_kernel(NodeArrays nd, const LevelInfo *__restrict__ lv,
         for (;;) {
             const int par = nd.parent[node];
             if (par < 0) break;
+            const int nc = (int)nchild32[par];
             __threadfence();
             const uint32_t arrived = atomicAdd(&nd.arrivals[par], 1u);
-            if (arrived + 1u != (uint32_t)nd.nchild[par]) break;
+            if (arrived + 1u != (uint32_t)nc) break;
             __threadfence();
             nd.arrivals[par] = 0u;  // ready for the next build
-            const int fc = nd.child[par], nc = nd.nchild[par];
+            const int fc = nd.child[par];
             float4 ph = __ldcg(&nd.msum_hi[fc]), pl = __ldcg(&nd.msum_lo[fc]);
+            int count = __ldcg(&nd.count[fc]);
             for (int k = fc + 1; k < fc + nc; ++k) {
                 const float4 ch = __ldcg(&nd.msum_hi[k]), cl = __ldcg(&nd.msum_lo[k]);
                 df_add(ph.x, pl.x, ch.x, cl.x);
                 df_add(ph.y, pl.y, ch.y, cl.y);
                 df_add(ph.z, pl.z, ch.z, cl.z);
                 df_add(ph.w, pl.w, ch.w, cl.w);
+                count += __ldcg(&nd.count[k]);
             }
             nd.msum_hi[par] = ph;
             nd.msum_lo[par] = pl;
+            nd.count[par] = count;
+            nd.nchild[par] = (uint8_t)nc;
+            nd.meta[par] = make_int4(par | (nc << 28), fc, nd.begin[par], count);
             const float4 cp = df_com(ph, pl, nd.geo[par]);
             nd.com[par] = cp;
             if (quad) {
@@ -867,7 +960,7 @@ __global__ void moments_kernel(NodeArrays nd, const LevelInfo *__restrict__ lv,
 struct TravArgs {
     NodeArrays nd;
     const float4 *sbody;
-    const double *spos;
+    const double *bx, *by, *bz;  // the f64 state, unsorted (body order[k] is sorted body k)
     const uint32_t *order;
     const LevelInfo *lv;
     int n;
@@ -937,9 +1030,10 @@ __device__ __forceinline__ bool accept_cell(const TravArgs &a, int node, float4 
     if (fabsf(ratio - a.theta) > band && ratio == ratio && r2 > 1e-30f)
         return ratio < a.theta;
     const size_t cap = a.nd.cap;
-    const double d0 = a.spos[k] - a.nd.c64[node];
-    const double d1 = a.spos[a.n + k] - a.nd.c64[cap + node];
-    const double d2 = a.spos[2 * (size_t)a.n + k] - a.nd.c64[2 * cap + node];
+    const uint32_t i = a.order[k];
+    const double d0 = a.bx[i] - a.nd.c64[node];
+    const double d1 = a.by[i] - a.nd.c64[cap + node];
+    const double d2 = a.bz[i] - a.nd.c64[2 * cap + node];
     const double r64 = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
     return a.nd.c64[3 * cap + node] / r64 < a.theta64;
 }
@@ -1072,6 +1166,8 @@ __global__ void __launch_bounds__(kTravWarps * 32)
 traverse_exact_kernel(TravArgs a_in)
 {
     __shared__ StackEntry stack[kTravWarps][kStack];
+    // a failed sort left no tree to walk (the node arrays may hold anything)
+    if (sort_failed(a_in.flags)) return;
     TravArgs a = a_in;
     a.extent = load_extent(a_in);
     set_pair_scale(a);
@@ -1201,6 +1297,8 @@ traverse_warp_kernel(TravArgs a_in)
     __shared__ float4 tile[kTravWarps][32];
     __shared__ float4 tqa[kQuad ? kTravWarps : 1][32];
     __shared__ float4 tqb[kQuad ? kTravWarps : 1][32];
+    // a failed sort left no tree to walk (the node arrays may hold anything)
+    if (sort_failed(a_in.flags)) return;
     TravArgs a = a_in;
     a.extent = load_extent(a_in);
     set_pair_scale(a);
@@ -1455,22 +1553,23 @@ struct BhWorkspace {
     int device = 0;
     cudaStream_t stream = nullptr;  // allocations and frees are ordered on it
     size_t cap_n = 0;
-    int grid_build = 0;  // blocks of the per-level build kernels
     uint64_t *keys[2] = {nullptr, nullptr};
     uint32_t *vals[2] = {nullptr, nullptr};
-    // sort_meta: [0, 2048) digit histograms of the 8 passes, [2048, 2056) tile
-    // counters, [2056] epoch; sort_status: look-back words, tiles x 256
+    // sort_meta: digit histograms of the passes, then the passes' tile
+    // counters, then the epoch; sort_status: look-back words, tiles x digits
     uint32_t *sort_meta = nullptr;
     unsigned long long *sort_status = nullptr;
     float4 *sbody = nullptr;
-    double *spos = nullptr, *smass = nullptr;
+    uint8_t *lcp = nullptr;        // L(k): leading digits keys[k-1] and keys[k] share
+    uint32_t *mask = nullptr;      // level mask of each sorted body
+    uint8_t *leafcnt = nullptr;    // bodies of the leaf starting at each sorted body
+    uint32_t *blk_cnt = nullptr;   // per level and tree block: nodes starting in it
+    uint32_t *blk_off = nullptr;   // ... and the level's nodes before the block
+    uint32_t *nchild32 = nullptr;  // children of each node (counted by the node kernel)
     NodeArrays nd = {};
     LevelInfo *lv = nullptr;
-    unsigned long long *level_status = nullptr;  // look-back words of the level build
     unsigned long long *extent_bits = nullptr;
     unsigned long long *stats = nullptr;  // node visits, pair interactions of the last traversal
-    int32_t *top = nullptr;               // cell starts of tree level K (see top_levels)
-    int32_t *top_blockmin = nullptr;      // per-1024-cell minima while filling `top`
     uint32_t *flags = nullptr;
     int launches = 0;
     // which key/val buffer holds the sorted result
@@ -1483,14 +1582,14 @@ struct BhWorkspace {
 
 static void ws_release(BhWorkspace *ws)
 {
-    void *p[] = {ws->keys[0],  ws->keys[1],   ws->vals[0],       ws->vals[1],     ws->sort_meta,
-                 ws->sort_status,
-                 ws->sbody,    ws->spos,      ws->smass,      ws->nd.msum_hi, ws->nd.msum_lo,
-                 ws->nd.begin, ws->nd.count,  ws->nd.child,      ws->nd.nchild,   ws->nd.level,
-                 ws->nd.c64,   ws->nd.geo,    ws->nd.com,        ws->lv,          ws->level_status,
-                 ws->extent_bits, ws->flags, ws->nd.meta, ws->stats,
-                 ws->top, ws->top_blockmin, ws->nd.parent, ws->nd.quad_a, ws->nd.quad_b,
-                 ws->nd.arrivals};
+    void *p[] = {ws->keys[0],     ws->keys[1],    ws->vals[0],    ws->vals[1],
+                 ws->sort_meta,   ws->sort_status, ws->sbody,     ws->lcp,
+                 ws->mask,        ws->leafcnt,    ws->blk_cnt,    ws->blk_off,
+                 ws->nchild32,    ws->nd.msum_hi, ws->nd.msum_lo, ws->nd.begin,
+                 ws->nd.count,    ws->nd.child,   ws->nd.nchild,  ws->nd.level,
+                 ws->nd.c64,      ws->nd.geo,     ws->nd.com,     ws->lv,
+                 ws->extent_bits, ws->flags,      ws->nd.meta,    ws->stats,
+                 ws->nd.parent,   ws->nd.quad_a,  ws->nd.quad_b,  ws->nd.arrivals};
     for (void *q : p) dev_free(q, ws->stream);
 }
 
@@ -1515,9 +1614,8 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf, cudaStream_t st
     w->stream = stream;
     const size_t cap = n < 64 ? 64 : n;
     w->cap_n = cap;
-    const int sms = device_sm_count(device);
-    w->grid_build = sms * 2;
     const int tiles = cdiv((long long)cap, kSortTile);
+    const size_t tree_blocks = (size_t)cdiv((long long)cap, kTreeBlock);
     // Node capacity: leaves hold about leaf/4 bodies on average, so 8N/leaf
     // (at most 4N) nodes hold every non-degenerate distribution; deeper
     // chains only leave levels unsplit (exact, slower) and raise a flag.
@@ -1533,8 +1631,12 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf, cudaStream_t st
     PG_WA(w->sort_meta, (size_t)kSortPasses * kRadixBuckets + kSortPasses + 1);
     PG_WA(w->sort_status, (size_t)kRadixBuckets * tiles);
     PG_WA(w->sbody, cap);
-    PG_WA(w->spos, 3 * cap);
-    PG_WA(w->smass, cap);
+    PG_WA(w->lcp, cap);
+    PG_WA(w->mask, cap);
+    PG_WA(w->leafcnt, cap);
+    PG_WA(w->blk_cnt, 32 * tree_blocks);
+    PG_WA(w->blk_off, 32 * tree_blocks);
+    PG_WA(w->nchild32, ncap);
     PG_WA(w->nd.begin, ncap);
     PG_WA(w->nd.count, ncap);
     PG_WA(w->nd.child, ncap);
@@ -1551,11 +1653,7 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf, cudaStream_t st
     PG_WA(w->nd.quad_b, ncap);
     PG_WA(w->nd.arrivals, ncap);
     PG_WA(w->stats, 4);
-    // top tables of both tree kinds fit 2^21 + 1 entries
-    PG_WA(w->top, ((size_t)1 << 21) + 1);
-    PG_WA(w->top_blockmin, ((size_t)1 << 21) / 1024);
     PG_WA(w->lv, 1);
-    PG_WA(w->level_status, ncap / kBuildThreads + 2);
     PG_WA(w->extent_bits, 1);
     PG_WA(w->flags, 4);
 #undef PG_WA
@@ -1564,9 +1662,6 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf, cudaStream_t st
         (cudaMemsetAsync(w->flags, 0, 4 * sizeof(uint32_t), stream) != cudaSuccess ||
          cudaMemsetAsync(w->nd.arrivals, 0, ncap * sizeof(uint32_t), stream) != cudaSuccess ||
          cudaMemsetAsync(w->lv, 0, sizeof(LevelInfo), stream) != cudaSuccess ||
-         cudaMemsetAsync(w->level_status, 0,
-                         (ncap / kBuildThreads + 2) * sizeof(unsigned long long),
-                         stream) != cudaSuccess ||
          cudaMemsetAsync(w->sort_meta, 0,
                          ((size_t)kSortPasses * kRadixBuckets + kSortPasses + 1) * sizeof(uint32_t),
                          stream) != cudaSuccess ||
@@ -1642,6 +1737,16 @@ int bh_stats(BhWorkspace *ws, cudaStream_t st, uint64_t out[2])
     return PHYSIM_OK;
 }
 
+namespace {
+std::atomic<uint32_t> g_wait_limit{0};  // 0: kLookbackSpins
+std::atomic<int32_t> g_stall_tile{-1};
+int wait_limit()
+{
+    const uint32_t v = g_wait_limit.load();
+    return v == 0u ? kLookbackSpins : (int)std::min<uint32_t>(v, (uint32_t)INT32_MAX);
+}
+}  // namespace
+
 static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, cudaStream_t st)
 {
     const int n = (int)b.n;
@@ -1663,33 +1768,35 @@ static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, c
     for (int pass = 0; pass < kSortPasses; ++pass) {
         radix_pass_kernel<<<tiles, kSortThreads, 0, st>>>(
             ws->keys[cur], pass == 0 ? nullptr : ws->vals[cur], ws->keys[cur ^ 1],
-            ws->vals[cur ^ 1], n, pass, ghist, tile_ctr, ws->sort_status, epoch, ws->flags);
+            ws->vals[cur ^ 1], n, pass, ghist, tile_ctr, ws->sort_status, epoch, ws->flags,
+            wait_limit(), g_stall_tile.load());
         cur ^= 1;
         launches += 1;
     }
     ws->sorted = cur;
-    gather_kernel<<<cdiv(n, 256), 256, 0, st>>>(ws->vals[cur], n, b.body4, b.x, b.y, b.z, b.m,
-                                                ws->sbody, ws->spos, ws->smass);
-    root_kernel<<<1, 32, 0, st>>>(ws->nd, ws->lv, n, ws->extent_bits);
-    launches += 2;
-    const int D = tree_levels(p.nchild);
-    const int K = top_levels(p.nchild, n);
-    const int top_cells = 1 << (level_bits(p.nchild) * K);
-    PG_CUDA(cudaMemsetAsync(ws->top, 0xff, top_cells * sizeof(int32_t), st));
-    top_mark_kernel<<<cdiv(n, 256), 256, 0, st>>>(ws->keys[cur], n, level_bits(p.nchild) * (D - K),
-                                                  ws->top);
-    top_blockmin_kernel<<<top_cells / 1024, 1024, 0, st>>>(ws->top, n, ws->top_blockmin);
-    top_fill_kernel<<<top_cells / 1024, 1024, 0, st>>>(ws->top, top_cells, n, ws->top_blockmin);
-    launches += 3;
-    for (int level = 0; level < D; ++level) {
-        level_kernel<<<ws->grid_build, kBuildThreads, 0, st>>>(
-            ws->keys[cur], ws->nd, ws->lv, level, p.leaf_size, p.nchild, ws->top, K,
-            ws->level_status, ws->flags);
-        launches += 1;
-    }
-    moments_kernel<<<sms * 4, 256, 0, st>>>(ws->nd, ws->lv, ws->sbody, ws->spos, ws->smass, n,
-                                            p.multipole == kMultipoleQuadrupole ? 1 : 0);
-    launches += 1;
+    // the tree: boundaries (+ sorted f32 bodies), level masks, one scan, node
+    // records, centres, moments
+    boundary_kernel<<<cdiv(n, 256), 256, 0, st>>>(ws->keys[cur], ws->vals[cur], n, p.nchild,
+                                                  b.body4, ws->sbody, ws->lcp, ws->flags);
+    const int tree_blocks = cdiv(n, kTreeBlock);
+    PG_CHECK(p.leaf_size >= 1 && p.leaf_size <= kMaxLeaf, PHYSIM_ERR_ARGUMENT,
+             "leaf size %d outside 1..%d", p.leaf_size, kMaxLeaf);
+    mask_kernel<<<tree_blocks, kTreeBlock, 0, st>>>(ws->keys[cur], ws->lcp, n, p.nchild,
+                                                    p.leaf_size, ws->mask, ws->blk_cnt,
+                                                    tree_blocks, ws->leafcnt, ws->nchild32,
+                                                    ws->nd.cap, ws->flags);
+    level_scan_kernel<<<1, 1024, 0, st>>>(ws->blk_cnt, tree_blocks, p.nchild, ws->blk_off, ws->lv,
+                                          ws->nd.cap, ws->flags);
+    node_kernel<<<tree_blocks, kTreeBlock, 0, st>>>(ws->keys[cur], ws->leafcnt, ws->mask,
+                                                    ws->blk_off, tree_blocks, n, p.nchild, ws->nd,
+                                                    ws->lv, ws->nchild32, ws->flags);
+    centre_kernel<<<sms * 8, 256, 0, st>>>(ws->keys[cur], ws->nd, ws->lv, p.nchild,
+                                           p.traversal == PHYSIM_TRAVERSAL_EXACT ? 1 : 0,
+                                           ws->extent_bits, ws->flags);
+    moments_kernel<<<sms * 4, 256, 0, st>>>(ws->nd, ws->lv, ws->sbody,
+                                            p.multipole == kMultipoleQuadrupole ? 1 : 0,
+                                            ws->nchild32, ws->flags);
+    launches += 6;
     PG_CUDA(cudaGetLastError());
     ws->launches = launches;
     return PHYSIM_OK;
@@ -1707,7 +1814,9 @@ int bh_accelerations(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, 
     TravArgs a;
     a.nd = ws->nd;
     a.sbody = ws->sbody;
-    a.spos = ws->spos;
+    a.bx = b.x;
+    a.by = b.y;
+    a.bz = b.z;
     a.order = ws->vals[ws->sorted];
     a.lv = ws->lv;
     a.n = n;
@@ -1785,3 +1894,15 @@ int bh_snapshot(BhWorkspace *ws, size_t n, cudaStream_t st, PhysimTreeSnapshot *
 }
 
 }  // namespace pg
+
+extern "C" int physim_gpu_set_wait_limit(uint32_t polls)
+{
+    pg::g_wait_limit.store(polls);
+    return PHYSIM_OK;
+}
+
+extern "C" int physim_gpu_test_stall_sort(int32_t tile)
+{
+    pg::g_stall_tile.store(tile < 0 ? -1 : tile);
+    return PHYSIM_OK;
+}

@@ -218,3 +218,37 @@ def test_full_size_workload(oracle_mod, theta):
     ref = oracle_mod.barnes_hut(s, theta, 0.01, nchild=8, idx=idx)
     e_ref, e_gpu = rms(rel_err(ref, exact)), rms(rel_err(a[idx], exact))
     assert e_gpu <= 1.05 * e_ref + 1e-6, (e_gpu, e_ref)
+
+
+def test_bounded_sort_wait_reports_timeout(oracle_mod):
+    """The radix sort's look-back waits are bounded: with a short limit and a
+    tile whose look-back never sees its predecessors, the wait runs out, the
+    rest of the build and the traversal are skipped, and the next
+    synchronising call returns PHYSIM_ERR_TIMEOUT instead of hanging; the
+    library works normally after."""
+    import time
+
+    import physim_gb300 as pg
+    from physim_gb300 import ics
+    lib = pg.lib
+    s = ics.cube_with_stars(40000, seed=3)  # 5 sort tiles of 8,192 keys
+    cfg = pg.SimConfig(gravity="astro2", theta=0.5, e=0.01, leaf_size=16, traversal="warp")
+    lib.physim_gpu_set_wait_limit(1000)
+    lib.physim_gpu_test_stall_sort(2)
+    try:
+        with pg.Simulation(s, cfg) as sim:
+            t0 = time.perf_counter()
+            with pytest.raises(pg.PhysimError) as err:
+                sim.step(2)
+                sim.synchronize()
+            assert err.value.code == 5  # PHYSIM_ERR_TIMEOUT
+            assert time.perf_counter() - t0 < 30.0
+    finally:
+        lib.physim_gpu_test_stall_sort(-1)
+        lib.physim_gpu_set_wait_limit(0)
+    idx = np.arange(0, len(s), 997)
+    with pg.Simulation(s, cfg) as sim:
+        got = sim.accelerations()
+        ref = sim.accelerations_f64(idx)
+    assert np.isfinite(_vec(got)).all()
+    assert rms(rel_err(got[idx], ref)) < 0.05
