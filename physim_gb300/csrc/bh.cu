@@ -11,16 +11,17 @@
 //                octree 21 levels x 3 bits = 63 bits, quadtree 31 x 2 = 62.
 //                Bodies within a rounding margin of a cell boundary re-derive
 //                q by replaying the reference's f64 centre arithmetic.
-//   3. sort      stable LSD radix sort of (key, body) pairs, 8-bit digits.
-//   4. tree      level-by-level, not path-compressed (as the reference's
-//                pointer tree): a cell with more than leaf_size bodies that
-//                are not all at one key splits into its non-empty children;
-//                children are contiguous, levels are contiguous, and node
-//                order is deterministic (per-level scans, no atomics).
-//                Geometric centres are computed exactly as the reference does
-//                (child = parent +- extent/2, octree.rs:167-215).
-//   5. moments   mass, centre of mass (f64 sums) and optionally second
-//                moments (f32) of every cell, bottom up in one launch.
+//   3. sort      stable LSD radix sort of (key, body) pairs, 9-bit digits.
+//   4. tree      not path-compressed (as the reference's pointer tree): a
+//                cell with more than leaf_size bodies that are not all at
+//                one key splits into its non-empty children; breadth-first
+//                layout (levels contiguous, children contiguous in key
+//                order), built flat for all levels at once from the
+//                key-prefix boundaries (section 4).  Geometric centres are
+//                computed exactly as the reference does (child = parent +-
+//                extent/2, octree.rs:167-215).
+//   5. moments   mass, centre of mass (double-float sums) and optionally
+//                second moments (f32) of every cell, bottom up in one launch.
 //   6. traversal one warp per 32 consecutive sorted bodies, DFS with a shared
 //                stack, the reference's opening rule extent/|x - centre| < theta
 //                (octree.rs:137-144).  EXACT: every body keeps its own
@@ -30,6 +31,8 @@
 //                MUFU.RSQ per pair and compensated per-body sums.
 #include <stdio.h>
 #include <string.h>
+
+#include <cuda/atomic>
 
 #include <algorithm>
 #include <atomic>
@@ -42,7 +45,7 @@ namespace pg {
 
 namespace {
 
-constexpr int kRadixBits = 8;
+constexpr int kRadixBits = 9;
 constexpr int kRadixBuckets = 1 << kRadixBits;
 // 8,192 keys per tile: few tiles keep the look-back chains of a pass short
 // (all tiles of a 1M-key sort are resident at once, so a pass's time is set
@@ -64,8 +67,9 @@ constexpr int kFlagNodes = 0;
 constexpr int kFlagStack = 1;
 constexpr int kFlagSort = 2;
 
-// Radix sort of the 63-bit (62-bit) keys: 8 passes of 8-bit digits.
-constexpr int kSortPasses = 8;
+// Radix sort of the 63-bit (62-bit) keys: 7 passes of 9-bit digits (512
+// digits: one look-back thread each in a 512-thread tile).
+constexpr int kSortPasses = 7;
 // Look-back spin limit per digit (each spin is one L2 load, ~0.5 us worst
 // case), far above any wait of a running predecessor tile; the default of
 // physim_gpu_set_wait_limit.
@@ -176,7 +180,7 @@ __device__ __forceinline__ uint64_t spread2(uint32_t v)
     return x;
 }
 
-// Keys, plus the histograms of all 8 radix digits of all keys (block-local in
+// Keys, plus the histograms of all 7 radix digits of all keys (block-local in
 // shared memory, then one global atomic per non-empty bucket), for the
 // one-sweep sort.  ghist [8][256] must be zero on entry.  Block 0 also resets
 // the sort's tile counters and advances its epoch (see radix_pass_kernel).
@@ -226,7 +230,7 @@ keys_kernel(const double *__restrict__ x, const double *__restrict__ y,
 }
 
 // ---------------------------------------------------------------------------
-// 3. radix sort (stable, LSD, 8-bit digits)
+// 3. radix sort (stable, LSD, 9-bit digits)
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t lanemask_lt()
 {
@@ -813,7 +817,7 @@ __global__ void centre_kernel(const uint64_t *__restrict__ keys, NodeArrays nd,
 // double-float (hi + lo f32) pairs, each product m x taken exactly (TwoProduct
 // by FMA) -- FP32 arithmetic only, as GB300 issues f64 instructions at a small
 // fraction of its f32 rate.  A parent is finished by the thread of its last
-// child to arrive (atomic count of arrivals after a fence; nothing waits),
+// child to arrive (an acquire-release count of arrivals; nothing waits),
 // which adds the children's pairs in child order -- so results do not depend
 // on the arrival order -- and continues upwards; it also completes the
 // parent's body count, child count and traversal metadata.  The f32 centre
@@ -910,10 +914,11 @@ __global__ void moments_kernel(NodeArrays nd, const LevelInfo *__restrict__ lv,
             const int par = nd.parent[node];
             if (par < 0) break;
             const int nc = (int)nchild32[par];
-            __threadfence();
-            const uint32_t arrived = atomicAdd(&nd.arrivals[par], 1u);
+            // release: this child's sums are visible before its arrival
+            // counts; acquire: the last arriver sees every sibling's
+            cuda::atomic_ref<uint32_t, cuda::thread_scope_device> arrivals(nd.arrivals[par]);
+            const uint32_t arrived = arrivals.fetch_add(1u, cuda::memory_order_acq_rel);
             if (arrived + 1u != (uint32_t)nc) break;
-            __threadfence();
             nd.arrivals[par] = 0u;  // ready for the next build
             const int fc = nd.child[par];
             float4 ph = __ldcg(&nd.msum_hi[fc]), pl = __ldcg(&nd.msum_lo[fc]);
@@ -1762,7 +1767,7 @@ static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, c
         b.x, b.y, b.z, n, p.nchild, ws->extent_bits, ws->keys[0], ws->vals[0], ghist, tile_ctr,
         epoch);
     launches += 2;
-    // one-sweep radix sort: one launch per 8-bit digit
+    // one-sweep radix sort: one launch per 9-bit digit
     const int tiles = cdiv(n, kSortTile);
     int cur = 0;
     for (int pass = 0; pass < kSortPasses; ++pass) {
