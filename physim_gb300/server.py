@@ -44,8 +44,11 @@ BYTES_PER_BODY_DIRECT = 200
 BYTES_PER_BODY_TREE = 700
 BYTES_FIXED = 4 << 20
 # Smallest direct-sum job that may evaluate each unordered pair once (the
-# lowest size threshold the ensemble autotuner picks)
+# lowest size threshold the ensemble autotuner picks), and the largest slot
+# buffer the library gives that plan (a quarter of a GB300's memory; above it
+# the library takes a one-pair plan, which has no slot buffer)
 SYMMETRIC_FROM = 8192
+SYMMETRIC_CAP_BYTES = 288 * (1 << 30) // 4
 
 
 @dataclass(order=True)
@@ -66,8 +69,10 @@ class JobSpec:
         per = BYTES_PER_BODY_DIRECT if self.gravity == "simple_astro" else BYTES_PER_BODY_TREE
         if self.gravity == "simple_astro" and self.n >= SYMMETRIC_FROM:
             # evaluating each unordered pair once keeps an f32 slot sum per
-            # body for every 1,024-body tile
-            per += 12 * ((self.n + 1023) // 1024)
+            # body for every 1,024-body tile, while that fits the library's cap
+            slots = 12 * ((self.n + 1023) // 1024)
+            if slots * self.n <= SYMMETRIC_CAP_BYTES:
+                per += slots
         return BYTES_FIXED + per * self.n
 
     def step_seconds(self) -> float:

@@ -289,6 +289,20 @@ def test_device_bytes_estimates():
     assert tree.device_bytes() == BYTES_FIXED + BYTES_PER_BODY_TREE * tree.n
 
 
+def test_device_bytes_mirror_the_symmetric_cap():
+    """Above the library's cap on the slot buffer (a quarter of a GB300's
+    memory: about 2.4M bodies) direct sums take a one-pair plan, which keeps
+    no slot sums, so the estimate counts none."""
+    from physim_gb300.server import SYMMETRIC_CAP_BYTES
+    under = job(0, 2_000_000, 10)
+    over = job(1, 3_000_000, 10)
+    slots_under = 12 * ((under.n + 1023) // 1024)
+    assert slots_under * under.n <= SYMMETRIC_CAP_BYTES
+    assert under.device_bytes() == BYTES_FIXED + (BYTES_PER_BODY_DIRECT + slots_under) * under.n
+    assert 12 * ((over.n + 1023) // 1024) * over.n > SYMMETRIC_CAP_BYTES
+    assert over.device_bytes() == BYTES_FIXED + BYTES_PER_BODY_DIRECT * over.n
+
+
 def test_async_admission_cutoff_while_building():
     """A run cut off while units are still being built counts their jobs as
     unfinished, and close() waits for the builds and closes their units."""
