@@ -432,11 +432,15 @@ def measure_direct(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict
     achieved = flops_step / (kern_ms / 1e3) / 1e12
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
     peak = sms * FP32_LANES_PER_SM * 2 * sm_max * 1e6 / 1e12
-    traffic = None
+    # DRAM bytes per launch from a committed ncu capture of a smaller case,
+    # scaled to this workload (not measured in this run)
+    traffic, traffic_source = None, None
     tfile = ROOT / "profiles" / "direct_forces_traffic.json"
     if tfile.exists() and args.bodies == N_CUBE:
         try:
-            traffic = json.loads(tfile.read_text()).get(kernel, {}).get("bytes_per_launch")
+            rec = json.loads(tfile.read_text()).get(kernel, {})
+            traffic = rec.get("bytes_per_launch")
+            traffic_source = "committed capture, not this run: " + rec.get("basis", "")
         except (ValueError, AttributeError):
             traffic = None
     out = {"value": all_pairs / (total_ms / 1e3) / 1e9, "ms_per_step": total_ms / args.steps,
@@ -444,7 +448,7 @@ def measure_direct(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict
            "plan": plan,
            "roofline": {"bound": "fp32", "kernel": kernel, "achieved": achieved,
                         "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                        "traffic": traffic,
+                        "traffic": traffic, "traffic_source": traffic_source,
                         "peak_basis": f"{sms} SMs x {FP32_LANES_PER_SM} FP32 lanes x 2 x "
                                       f"{sm_max:.0f} MHz (max SM clock, measured-peaks file)",
                         "flop_per_pair": flop_note,
@@ -459,7 +463,7 @@ def measure_direct(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict
                 sms * FP32_LANES_PER_SM * 2 * clk["sm_mhz"] * 1e6 / 1e12)
 
     if not args.skip_e2e:
-        e2e_steps = args.e2e_steps or max(2, min(args.steps, 3))
+        e2e_steps = args.e2e_steps or max(3, min(args.steps, 5))
         props = {"e": E, "device": device}
         runs = {m: host_array_steps(pg, "simple_astro", props, state, e2e_steps, device, m)
                 for m in ("copy", "auto")}

@@ -54,6 +54,7 @@ constexpr int kSortThreads = 512;
 constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr int kSortWarps = kSortThreads / 32;
+constexpr size_t kSortSmem = (size_t)kSortTile * (sizeof(uint64_t) + sizeof(uint32_t));  // staged tile
 
 constexpr int kMaxLevels = 31;
 
@@ -273,9 +274,11 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *w
 // Adinets & Merrill 2022).  Tiles of kSortTile keys are claimed in launch
 // order from an atomic counter, so every tile a block looks back at is held
 // by a block that is already running.  Each block ranks its keys by digit
-// (warp by warp, stable), publishes its per-digit counts, then walks back over
-// the preceding tiles' published words until it meets an inclusive prefix,
-// publishes its own inclusive prefix, and scatters.  A status word is
+// (warp by warp, stable, lanes of equal digit found by one ballot per digit
+// bit), publishes its per-digit counts, then walks back over the preceding
+// tiles' published words until it meets an inclusive prefix, publishes its
+// own inclusive prefix, and scatters: the tile is first put in digit order
+// in shared memory, so each digit's keys leave in one contiguous run.  A status word is
 // (epoch * 4 + flag) << 32 | count, flag 1 = tile count, 2 = inclusive
 // prefix, and epoch counts (sort, pass) pairs; words of earlier passes and
 // sorts carry older epochs and read as not ready, so the status array needs
@@ -299,6 +302,7 @@ radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restri
     if (*(volatile const uint32_t *)&flags[kFlagSort] != 0u) return;  // an earlier wait failed
     __shared__ uint32_t h[kSortWarps][kRadixBuckets];
     __shared__ uint32_t digit_off[kRadixBuckets];
+    __shared__ uint32_t local_start[kRadixBuckets];  // the digit's first key in the staged tile
     __shared__ uint32_t ws[33];
     __shared__ int s_tile;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -329,8 +333,16 @@ radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restri
     for (int r = 0; r < kSortItems; ++r) {
         const int idx = base + r * 32 + lane;
         const bool valid = idx < n;
-        const uint32_t d = valid ? (uint32_t)(kk[r] >> shift) & (kRadixBuckets - 1) : 0xffffffffu;
-        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        // lanes with this lane's digit: one vote per digit bit (MATCH.ANY is
+        // several times slower here)
+        const uint32_t d = valid ? (uint32_t)(kk[r] >> shift) & (kRadixBuckets - 1) : 0u;
+        uint32_t peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+        for (int b = 0; b < kRadixBits; ++b) {
+            const uint32_t bit = (d >> b) & 1u;
+            const uint32_t vote = __ballot_sync(0xffffffffu, bit);
+            peers &= bit ? vote : ~vote;
+        }
         const uint32_t before = __popc(peers & lanemask_lt());
         uint32_t cur = 0;
         if (valid) cur = h[warp][d];
@@ -349,6 +361,10 @@ radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restri
             const uint32_t c = h[w][d];
             h[w][d] = count;
             count += c;
+        }
+        {
+            uint32_t total;
+            local_start[d] = block_exclusive_scan(count, ws, total);
         }
         // tag base of this sort and pass: the passes share the status array
         const unsigned long long ep =
@@ -395,14 +411,28 @@ radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restri
         digit_off[d] = digit_base + excl;
     }
     __syncthreads();
+    // the tile in digit order in shared memory, then each digit's run written
+    // to its place in one contiguous stretch (scattered 8-byte stores cost
+    // a third of the pass)
+    extern __shared__ uint64_t skeys[];  // kSortTile keys, then kSortTile values
+    uint32_t *svals = reinterpret_cast<uint32_t *>(skeys + kSortTile);
 #pragma unroll
     for (int r = 0; r < kSortItems; ++r) {
         const int idx = base + r * 32 + lane;
         if (idx >= n) continue;
         const uint32_t dg = (uint32_t)(kk[r] >> shift) & (kRadixBuckets - 1);
-        const uint32_t pos = digit_off[dg] + h[warp][dg] + rank[r];
-        keys_out[pos] = kk[r];
-        vals_out[pos] = vv[r];
+        const uint32_t lp = local_start[dg] + h[warp][dg] + rank[r];
+        skeys[lp] = kk[r];
+        svals[lp] = vv[r];
+    }
+    __syncthreads();
+    const int cnt = min(kSortTile, n - tile * kSortTile);
+    for (int j = threadIdx.x; j < cnt; j += kSortThreads) {
+        const uint64_t key = skeys[j];
+        const uint32_t dg = (uint32_t)(key >> shift) & (kRadixBuckets - 1);
+        const uint32_t pos = digit_off[dg] + (uint32_t)j - local_start[dg];
+        keys_out[pos] = key;
+        vals_out[pos] = svals[j];
     }
 }
 
@@ -1613,6 +1643,14 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf, cudaStream_t st
         delete ws;
         ws = nullptr;
     }
+    // the radix pass stages its tile in 96 KB of dynamic shared memory; set
+    // once per device, here (never inside a stream capture)
+    static std::atomic<bool> sort_smem_set[64];
+    if (device >= 0 && device < 64 && !sort_smem_set[device].load()) {
+        PG_CUDA(cudaFuncSetAttribute(radix_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kSortSmem));
+        sort_smem_set[device].store(true);
+    }
     BhWorkspace *w = new (std::nothrow) BhWorkspace();
     PG_CHECK(w, PHYSIM_ERR_MEMORY, "out of host memory");
     w->device = device;
@@ -1771,7 +1809,7 @@ static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, c
     const int tiles = cdiv(n, kSortTile);
     int cur = 0;
     for (int pass = 0; pass < kSortPasses; ++pass) {
-        radix_pass_kernel<<<tiles, kSortThreads, 0, st>>>(
+        radix_pass_kernel<<<tiles, kSortThreads, kSortSmem, st>>>(
             ws->keys[cur], pass == 0 ? nullptr : ws->vals[cur], ws->keys[cur ^ 1],
             ws->vals[cur ^ 1], n, pass, ghist, tile_ctr, ws->sort_status, epoch, ws->flags,
             wait_limit(), g_stall_tile.load());
