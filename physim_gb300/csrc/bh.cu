@@ -1836,9 +1836,11 @@ static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, c
     centre_kernel<<<sms * 8, 256, 0, st>>>(ws->keys[cur], ws->nd, ws->lv, p.nchild,
                                            p.traversal == PHYSIM_TRAVERSAL_EXACT ? 1 : 0,
                                            ws->extent_bits, ws->flags);
-    moments_kernel<<<sms * 4, 256, 0, st>>>(ws->nd, ws->lv, ws->sbody,
-                                            p.multipole == kMultipoleQuadrupole ? 1 : 0,
-                                            ws->nchild32, ws->flags);
+    // one thread per node (the capacity bounds the count): a grid-stride loop
+    // would queue a second leaf's climb behind the first's on one thread
+    moments_kernel<<<cdiv(ws->nd.cap, 256), 256, 0, st>>>(
+        ws->nd, ws->lv, ws->sbody, p.multipole == kMultipoleQuadrupole ? 1 : 0, ws->nchild32,
+        ws->flags);
     launches += 6;
     PG_CUDA(cudaGetLastError());
     ws->launches = launches;
