@@ -252,3 +252,67 @@ def test_bounded_sort_wait_reports_timeout(oracle_mod):
         ref = sim.accelerations_f64(idx)
     assert np.isfinite(_vec(got)).all()
     assert rms(rel_err(got[idx], ref)) < 0.05
+
+
+def _near_coincident_state():
+    """3,000 cube bodies + 2 stars, then four groups of three bodies within
+    4e-10 of an f32-exact point on every axis (masses 1, 2, 3)."""
+    from physim_gb300 import ics
+    s = ics.cube_with_stars(3000, seed=81, stars=ics.STARS_2)
+    rng = np.random.default_rng(5)
+    bases = np.float32(rng.uniform(-0.4, 0.4, size=(4, 3))).astype(np.float64)
+    extra, groups = [], []
+    for b in bases:
+        idx = []
+        for k in range(3):
+            e = s[:1].copy()
+            e["x"], e["y"], e["z"] = b + rng.uniform(1e-10, 4e-10, 3) * rng.choice([-1, 1], 3)
+            e["vx"] = e["vy"] = e["vz"] = 0.0
+            e["mass"] = 1.0 + k
+            extra.append(e)
+            idx.append(len(s) + len(extra) - 1)
+        groups.append(idx)
+    return np.concatenate([s] + extra), groups, bases
+
+
+def test_near_coincident_bodies_against_the_reference_merge(oracle_mod):
+    """The reference merges a body within 1e-9 of a leaf's body on every axis
+    into one pseudo-particle with their summed mass at the newer body's
+    position (astro/src/octree.rs:69-80); this build keeps the bodies
+    individual, and in its FP32 pair arithmetic they coincide (zero force
+    between them).  Measured here on a direct-sum traversal (theta < 0, every
+    leaf opened, so the tree's contents are all that differs):
+      * every other body matches the reference within the FP32 tolerance (the
+        merge moves a group's mass by < 1e-9);
+      * a group member's acceleration differs from the reference's by exactly
+        the pseudo-particle's pull, M d / sqrt(r^2 (r^2 + e)^2) toward the
+        newest member (zero for the newest), to 1e-5 of |a|; on this state
+        that pull is 1.2e-3 .. 2.8e-3 of |a| (e = 0.01)."""
+    import physim_gb300 as pg
+    s, groups, bases = _near_coincident_state()
+    e = 0.01
+    acc = pg.accelerations(len(s))
+    with pg.TransformElementHandler("astro2", {"theta": -0.1, "e": e}) as el:
+        el.transform(s, acc)
+    # this build's result: the direct sum with each group at its shared f32 point
+    col = s.copy()
+    for idx, b in zip(groups, bases):
+        col["x"][idx], col["y"][idx], col["z"][idx] = b
+    assert rel_err(acc, oracle_mod.simple_astro(col, e)).max() < RTOL
+    ref = oracle_mod.barnes_hut(s, -0.1, e, nchild=8)
+    grp = np.array(sum(groups, []))
+    other = np.setdiff1d(np.arange(len(s)), grp)
+    assert rel_err(acc[other], ref[other]).max() < RTOL
+    pos = np.stack([s["x"], s["y"], s["z"]], axis=1)
+    diff = _vec(ref) - _vec(acc)
+    pulls = []
+    for idx in groups:
+        p, mass = pos[idx[-1]], s["mass"][idx].sum()
+        for k in idx:
+            d = p - pos[k]
+            r2 = float(d @ d)
+            pull = mass * d / np.sqrt(r2 * (r2 + e) ** 2) if r2 > 0.0 else np.zeros(3)
+            norm = np.linalg.norm(_vec(ref)[k])
+            assert np.linalg.norm(diff[k] - pull) < RTOL * norm, k
+            pulls.append(np.linalg.norm(pull) / norm)
+    assert 1e-3 < max(pulls) < 1e-2 and min(pulls) == 0.0
