@@ -89,7 +89,10 @@ def parse():
                         "within an in-flight budget, or every admitted unit at once")
     p.add_argument("--serve-inflight-ms", type=float, default=30.0,
                    help="estimated device work kept in flight under srpt scheduling")
-    p.add_argument("--serve-max-units", type=int, default=512,
+    p.add_argument("--serve-queue-ms", type=float, default=0.0,
+                   help="under 'all' scheduling, estimated device work queued at most (units "
+                        "ticked least recently first); 0 hands every idle unit a tick at once")
+    p.add_argument("--serve-max-units", type=int, default=2048,
                    help="most units (ensembles, simulations) admitted at one time; the default "
                         "is high enough that the 150 GB HBM budget is what limits admission")
     p.add_argument("--serve-fifo-baseline", action="store_true",
@@ -840,7 +843,9 @@ def measure_served(args, dist: Dist, device: int) -> dict:
                          admission=args.serve_admission, scheduling=args.serve_scheduling,
                          inflight_seconds=args.serve_inflight_ms / 1e3,
                          async_admission=bool(args.serve_async_admission),
-                         max_units=args.serve_max_units)
+                         max_units=args.serve_max_units,
+                         queue_seconds=(args.serve_queue_ms / 1e3 if args.serve_queue_ms > 0
+                                        else None))
     plain_same = _serve_once(served_mix(rate=50.0, seconds=args.serve_seconds, seed=5),
                              PlainExecutor(device=device, download=True), until, max_units=1,
                              max_batch=1, admission=args.serve_admission)
@@ -858,7 +863,12 @@ def measure_served(args, dist: Dist, device: int) -> dict:
                           "Barnes-Hut job, each on its own stream)"
                         + (", units built on a worker thread" if args.serve_async_admission
                            else ""),
-           "scheduling": args.serve_scheduling,
+           "scheduling": args.serve_scheduling
+                         + (f" (at most {args.serve_queue_ms:.0f} ms of estimated device work "
+                            "queued, units ticked least recently first)"
+                            if args.serve_scheduling == "all" and args.serve_queue_ms > 0
+                            else f" (in flight {args.serve_inflight_ms:.0f} ms)"
+                            if args.serve_scheduling == "srpt" else ""),
            "jobs_arrived": len(jobs), "arrival_seconds": args.serve_seconds,
            "drain_seconds": args.serve_drain, "offered_direct_pairs": offered_direct}
     out.update(served)

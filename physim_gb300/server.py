@@ -100,7 +100,25 @@ class JobResult:
         return self.finished - self.spec.arrival
 
 
+def job_initialiser(spec: JobSpec) -> tuple[str, dict]:
+    """The device initialiser and its properties for a Barnes-Hut job's
+    bodies: the seeded cube (x, y in [-0.5, 0.5), z in [0, 0.5)) or Plummer
+    sphere (a = 0.1) of physim_gb300.initialisers, total mass 1, generated on
+    the GPU where the job's state lives (no host generation or upload when
+    its unit is built)."""
+    if spec.ic == "plummer":
+        return "plummer", {"n": spec.n, "seed": spec.seed, "a": 0.1}
+    return "cube", {"n": spec.n, "seed": spec.seed, "size": 0.5}
+
+
 def initial_state(spec: JobSpec) -> np.ndarray:
+    """A job's initial bodies on the host: for Barnes-Hut jobs the bodies
+    their units generate on the device (job_initialiser), for direct-sum jobs
+    the seeded host generators of physim_gb300.ics."""
+    if spec.gravity != "simple_astro":
+        from . import initialisers
+        kind, props = job_initialiser(spec)
+        return getattr(initialisers, kind)(props)
     from . import ics
     if spec.ic == "plummer":
         return ics.plummer(spec.n, seed=spec.seed, a=0.1)
@@ -408,12 +426,12 @@ class _SimUnit(Unit):
         self.ex = ex
         self.torch_stream = ex.stream_for(job.step_seconds()) \
             if hasattr(ex, "stream_for") else None
-        self.sim = Simulation(initial_state(job),
-                              SimConfig(gravity=job.gravity, theta=job.theta, e=job.e, dt=job.dt,
-                                        leaf_size=job.leaf_size, traversal="warp",
-                                        device=ex.device,
-                                        stream=(self.torch_stream.cuda_stream
-                                                if self.torch_stream else None)))
+        kind, props = job_initialiser(job)
+        self.sim = Simulation.generated(
+            kind, props,
+            SimConfig(gravity=job.gravity, theta=job.theta, e=job.e, dt=job.dt,
+                      leaf_size=job.leaf_size, traversal="warp", device=ex.device,
+                      stream=self.torch_stream.cuda_stream if self.torch_stream else None))
         self.tick = _CudaTick(self.sim.stream, ex.device)
         est_ms = max(job.n * 1.6e-6, 0.05) if job.gravity != "simple_astro" else \
             max(job.n * job.n / 2.0e12 * 1e3, 0.02)
@@ -460,7 +478,8 @@ class Server:
                  clock: Callable[[], float] = time.perf_counter,
                  max_units: int = 64, max_batch: int = 16, keep_states: bool = False,
                  admission: str = "fifo", scheduling: str = "all",
-                 inflight_seconds: float = 0.03, async_admission: bool = False):
+                 inflight_seconds: float = 0.03, async_admission: bool = False,
+                 queue_seconds: float | None = None):
         if admission not in ("fifo", "shortest"):
             raise ValueError(f"unknown admission policy {admission!r}")
         if scheduling not in ("all", "srpt"):
@@ -475,6 +494,13 @@ class Server:
         # preemption point is the end of a tick.
         self.scheduling = scheduling
         self.inflight_seconds = inflight_seconds
+        # queue_seconds (scheduling "all"): hand out ticks, least recently
+        # ticked unit first, only while the estimated device work in flight
+        # is below this; None hands every idle unit a tick at once.  Under a
+        # saturated GPU an unbounded round enqueues seconds of work, the host
+        # blocks in the launch calls and admission stalls with it.
+        self.queue_seconds = queue_seconds
+        self._ticks = 0
         # async_admission: admitted jobs' units (initial states, device
         # allocations, uploads) are built on a worker thread, so the loop
         # that hands out ticks never waits for them
@@ -608,9 +634,18 @@ class Server:
     def _dispatch(self) -> None:
         """Hands out ticks to the units that have none in flight."""
         idle = [u for u in self.units if not u.in_flight]
-        if self.scheduling == "all":
+        if self.scheduling == "all" and self.queue_seconds is None:
             for u in idle:
                 self._launch(u)
+        elif self.scheduling == "all":
+            inflight = sum(u.tick_seconds for u in self.units if u.in_flight)
+            for u in sorted(idle, key=lambda v: getattr(v, "last_tick", -1)):
+                if inflight >= self.queue_seconds:
+                    break
+                if self._launch(u):
+                    self._ticks += 1
+                    u.last_tick = self._ticks
+                    inflight += u.tick_seconds
         else:
             busy = [u for u in self.units if u.in_flight]
             inflight = sum(u.tick_seconds for u in busy)

@@ -320,3 +320,41 @@ def test_async_admission_cutoff_while_building():
     assert res == [] and srv.unfinished() == 3
     srv.close()
     assert ex.closed >= 1  # the unit built after the cut-off was closed
+
+
+def test_all_scheduling_queue_cap_round_robin():
+    """Under 'all' scheduling with queue_seconds, ticks go out least recently
+    ticked unit first while the estimated work in flight is below the cap
+    (at least one tick is always handed out)."""
+
+    class SlowUnit(FakeUnit):
+        def __init__(self, jobs, ex):
+            super().__init__(jobs, ex)
+            self.flight = 0
+
+        def launch_tick(self):
+            super().launch_tick()
+            self.tick_seconds = 0.004
+            self.flight = 2  # done after two polls
+            self.ex.order.append(self.jobs[0].id)
+
+        def tick_done(self):
+            self.flight -= 1
+            return self.flight <= 0
+
+    class SlowExecutor(FakeExecutor):
+        def __init__(self):
+            super().__init__(k=5)
+            self.order = []
+
+        def make_units(self, jobs):
+            return [SlowUnit([j], self) for j in jobs]
+
+    ex = SlowExecutor()
+    srv = Server(ex, hbm_budget=1 << 40, max_units=64, max_batch=64, queue_seconds=0.01)
+    srv.submit([JobSpec(arrival=0.0, id=i, n=1000, steps=20) for i in range(6)])
+    res = srv.run(until=30.0)
+    assert len(res) == 6 and not srv.failed
+    assert srv.max_running <= 3  # 3 x 4 ms reaches the 10 ms cap
+    # round robin: the first six ticks go to six different units
+    assert sorted(ex.order[:6]) == list(range(6))

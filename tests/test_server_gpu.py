@@ -24,10 +24,12 @@ def _alone(spec):
 
 @pytest.mark.parametrize("policy", [{}, {"async_admission": True},
                                     {"async_admission": True, "scheduling": "srpt",
-                                     "inflight_seconds": 0.01}])
+                                     "inflight_seconds": 0.01},
+                                    {"async_admission": True, "queue_seconds": 0.005}])
 def test_mix_equals_alone(policy):
-    """Also with units built on a worker thread while others run, and with
-    shortest-remaining-work tick scheduling."""
+    """Also with units built on a worker thread while others run, with
+    shortest-remaining-work tick scheduling, and with a cap on the work
+    queued under 'all' scheduling."""
     from physim_gb300.server import GpuExecutor, JobSpec, Server
     from test_verlet_gpu import trajectory_errors
     from physim_gb300.server import initial_state
