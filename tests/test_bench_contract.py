@@ -59,6 +59,7 @@ def test_parser_defaults(monkeypatch):
     a = bench.parse()
     assert (a.gpus, a.impl, a.only) == (1, "ours", "")
     assert a.warmup >= 3 and a.steps >= 1
-    assert a.serve_scheduling == "all" and a.serve_max_units == 512
+    assert a.serve_scheduling == "all" and a.serve_max_units == 2048
+    assert a.serve_queue_ms == 0.0  # every idle unit ticked at once
     assert a.serve_seconds == 120.0  # the configured 120 s of arrivals
     assert a.bh_sample == 16384 and a.bh_steps == 1000
