@@ -380,6 +380,15 @@ int physim_gpu_sim_set_plan(PhysimSim *sim, const PhysimDirectTuning *plan);
  * back to a one-pair plan.  Process-wide, read when a plan is made.  This
  * builds on simple_astro (transformers.rs:219-244), which has no plans. */
 int physim_gpu_set_symmetric_cap(uint64_t bytes);
+/* The each-pair-once plan runs one block per pair of 1,024-body tiles while
+ * that schedule's slot buffer (12 bytes per body per tile) is at most `bytes`
+ * (0 restores the default, 1 GiB: up to about 300,000 bodies), and in
+ * thread-block clusters over runs of tiles above that (slot sums 3T^2/32 x
+ * 12 KB for T tiles: 1.2 GB instead of 12.9 GB at 1,048,580 bodies).  Both
+ * give the same results within FP32 rounding.  Process-wide, read when a plan
+ * is made.  No reference counterpart (simple_astro, transformers.rs:219-244,
+ * has no plans). */
+int physim_gpu_set_symmetric_pairs_limit(uint64_t bytes);
 /* Barnes-Hut builds wait on other thread blocks only in the radix sort's
  * decoupled look-back; every such wait gives up after `polls` polls that saw
  * no progress (0 restores the default, 2^20), raising an error flag: later

@@ -9,7 +9,7 @@ that needs it (`lib.load()` loads it explicitly); that call fails loudly if
 the library is missing: there is no CPU fallback.
 """
 from ._lib import (LIB_PATH, PhysimError, host_access, last_error, lib, set_host_access,
-                   set_symmetric_cap)
+                   set_symmetric_cap, set_symmetric_pairs_limit)
 from .entity import ACCELERATION, ENTITY, accelerations, entities, entity_new
 from .plugin import (GpuIntegrator, GpuVerlet, NullElement, Pipeline, TransformElementHandler,
                      register)
@@ -20,5 +20,5 @@ __all__ = [
     "LIB_PATH", "PhysimError", "last_error", "lib", "ACCELERATION", "ENTITY", "accelerations",
     "entities", "entity_new", "GpuIntegrator", "GpuVerlet", "NullElement", "Pipeline",
     "TransformElementHandler", "register", "SimConfig", "Simulation", "Ensemble", "host_access",
-    "set_host_access", "set_symmetric_cap",
+    "set_host_access", "set_symmetric_cap", "set_symmetric_pairs_limit",
 ]

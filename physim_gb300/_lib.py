@@ -153,6 +153,7 @@ def _load() -> C.CDLL:
         "physim_gpu_sim_set_plan": (C.c_int, [vp, C.POINTER(PhysimDirectTuning)]),
         "physim_gpu_sim_plan": (C.c_int, [vp, C.POINTER(PhysimDirectTuning)]),
         "physim_gpu_set_symmetric_cap": (C.c_int, [C.c_uint64]),
+        "physim_gpu_set_symmetric_pairs_limit": (C.c_int, [C.c_uint64]),
         "physim_gpu_set_bus_callback": (C.c_int, [BusFn]),
         "physim_gpu_set_wait_limit": (C.c_int, [u32]),
         "physim_gpu_test_stall_sort": (C.c_int, [i32]),
@@ -255,6 +256,13 @@ def set_symmetric_cap(nbytes: int) -> None:
     """Largest slot buffer the heuristic direct-sum plans give the
     each-pair-once plan (0: a quarter of the device's memory)."""
     check(lib.physim_gpu_set_symmetric_cap(int(nbytes)), "physim_gpu_set_symmetric_cap")
+
+
+def set_symmetric_pairs_limit(nbytes: int) -> None:
+    """Largest slot buffer with which the each-pair-once plan runs one block
+    per tile pair; larger problems use the cluster schedule (0: 1 GiB)."""
+    check(lib.physim_gpu_set_symmetric_pairs_limit(int(nbytes)),
+          "physim_gpu_set_symmetric_pairs_limit")
 
 
 def host_access(device: int = 0) -> str:

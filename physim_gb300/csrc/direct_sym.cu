@@ -21,6 +21,14 @@
 // diagonal tile pair (I, I) evaluates all ordered pairs of the tile and
 // updates a_i only.
 //
+// Two schedules share that core.  With few tiles (one [3][n] f32 slot per
+// tile fits in kSymPairsSlotBytes) every tile pair (I, J), I <= J, is one
+// block (sym_tile_pair in direct_sym_tile.cuh): tile J's contribution to tile
+// I goes to slot J, tile I's to tile J to slot I, and a reduce adds each
+// body's T slots.  That keeps every SM busy at any size and is the faster of
+// the two, but its slots grow as 12 T n bytes (12.9 GB at 1,048,580 bodies),
+// so from that size on the cluster schedule below takes over.
+//
 // Blocks work in thread-block clusters of kSymCluster (8) blocks: a cluster
 // takes the I tiles g*8 .. g*8+7 (one per block) and a run of kSymRun (16) J
 // tiles r*16 .. r*16+15, the pairs with I <= J.  A block's a_i accumulates
@@ -69,6 +77,11 @@ namespace pg {
 namespace cg = cooperative_groups;
 
 namespace {
+
+// The tile-pair schedule while its slot buffer (12 B per body per tile) fits
+// in 1 GiB (up to about 300,000 bodies) or the physim_gpu_set_symmetric_pairs_limit.
+constexpr size_t kSymPairsSlotBytes = size_t(1) << 30;
+std::atomic<uint64_t> g_pairs_limit{0};
 
 constexpr int kSymCluster = 8;  // I tiles per thread-block cluster (a portable size)
 constexpr int kSymRun = 16;     // J tiles per run
@@ -291,6 +304,42 @@ __global__ void sym_reduce_kernel(const float *__restrict__ Pi, const float *__r
     out[idx] = ((double)hi + (double)lo) * pow2d(scale->km - 2 * scale->k);
 }
 
+// The tile-pair schedule: block u takes tile pair (I, J) (unit_tiles).
+__global__ void __launch_bounds__(kSymThreads, 3)
+direct_sym_pairs_kernel(const float4 *__restrict__ body, int n, float e,
+                        const PairScale *__restrict__ scale, float *__restrict__ P)
+{
+    __shared__ float jacc[kSymWarps][kSymTile][3];
+    int I, J;
+    unit_tiles(blockIdx.x, I, J);
+    const int sk = scale->k, skm = scale->km;
+    if (I == J)
+        sym_tile_pair<true>(body, n, I, J, e, sk, skm, P, jacc);
+    else
+        sym_tile_pair<false>(body, n, I, J, e, sk, skm, P, jacc);
+}
+
+// out[idx] = the sum of entry idx of the T slots P[t][3][n], in slot order,
+// TwoSum-compensated, rounded once to f64 and unscaled (x 2^(km - 2k)).
+__global__ void sym_pairs_reduce_kernel(const float *__restrict__ P, long long n3, int T,
+                                        const PairScale *__restrict__ scale,
+                                        double *__restrict__ out)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n3) return;
+    float hi = 0.f, lo = 0.f;
+    const float *p = P + idx;
+#pragma unroll 8
+    for (int t = 0; t < T; ++t) {
+        const float v = __ldcs(p + (size_t)t * n3);
+        float s, err;
+        two_sum(hi, v, s, err);
+        hi = s;
+        lo += err;
+    }
+    out[idx] = ((double)hi + (double)lo) * pow2d(scale->km - 2 * scale->k);
+}
+
 }  // namespace
 
 DirectPlan make_symmetric_plan(int n)
@@ -309,6 +358,10 @@ DirectPlan make_symmetric_plan(int n)
         if (cudaFuncSetAttribute(direct_sym_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             (void)cudaGetLastError();  // a hint only: the kernel runs without it
+        if (cudaFuncSetAttribute(direct_sym_pairs_kernel,
+                                 cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+            (void)cudaGetLastError();
     }
     DirectPlan p;
     p.symmetric = true;
@@ -321,6 +374,9 @@ DirectPlan make_symmetric_plan(int n)
     p.n_itiles = p.tiles;
     p.n_jtiles = p.tiles;
     p.chunk_tiles = p.tiles;
+    const uint64_t limit = g_pairs_limit.load();
+    p.clusters = (size_t)p.tiles * 12 * (size_t)(n > 0 ? n : 1) >
+                 (limit ? (size_t)limit : kSymPairsSlotBytes);
     return p;
 }
 
@@ -339,6 +395,7 @@ size_t direct_partial_doubles(const DirectPlan &p)
     const size_t n3 = 3 * (size_t)(p.n > 0 ? p.n : 1);
     if (!p.symmetric) return (size_t)p.splits * n3;
     // f64 sums, then the f32 slots carved after them
+    if (!p.clusters) return n3 + ((size_t)p.tiles * n3 + 1) / 2;
     return n3 + (sym_slot_floats(p.tiles, nullptr) + 1) / 2;
 }
 
@@ -347,6 +404,22 @@ int launch_direct_symmetric(const DirectPlan &plan, const float4 *body4, float e
                             cudaEvent_t pairs_done)
 {
     if (plan.n <= 0) return PHYSIM_OK;
+    if (!plan.clusters) {
+        const long long T = plan.tiles;
+        const long long units = T * (T + 1) / 2;
+        PG_CHECK(units < (1ll << 31), PHYSIM_ERR_ARGUMENT, "too many bodies for one pass: %d",
+                 plan.n);
+        const long long n3 = 3ll * plan.n;
+        float *P = (float *)(partial + n3);
+        direct_sym_pairs_kernel<<<(unsigned)units, kSymThreads, 0, stream>>>(body4, plan.n, e,
+                                                                            scale, P);
+        PG_CUDA(cudaGetLastError());
+        if (pairs_done) PG_TRY(record_event(pairs_done, stream));
+        sym_pairs_reduce_kernel<<<(unsigned)((n3 + 255) / 256), 256, 0, stream>>>(
+            P, n3, (int)T, scale, partial);
+        PG_CUDA(cudaGetLastError());
+        return PHYSIM_OK;
+    }
     const int T = plan.tiles;
     const long long blocks = sym_clusters(T) * kSymCluster;
     PG_CHECK(blocks < (1ll << 31), PHYSIM_ERR_ARGUMENT, "too many bodies for one pass: %d",
@@ -367,3 +440,9 @@ int launch_direct_symmetric(const DirectPlan &plan, const float4 *body4, float e
 }
 
 }  // namespace pg
+
+extern "C" int physim_gpu_set_symmetric_pairs_limit(uint64_t bytes)
+{
+    pg::g_pairs_limit.store(bytes);
+    return PHYSIM_OK;
+}

@@ -108,10 +108,13 @@ struct DirectPlan {
     int chunk_tiles = 0;   // j tiles per split
     bool compensated = true;
     // Every unordered pair evaluated once (direct_sym.cu): `tiles` body tiles
-    // of 1,024, one block per tile pair; the partial sums come out as one
-    // split, after a f32 slot buffer the same allocation holds.
+    // of 1,024; the partial sums come out as one split, after f32 slot sums
+    // the same allocation holds.  clusters: thread-block clusters over runs of
+    // tiles (3T^2/32 slots of 3 x 1,024 floats); otherwise one block per tile
+    // pair (one [3][n] slot per tile).
     bool symmetric = false;
     int tiles = 0;
+    bool clusters = false;
 };
 
 // Heuristic plan that fills the GPU: picks the i-tile shape and the number of

@@ -1,6 +1,8 @@
 """simple_astro with every unordered pair evaluated once (the symmetric plan)
 against the oracle (astro/src/transformers.rs:219-244) and against the
-one-pair kernels.
+one-pair kernels, under both of its schedules: one block per tile pair (the
+default up to ~300,000 bodies) and thread-block clusters (the default above;
+forced here at every size with physim_gpu_set_symmetric_pairs_limit).
 
 Tolerances: per-body relative error 1e-5 against the f64 oracle (as for the
 one-pair kernels); 2e-6 against the one-pair kernels (both FP32 pair
@@ -14,6 +16,14 @@ import pytest
 from test_direct_gpu import RTOL, _vec, rel_err
 
 pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True, params=["pairs", "clusters"])
+def schedule(request):
+    import physim_gb300 as pg
+    pg.set_symmetric_pairs_limit(1 if request.param == "clusters" else 0)
+    yield request.param
+    pg.set_symmetric_pairs_limit(0)
 
 
 def _sim_acc(state, e, symmetric=True, **plan):
@@ -145,3 +155,19 @@ def test_symmetric_cap_falls_back_to_one_pair_plans(oracle_mod):
         assert rel_err(got[idx][live], ref[live]).max() < RTOL
     keep = ~np.isnan(_vec(sym)).any(axis=1) & (s["fixed"] == 0)
     assert rel_err(one[keep], sym[keep]).max() < 2e-6
+
+
+def test_schedules_agree():
+    """The two schedules on the same state: within FP32 rounding of each other
+    (2e-6 per body), each deterministic."""
+    import physim_gb300 as pg
+    from physim_gb300 import ics
+    s = ics.plummer(30_000, seed=12, a=0.1)
+    out = {}
+    try:
+        for name, limit in (("pairs", 0), ("clusters", 1)):
+            pg.set_symmetric_pairs_limit(limit)
+            out[name] = _sim_acc(s, 1e-3)
+    finally:
+        pg.set_symmetric_pairs_limit(0)
+    assert np.all(rel_err(out["pairs"], out["clusters"]) < 2e-6)
