@@ -1201,6 +1201,8 @@ __global__ void __launch_bounds__(kTravWarps * 32)
 traverse_exact_kernel(TravArgs a_in)
 {
     __shared__ StackEntry stack[kTravWarps][kStack];
+    __shared__ float4 child_geo[kTravWarps][8];  // the children being tested
+    __shared__ int4 child_meta[kTravWarps][8];
     // a failed sort left no tree to walk (the node arrays may hold anything)
     if (sort_failed(a_in.flags)) return;
     TravArgs a = a_in;
@@ -1218,24 +1220,21 @@ traverse_exact_kernel(TravArgs a_in)
     const float4 qs = scaled(q, a.sc, a.msc);
     float ax = 0.f, ay = 0.f, az = 0.f, hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
     int sp = 0;
-    if (lane == 0) stack[warp][0] = {0, active};
-    sp = 1;
     int since_fold = 0;
-    __syncwarp();
-    while (sp > 0) {
-        const StackEntry top = stack[warp][sp - 1];
-        --sp;
-        __syncwarp();
-        const int node = top.node;
-        const bool in = (top.mask >> lane) & 1u;
-        const float4 geo = a.nd.geo[node];
-        const int child = a.nd.child[node];
+    bool overflow = false;
+    // Tests cell `node` (geometry `geo`, record `meta`) for the lanes of
+    // `mask`, each with the reference's own opening rule for its body:
+    // accepted lanes take the cell's monopole (and quadrupole); the lanes that
+    // open a leaf take its bodies here; an internal cell opened by any lane
+    // goes on the stack with those lanes, to have its children tested.
+    auto visit = [&](int node, uint32_t mask, float4 geo, int4 meta) {
+        const bool in = (mask >> lane) & 1u;
         bool acc = false;
         if (in) {
             acc = accept_cell(a, node, geo, q.x, q.y, q.z, k);
             if (acc && a.com_theta > 0.f) acc = com_guard(a, geo, a.nd.com[node], q.x, q.y, q.z);
         }
-        const uint32_t open = top.mask & ~__ballot_sync(0xffffffffu, acc);
+        const uint32_t open = mask & ~__ballot_sync(0xffffffffu, acc);
         ++visits;
         if (acc) {
             const float4 cm = scaled(a.nd.com[node], a.sc, a.msc);
@@ -1246,28 +1245,21 @@ traverse_exact_kernel(TravArgs a_in)
             ++pairs;
         }
         ++since_fold;
-        if (child < 0) {
-            if (open) {
-                const int b = a.nd.begin[node], c = a.nd.count[node];
-                const bool mine = (open >> lane) & 1u;
-                for (int j = b; j < b + c; ++j) {
-                    const float4 bj = scaled(a.sbody[j], a.sc, a.msc);
-                    if (mine) pair_acc(qs.x, qs.y, qs.z, bj, a.es, ax, ay, az);
-                }
-                if (mine) pairs += c;
-                since_fold += c;
+        if (!open) return;
+        if (meta.y < 0) {
+            const int b = meta.z, c = meta.w;
+            const bool mine = (open >> lane) & 1u;
+            for (int j = b; j < b + c; ++j) {
+                const float4 bj = scaled(a.sbody[j], a.sc, a.msc);
+                if (mine) pair_acc(qs.x, qs.y, qs.z, bj, a.es, ax, ay, az);
             }
-        } else if (open) {
-            const int nc = a.nd.nchild[node];
-            if (sp + nc > kStack) {
-                if (lane == 0) atomicOr(&a.flags[kFlagStack], 1u);
-                break;
-            }
-            // push children 0..nc-1 so the last child is popped first, the
-            // reference's pop order (octree.rs:152-154)
-            if (lane < nc) stack[warp][sp + lane] = {child + lane, open};
-            sp += nc;
-            __syncwarp();
+            if (mine) pairs += c;
+            since_fold += c;
+        } else if (sp < kStack) {
+            if (lane == 0) stack[warp][sp] = {node, open};
+            ++sp;
+        } else {
+            overflow = true;
         }
         if (since_fold >= 64) {
             fold(hx, lx, ax);
@@ -1275,7 +1267,27 @@ traverse_exact_kernel(TravArgs a_in)
             fold(hz, lz, az);
             since_fold = 0;
         }
+    };
+    visit(0, active, a.nd.geo[0], a.nd.meta[0]);
+    while (sp > 0 && !overflow) {
+        __syncwarp();
+        const StackEntry top = stack[warp][sp - 1];
+        --sp;
+        __syncwarp();
+        const int4 pm = a.nd.meta[top.node];
+        const int fc = pm.y, nc = (int)((uint32_t)pm.x >> 28);
+        // the children's records, one lane each, loaded together
+        if (lane < nc) {
+            child_geo[warp][lane] = a.nd.geo[fc + lane];
+            child_meta[warp][lane] = a.nd.meta[fc + lane];
+        }
+        __syncwarp();
+        // last child first, as the reference pops them (octree.rs:152-154)
+#pragma unroll 1
+        for (int c = nc - 1; c >= 0; --c)
+            visit(fc + c, top.mask, child_geo[warp][c], child_meta[warp][c]);
     }
+    if (overflow && lane == 0) atomicOr(&a.flags[kFlagStack], 1u);
     fold(hx, lx, ax);
     fold(hy, ly, ay);
     fold(hz, lz, az);
