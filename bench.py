@@ -583,6 +583,31 @@ def measure_bh(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict:
                          "gpu_launches": sim.launches_per_step * steps,
                          "acc_error_vs_f64": err, "clocks": clk}
         sim.close()
+        if not extra:
+            # the same steps as one sim.step(steps) call, as a simulation runs
+            # them: a fresh simulation from the same state, the same warm-up,
+            # one L2 flush before the timed region and none between steps (the
+            # step's working set, ~250 MB at 1M bodies, exceeds the 129 MB L2)
+            sim = pg.Simulation(state, pg.SimConfig(gravity="astro2", theta=theta, e=E, dt=DT,
+                                                    leaf_size=16, traversal="warp",
+                                                    device=device, stream=stream.cuda_stream))
+            with torch.cuda.stream(stream):
+                sim.step(max(args.warmup, 3))
+            sim.synchronize()
+            dist.barrier()
+            e0, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0.record(stream)
+                sim.step(steps)
+                e1.record(stream)
+            torch.cuda.synchronize()
+            b2b = dist.max(e0.elapsed_time(e1))
+            results[name]["back_to_back"] = {
+                "steps_per_s": dist.sum(float(steps)) / (b2b / 1e3), "ms_per_step": b2b / steps,
+                "steps": steps, "path": "one physim_gpu_sim_step(steps) call, CUDA events on the "
+                                        "simulation's stream, no L2 flush between steps"}
+            sim.close()
     main = results["0.5"]
     bytes_step = sum(BH_BYTES_PER_BODY.values()) * n
     hbm = float(peaks.get("hbm_gbs", 6800.0))
