@@ -108,6 +108,9 @@ def parse():
                         "through the plugin on host arrays, per theta")
     p.add_argument("--bh-sample", type=int, default=16384,
                    help="bodies whose accelerations are checked against the f64 reference law")
+    p.add_argument("--sym-pairs-limit", type=int, default=0,
+                   help="slot bytes up to which the each-pair-once plan runs one block per tile "
+                        "pair (0: the library's 1 GiB; 1: thread-block clusters at any size)")
     p.add_argument("--bodies", type=int, default=N_CUBE,
                    help="cube bodies (profiling of smaller cases; the reported workload is "
                         "the default 1,048,576)")
@@ -984,6 +987,9 @@ def measure_tour(args, dist: Dist, device: int) -> dict:
 
 def run_ours(args, dist: Dist):
     device, sms = _device_context(dist)
+    if args.sym_pairs_limit:
+        import physim_gb300 as pg
+        pg.set_symmetric_pairs_limit(args.sym_pairs_limit)
     peaks = measured_peaks()
     parts = (args.only.split(",") if args.only
              else ["direct", "bh", "ensemble", "served", "precision"])
