@@ -626,7 +626,10 @@ def measure_bh(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict:
            "roofline": {"bound": "hbm", "kernel": "whole step", "achieved": achieved,
                         "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
                         "algorithmic_bytes_per_body": BH_BYTES_PER_BODY,
-                        "note": "interaction-list node reads (L2-resident tree) excluded"},
+                        "note": "interaction-list node reads (L2-resident tree) excluded",
+                        "frac_by_theta": {
+                            k: bytes_step / (v["ms_per_step"] / 1e3) / 1e9 / hbm
+                            for k, v in results.items() if "quadrupole" not in k}},
            "traversal_roofline": {"bound": "fp32", "kernel": "traverse_warp_kernel",
                                   "achieved": trav_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
                                   "frac": trav_tflops / fp32_peak if trav_tflops else None,
