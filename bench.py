@@ -433,6 +433,32 @@ def measure_direct(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict
     launches = sim.launches_per_step * args.steps
     sim.close()
 
+    # the other each-pair-once schedule at this size, for the record: one block
+    # per tile pair (faster, but one [3][n] f32 slot per tile: 12.9 GB at 1M
+    # bodies), same state, same steps
+    alt = None
+    if plan.get("symmetric") and args.bodies == N_CUBE and not args.sym_pairs_limit:
+        slot_bytes = 12 * plan["tiles"] * n
+        pg.set_symmetric_pairs_limit(slot_bytes)
+        try:
+            sim = pg.Simulation(state, pg.SimConfig(gravity="simple_astro", e=E, dt=DT,
+                                                    device=device, stream=stream.cuda_stream))
+            sim.set_plan(symmetric=True)
+            sim.set_profiling(True)
+            with torch.cuda.stream(stream):
+                sim.step(args.warmup)
+            sim.synchronize()
+            alt_ms, _, alt_pair = _timed_steps(sim, stream, args.steps, flush, pair=True)
+            sim.close()
+            alt = {"value": dist.sum(float(pairs_step * args.steps)) / (dist.max(sum(alt_ms)) / 1e3)
+                   / 1e9, "unit": "Gpair-interactions/s",
+                   "ms_per_step": dist.max(sum(alt_ms)) / args.steps,
+                   "kernel_ms": statistics.mean(alt_pair), "slot_gb": slot_bytes / 1e9,
+                   "schedule": "one block per pair of 1,024-body tiles, one slot per tile "
+                               "(physim_gpu_set_symmetric_pairs_limit above its slot bytes)"}
+        finally:
+            pg.set_symmetric_pairs_limit(0)
+
     kern_ms = statistics.mean(pair_ms)
     if plan.get("symmetric"):
         # each unordered pair evaluated once: 27 flop (FFMA = 2) per pair
@@ -457,7 +483,7 @@ def measure_direct(args, dist: Dist, device: int, sms: int, peaks: dict) -> dict
             traffic = None
     out = {"value": all_pairs / (total_ms / 1e3) / 1e9, "ms_per_step": total_ms / args.steps,
            "bodies": n, "pairs_per_step": pairs_step, "wall_s": wall, "gpu_launches": launches,
-           "plan": plan,
+           "plan": plan, "tile_pair_schedule": alt,
            "roofline": {"bound": "fp32", "kernel": kernel, "achieved": achieved,
                         "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                         "traffic": traffic, "traffic_source": traffic_source,
@@ -1037,7 +1063,8 @@ def run_ours(args, dist: Dist):
         line["config"] = bench_config(args.bodies, args.gpus)
         line["pair_kernel_plan"] = direct["plan"]
         line["compensated_sums"] = True
-        for k in ("roofline", "e2e", "gpu_launches", "cpu_baseline", "clocks"):
+        for k in ("roofline", "e2e", "gpu_launches", "cpu_baseline", "clocks",
+                  "tile_pair_schedule"):
             if k in direct:
                 line[k] = direct[k]
     if served:
