@@ -1,8 +1,8 @@
 """CPU oracle for physim's gravity + integration hot path -- TEST INFRASTRUCTURE.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
-package, and only as the checker (or the timed CPU baseline).  The shipped
-library never loads it.
+package: as the reference the CUDA results are compared with, or as the timed
+CPU baseline.  The shipped library never loads it.
 
 `physim_oracle.c` restates the reference's Rust algorithms in C (f64, same
 operation order); see its header for the file:line of each function and for

@@ -2,7 +2,7 @@
  * physim_oracle.c -- CPU restatement of physim's gravity + integration hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the shipped library links, loads or
- * calls this file.  It is the checker that the CUDA path is compared against
+ * calls this file.  It is what the CUDA path's results are compared against
  * (tests/, __graft_entry__.smoke(), and bench.py's CPU-baseline leg).
  *
  * Every function restates the reference algorithm in plain C with f64
