@@ -966,6 +966,15 @@ def measure_tour(args, dist: Dist, device: int) -> dict:
         sim.accelerations_f64(np.arange(64))
         sim.download()
     paths.append("simple_astro 65,536 each pair once + verlet, diagnostics, f64 sample")
+    # the same sum in thread-block clusters (the schedule of large states)
+    pg.set_symmetric_pairs_limit(1)
+    try:
+        with pg.Simulation(cube, pg.SimConfig(gravity="simple_astro", e=E, dt=DT,
+                                              device=device)) as sim:
+            sim.step(2)
+    finally:
+        pg.set_symmetric_pairs_limit(0)
+    paths.append("simple_astro 65,536 each pair once in thread-block clusters")
     for integ in ("euler", "rk4"):
         with pg.Simulation(small, pg.SimConfig(gravity="simple_astro", e=E, dt=DT,
                                                integrator=integ, device=device)) as sim:
