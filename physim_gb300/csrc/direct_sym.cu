@@ -27,7 +27,8 @@
 // I goes to slot J, tile I's to tile J to slot I, and a reduce adds each
 // body's T slots.  That keeps every SM busy at any size and is the faster of
 // the two, but its slots grow as 12 T n bytes (12.9 GB at 1,048,580 bodies),
-// so from that size on the cluster schedule below takes over.
+// so once they would exceed kSymPairsSlotBytes (1 GiB, about 300,000 bodies)
+// the cluster schedule below takes over.
 //
 // Blocks work in thread-block clusters of kSymCluster (8) blocks: a cluster
 // takes the I tiles g*8 .. g*8+7 (one per block) and a run of kSymRun (16) J
@@ -52,7 +53,7 @@
 // block of a cluster takes the same arrivals and waits (its run's length
 // plus one), and a last arrive-and-wait keeps each block's shared memory
 // alive until the others have read it.
-// Output.  Tile K has Rn - floor(K / 16) i-side slots (the runs r whose last
+// Cluster schedule output.  Tile K has Rn - floor(K / 16) i-side slots (the runs r whose last
 // J tile is >= K) and floor(K / 8) + 1 j-side slots (the groups g with
 // 8 g <= K), each [3][1024] f32, packed tile after tile (offsets in closed
 // form, sym_iside_base / sym_jside_base): 1.2 GB at 1,048,580 bodies,
