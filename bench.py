@@ -1023,14 +1023,25 @@ def measure_tour(args, dist: Dist, device: int) -> dict:
     return {"metric": "kernel tour", "value": len(paths), "unit": "paths", "paths": paths}
 
 
+def bench_parts(only: str, world: int) -> list[str]:
+    """The parts a run measures: --only's list, else every part on one GPU and,
+    under torchrun (replicas), the headline direct sum and Barnes-Hut only -- the
+    ensemble, the served mix and the precision study are single-GPU studies,
+    measured in the N = 1 run."""
+    if only:
+        return only.split(",")
+    if world == 1:
+        return ["direct", "bh", "ensemble", "served", "precision"]
+    return ["direct", "bh"]
+
+
 def run_ours(args, dist: Dist):
     device, sms = _device_context(dist)
     if args.sym_pairs_limit:
         import physim_gb300 as pg
         pg.set_symmetric_pairs_limit(args.sym_pairs_limit)
     peaks = measured_peaks()
-    parts = (args.only.split(",") if args.only
-             else ["direct", "bh", "ensemble", "served", "precision"])
+    parts = bench_parts(args.only, dist.world)
     direct = measure_direct(args, dist, device, sms, peaks) if "direct" in parts else None
     bh = measure_bh(args, dist, device, sms, peaks) if "bh" in parts else None
     ens = measure_ensemble(args, dist, device) if "ensemble" in parts else None

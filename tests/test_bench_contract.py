@@ -63,3 +63,11 @@ def test_parser_defaults(monkeypatch):
     assert a.serve_queue_ms == 0.0  # every idle unit ticked at once
     assert a.serve_seconds == 120.0  # the configured 120 s of arrivals
     assert a.bh_sample == 16384 and a.bh_steps == 1000
+
+
+def test_parts_by_world_size():
+    sys.path.insert(0, str(ROOT))
+    import bench
+    assert bench.bench_parts("", 1) == ["direct", "bh", "ensemble", "served", "precision"]
+    assert bench.bench_parts("", 8) == ["direct", "bh"]
+    assert bench.bench_parts("served", 4) == ["served"]
