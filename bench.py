@@ -110,7 +110,7 @@ def parse():
                    help="bodies whose accelerations are checked against the f64 reference law")
     p.add_argument("--sym-pairs-limit", type=int, default=0,
                    help="slot bytes up to which the each-pair-once plan runs one block per tile "
-                        "pair (0: the library's 1 GiB; 1: thread-block clusters at any size)")
+                        "pair (0: the library's 4 GiB; 1: thread-block clusters at any size)")
     p.add_argument("--bodies", type=int, default=N_CUBE,
                    help="cube bodies (profiling of smaller cases; the reported workload is "
                         "the default 1,048,576)")

@@ -382,7 +382,7 @@ int physim_gpu_sim_set_plan(PhysimSim *sim, const PhysimDirectTuning *plan);
 int physim_gpu_set_symmetric_cap(uint64_t bytes);
 /* The each-pair-once plan runs one block per pair of 1,024-body tiles while
  * that schedule's slot buffer (12 bytes per body per tile) is at most `bytes`
- * (0 restores the default, 1 GiB: up to about 300,000 bodies), and in
+ * (0 restores the default, 4 GiB: up to about 600,000 bodies), and in
  * thread-block clusters over runs of tiles above that (slot sums 3T^2/32 x
  * 12 KB for T tiles: 1.2 GB instead of 12.9 GB at 1,048,580 bodies).  Both
  * give the same results within FP32 rounding.  Process-wide, read when a plan

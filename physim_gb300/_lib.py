@@ -260,7 +260,7 @@ def set_symmetric_cap(nbytes: int) -> None:
 
 def set_symmetric_pairs_limit(nbytes: int) -> None:
     """Largest slot buffer with which the each-pair-once plan runs one block
-    per tile pair; larger problems use the cluster schedule (0: 1 GiB)."""
+    per tile pair; larger problems use the cluster schedule (0: 4 GiB)."""
     check(lib.physim_gpu_set_symmetric_pairs_limit(int(nbytes)),
           "physim_gpu_set_symmetric_pairs_limit")
 

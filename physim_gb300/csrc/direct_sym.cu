@@ -27,7 +27,7 @@
 // I goes to slot J, tile I's to tile J to slot I, and a reduce adds each
 // body's T slots.  That keeps every SM busy at any size and is the faster of
 // the two, but its slots grow as 12 T n bytes (12.9 GB at 1,048,580 bodies),
-// so once they would exceed kSymPairsSlotBytes (1 GiB, about 300,000 bodies)
+// so once they would exceed kSymPairsSlotBytes (4 GiB, about 600,000 bodies)
 // the cluster schedule below takes over.
 //
 // Blocks work in thread-block clusters of kSymCluster (8) blocks: a cluster
@@ -80,8 +80,8 @@ namespace cg = cooperative_groups;
 namespace {
 
 // The tile-pair schedule while its slot buffer (12 B per body per tile) fits
-// in 1 GiB (up to about 300,000 bodies) or the physim_gpu_set_symmetric_pairs_limit.
-constexpr size_t kSymPairsSlotBytes = size_t(1) << 30;
+// in 4 GiB (up to about 600,000 bodies) or the physim_gpu_set_symmetric_pairs_limit.
+constexpr size_t kSymPairsSlotBytes = size_t(4) << 30;
 std::atomic<uint64_t> g_pairs_limit{0};
 
 constexpr int kSymCluster = 8;  // I tiles per thread-block cluster (a portable size)

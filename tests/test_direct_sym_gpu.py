@@ -1,7 +1,7 @@
 """simple_astro with every unordered pair evaluated once (the symmetric plan)
 against the oracle (astro/src/transformers.rs:219-244) and against the
 one-pair kernels, under both of its schedules: one block per tile pair (the
-default up to ~300,000 bodies) and thread-block clusters (the default above;
+default up to ~600,000 bodies) and thread-block clusters (the default above;
 forced here at every size with physim_gpu_set_symmetric_pairs_limit).
 
 Tolerances: per-body relative error 1e-5 against the f64 oracle (as for the
