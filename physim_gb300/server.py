@@ -160,6 +160,7 @@ class Unit:
     tick_steps: int = 0  # job-steps enqueued by the last launch_tick
     tick_seconds: float = 0.0  # estimated device seconds of the last launched tick
     in_flight: bool = False  # a launched tick has not completed yet
+    last_tick: int = -1  # order of its last tick ("all" with a queue cap: least recent first)
 
     def remaining_seconds(self) -> float:
         """Estimated device seconds of the unit's unfinished steps (used to
@@ -639,7 +640,7 @@ class Server:
                 self._launch(u)
         elif self.scheduling == "all":
             inflight = sum(u.tick_seconds for u in self.units if u.in_flight)
-            for u in sorted(idle, key=lambda v: getattr(v, "last_tick", -1)):
+            for u in sorted(idle, key=lambda v: v.last_tick):
                 if inflight >= self.queue_seconds:
                     break
                 if self._launch(u):
