@@ -990,6 +990,16 @@ def measure_tour(args, dist: Dist, device: int) -> dict:
         with pg.Simulation(big, pg.SimConfig(e=E, dt=DT, device=device, **cfg)) as sim:
             sim.step(2)
         paths.append(" ".join(f"{k}={v}" for k, v in cfg.items()))
+    # the radix sort as one launch per pass (the form without cooperative launches)
+    pg.lib.physim_gpu_set_sort_single_launch(0)
+    try:
+        with pg.Simulation(big, pg.SimConfig(gravity="astro2", theta=0.5, leaf_size=16,
+                                             traversal="warp", e=E, dt=DT,
+                                             device=device)) as sim:
+            sim.step(1)
+    finally:
+        pg.lib.physim_gpu_set_sort_single_launch(1)
+    paths.append("astro2 with the radix sort as one launch per pass")
     # host arrays: the plugin transform + verlet, in place and with copies
     try:
         for mode in ("direct", "copy"):

@@ -398,6 +398,14 @@ int physim_gpu_set_symmetric_pairs_limit(uint64_t bytes);
  * captured.  No reference counterpart (the reference builds its tree on one
  * CPU thread, octree.rs:27-128). */
 int physim_gpu_set_wait_limit(uint32_t polls);
+/* How the Barnes-Hut build runs its 7-pass radix sort: `on` != 0 (default)
+ * runs every pass in one cooperative launch where the device supports
+ * cooperative launches (a grid barrier between passes, bounded by the wait
+ * limit above), 0 runs one launch per pass.  The sorted order, and so every
+ * result, is the same either way.  Process-wide, read when a build is enqueued
+ * or captured.  No reference counterpart (octree.rs:27-128 sorts on one CPU
+ * thread). */
+int physim_gpu_set_sort_single_launch(int32_t on);
 /* Test hook for the path above: tile `tile` (>= 0; -1 turns it off) of each
  * radix pass sees no predecessor word, so its wait always runs out.
  * Process-wide, read when a build is enqueued or captured. */

@@ -157,6 +157,7 @@ def _load() -> C.CDLL:
         "physim_gpu_set_bus_callback": (C.c_int, [BusFn]),
         "physim_gpu_set_wait_limit": (C.c_int, [u32]),
         "physim_gpu_test_stall_sort": (C.c_int, [i32]),
+        "physim_gpu_set_sort_single_launch": (C.c_int, [i32]),
         "physim_gpu_energy_create": (C.c_int, [i32, C.POINTER(vp)]),
         "physim_gpu_energy_compute": (C.c_int, [vp, vp, sz, dbl, C.c_int,
                                                 C.POINTER(PhysimDiagnostics)]),

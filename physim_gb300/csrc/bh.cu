@@ -183,14 +183,16 @@ __device__ __forceinline__ uint64_t spread2(uint32_t v)
 
 // Keys, plus the histograms of all 7 radix digits of all keys (block-local in
 // shared memory, then one global atomic per non-empty bucket), for the
-// one-sweep sort.  ghist [8][256] must be zero on entry.  Block 0 also resets
-// the sort's tile counters and advances its epoch (see radix_pass_kernel).
+// one-sweep sort.  ghist [7][512] must be zero on entry.  Block 0 also resets
+// the sort's tile counters and grid barrier and advances its epoch (see
+// radix_pass_kernel).
 __global__ void __launch_bounds__(256)
 keys_kernel(const double *__restrict__ x, const double *__restrict__ y,
             const double *__restrict__ z, int n, int nchild,
             const unsigned long long *__restrict__ extent_bits, uint64_t *__restrict__ keys,
             uint32_t *__restrict__ vals, uint32_t *__restrict__ ghist,
-            uint32_t *__restrict__ tile_ctr, uint32_t *__restrict__ epoch)
+            uint32_t *__restrict__ tile_ctr, uint32_t *__restrict__ epoch,
+            uint32_t *__restrict__ sort_bar)
 {
     __shared__ double s_scale;
     __shared__ uint32_t h[kSortPasses][kRadixBuckets];
@@ -200,6 +202,7 @@ keys_kernel(const double *__restrict__ x, const double *__restrict__ y,
     if (threadIdx.x == 0) s_scale = X > 0.0 ? __ddiv_rn(ldexp(1.0, D - 1), X) : 0.0;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         for (int p = 0; p < kSortPasses; ++p) tile_ctr[p] = 0;
+        *sort_bar = 0;
         *epoch += 1u;
     }
     __syncthreads();
@@ -269,55 +272,24 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *w
     return r;
 }
 
-// One stable counting pass of the one-sweep LSD radix sort (single-pass
-// chained scan with decoupled look-back, after Merrill & Garland 2016 and
-// Adinets & Merrill 2022).  Tiles of kSortTile keys are claimed in launch
-// order from an atomic counter, so every tile a block looks back at is held
-// by a block that is already running.  Each block ranks its keys by digit
-// (warp by warp, stable, lanes of equal digit found by one ballot per digit
-// bit), publishes its per-digit counts, then walks back over the preceding
-// tiles' published words until it meets an inclusive prefix, publishes its
-// own inclusive prefix, and scatters: the tile is first put in digit order
-// in shared memory, so each digit's keys leave in one contiguous run.  A status word is
-// (epoch * 4 + flag) << 32 | count, flag 1 = tile count, 2 = inclusive
-// prefix, and epoch counts (sort, pass) pairs; words of earlier passes and
-// sorts carry older epochs and read as not ready, so the status array needs
-// no clearing.  A wait that exceeds
-// the wait limit (kLookbackSpins unless physim_gpu_set_wait_limit set one)
-// sets flags[kFlagSort] and gives up: the tile still scatters, at positions no
-// higher than the right ones (its prefix is a partial sum), so every write
-// stays in bounds; every later kernel of the build and the traversal see the
-// flag and return at once, so nothing reads the invalid order or an unbuilt
-// tree, and the host reports PHYSIM_ERR_TIMEOUT.  stall_tile >= 0
-// (physim_gpu_test_stall_sort) makes that tile's look-back see no
-// predecessor word, so the limit is reached for sure.
-__global__ void __launch_bounds__(kSortThreads)
-radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
-                  uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int n,
-                  int pass, const uint32_t *__restrict__ ghist, uint32_t *__restrict__ tile_ctr,
-                  unsigned long long *__restrict__ status, const uint32_t *__restrict__ epoch_ptr,
-                  uint32_t *__restrict__ flags, int spin_limit, int stall_tile)
+// One tile of one pass of the radix sort (the body shared by the per-pass
+// kernel and the single-launch sort): ranks the tile's keys by digit,
+// publishes and looks back, and scatters through shared memory.  digit_base
+// is this thread's digit's first place in the output (the scan of the
+// pass's global histogram); h must be zero on entry.  The key and value
+// pointers carry no __restrict__: in the single-launch sort a pass reads what
+// other blocks of the same launch wrote, which the read-only cache path may
+// not serve.
+__device__ __forceinline__ void sort_tile(
+    const uint64_t *keys_in, const uint32_t *vals_in, uint64_t *keys_out, uint32_t *vals_out,
+    int n, int pass, int tile,
+    uint32_t digit_base, unsigned long long *__restrict__ status,
+    const uint32_t *__restrict__ epoch_ptr, uint32_t *__restrict__ flags, int spin_limit,
+    int stall_tile, uint32_t (*h)[kRadixBuckets], uint32_t *digit_off, uint32_t *local_start,
+    uint32_t *ws)
 {
-    static_assert(kSortThreads >= kRadixBuckets, "one thread per digit");
-    if (*(volatile const uint32_t *)&flags[kFlagSort] != 0u) return;  // an earlier wait failed
-    __shared__ uint32_t h[kSortWarps][kRadixBuckets];
-    __shared__ uint32_t digit_off[kRadixBuckets];
-    __shared__ uint32_t local_start[kRadixBuckets];  // the digit's first key in the staged tile
-    __shared__ uint32_t ws[33];
-    __shared__ int s_tile;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int shift = kRadixBits * pass;
-    if (threadIdx.x == 0) s_tile = (int)atomicAdd(&tile_ctr[pass], 1u);
-    for (int k = threadIdx.x; k < kSortWarps * kRadixBuckets; k += kSortThreads)
-        (&h[0][0])[k] = 0;
-    uint32_t digit_base;
-    {
-        uint32_t total;
-        const uint32_t c = threadIdx.x < kRadixBuckets ? ghist[pass * kRadixBuckets + threadIdx.x]
-                                                       : 0u;
-        digit_base = block_exclusive_scan(c, ws, total);
-    }
-    const int tile = s_tile;
     const int base = tile * kSortTile + warp * (kSortItems * 32);
     uint64_t kk[kSortItems];
     uint32_t vv[kSortItems];
@@ -433,6 +405,134 @@ radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restri
         const uint32_t pos = digit_off[dg] + (uint32_t)j - local_start[dg];
         keys_out[pos] = key;
         vals_out[pos] = svals[j];
+    }
+}
+
+// One stable counting pass of the one-sweep LSD radix sort (single-pass
+// chained scan with decoupled look-back, after Merrill & Garland 2016 and
+// Adinets & Merrill 2022).  Tiles of kSortTile keys are claimed in launch
+// order from an atomic counter, so every tile a block looks back at is held
+// by a block that is already running.  Each block ranks its keys by digit
+// (warp by warp, stable, lanes of equal digit found by one ballot per digit
+// bit), publishes its per-digit counts, then walks back over the preceding
+// tiles' published words until it meets an inclusive prefix, publishes its
+// own inclusive prefix, and scatters: the tile is first put in digit order
+// in shared memory, so each digit's keys leave in one contiguous run.  A status word is
+// (epoch * 4 + flag) << 32 | count, flag 1 = tile count, 2 = inclusive
+// prefix, and epoch counts (sort, pass) pairs; words of earlier passes and
+// sorts carry older epochs and read as not ready, so the status array needs
+// no clearing.  A wait that exceeds
+// the wait limit (kLookbackSpins unless physim_gpu_set_wait_limit set one)
+// sets flags[kFlagSort] and gives up: the tile still scatters, at positions no
+// higher than the right ones (its prefix is a partial sum), so every write
+// stays in bounds; every later kernel of the build and the traversal see the
+// flag and return at once, so nothing reads the invalid order or an unbuilt
+// tree, and the host reports PHYSIM_ERR_TIMEOUT.  stall_tile >= 0
+// (physim_gpu_test_stall_sort) makes that tile's look-back see no
+// predecessor word, so the limit is reached for sure.
+__global__ void __launch_bounds__(kSortThreads)
+radix_pass_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
+                  uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int n,
+                  int pass, const uint32_t *__restrict__ ghist, uint32_t *__restrict__ tile_ctr,
+                  unsigned long long *__restrict__ status, const uint32_t *__restrict__ epoch_ptr,
+                  uint32_t *__restrict__ flags, int spin_limit, int stall_tile)
+{
+    static_assert(kSortThreads >= kRadixBuckets, "one thread per digit");
+    __shared__ uint32_t h[kSortWarps][kRadixBuckets];
+    __shared__ uint32_t digit_off[kRadixBuckets];
+    __shared__ uint32_t local_start[kRadixBuckets];  // the digit's first key in the staged tile
+    __shared__ uint32_t ws[33];
+    __shared__ int s_tile, s_stop;
+    // an earlier wait failed: the whole block leaves (one read, shared, since
+    // another block of this launch may raise the flag meanwhile)
+    if (threadIdx.x == 0) {
+        s_stop = *(volatile const uint32_t *)&flags[kFlagSort] != 0u;
+        s_tile = (int)atomicAdd(&tile_ctr[pass], 1u);
+    }
+    __syncthreads();
+    if (s_stop) return;
+    for (int k = threadIdx.x; k < kSortWarps * kRadixBuckets; k += kSortThreads)
+        (&h[0][0])[k] = 0;
+    uint32_t digit_base;
+    {
+        uint32_t total;
+        const uint32_t c = threadIdx.x < kRadixBuckets ? ghist[pass * kRadixBuckets + threadIdx.x]
+                                                       : 0u;
+        digit_base = block_exclusive_scan(c, ws, total);
+    }
+    sort_tile(keys_in, vals_in, keys_out, vals_out, n, pass, s_tile, digit_base, status,
+              epoch_ptr, flags, spin_limit, stall_tile, h, digit_off, local_start, ws);
+}
+
+// All seven passes in one cooperative launch (every block resident, up to
+// one per SM): each block takes tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+// of every pass, and a grid barrier separates the passes (a pass reads keys
+// that every tile of the previous one wrote).  Every tile a look-back waits on
+// is lower-numbered, so it is held by a resident block that reaches it after
+// lower tiles only: the waits end.  The barrier is a counter each block adds
+// to once per pass (reset by keys_kernel); its wait gives up after the wait
+// limit, or at once when the sort's error flag is up, raising the flag, so no
+// block waits for one that has left.  Against one launch per pass this saves
+// six launch gaps and the tail of each pass.
+__device__ __forceinline__ bool sort_grid_barrier(uint32_t *bar, uint32_t target,
+                                                  uint32_t *flags, int spin_limit, int *s_ok)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(bar, 1u);
+        int spins = 0;
+        while (*(volatile uint32_t *)bar < target) {
+            if (*(volatile uint32_t *)&flags[kFlagSort] != 0u) break;
+            if (++spins > spin_limit) {
+                atomicOr(&flags[kFlagSort], 1u);
+                break;
+            }
+        }
+        __threadfence();
+        *s_ok = *(volatile uint32_t *)&flags[kFlagSort] == 0u;
+    }
+    __syncthreads();
+    return *s_ok != 0;
+}
+
+__global__ void __launch_bounds__(kSortThreads, 1)
+radix_sort_kernel(uint64_t *k0, uint32_t *v0, uint64_t *k1, uint32_t *v1, int n,
+                  const uint32_t *__restrict__ ghist, unsigned long long *__restrict__ status,
+                  const uint32_t *__restrict__ epoch_ptr, uint32_t *__restrict__ flags,
+                  int spin_limit, int stall_tile, uint32_t *bar)
+{
+    static_assert(kSortThreads == kRadixBuckets, "one thread per digit");
+    __shared__ uint32_t h[kSortWarps][kRadixBuckets];
+    __shared__ uint32_t digit_off[kRadixBuckets];
+    __shared__ uint32_t local_start[kRadixBuckets];
+    __shared__ uint32_t ws[33];
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) s_ok = *(volatile const uint32_t *)&flags[kFlagSort] == 0u;
+    __syncthreads();
+    if (!s_ok) return;
+    const int tiles = (n + kSortTile - 1) / kSortTile;
+    for (int pass = 0; pass < kSortPasses; ++pass) {
+        const uint64_t *keys_in = (pass & 1) ? k1 : k0;
+        const uint32_t *vals_in = pass == 0 ? nullptr : ((pass & 1) ? v1 : v0);
+        uint64_t *keys_out = (pass & 1) ? k0 : k1;
+        uint32_t *vals_out = (pass & 1) ? v0 : v1;
+        uint32_t digit_base;
+        {
+            uint32_t total;
+            digit_base = block_exclusive_scan(ghist[pass * kRadixBuckets + threadIdx.x], ws, total);
+        }
+        for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+            for (int k = threadIdx.x; k < kSortWarps * kRadixBuckets; k += kSortThreads)
+                (&h[0][0])[k] = 0;
+            __syncthreads();
+            sort_tile(keys_in, vals_in, keys_out, vals_out, n, pass, tile, digit_base, status,
+                      epoch_ptr, flags, spin_limit, stall_tile, h, digit_off, local_start, ws);
+            __syncthreads();  // the staged tile, h and the offsets serve the next tile
+        }
+        if (pass + 1 < kSortPasses &&
+            !sort_grid_barrier(bar, (uint32_t)(pass + 1) * gridDim.x, flags, spin_limit, &s_ok))
+            return;
     }
 }
 
@@ -1596,6 +1696,13 @@ inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
 // ---------------------------------------------------------------------------
 // workspace + host driver
 // ---------------------------------------------------------------------------
+namespace {
+// per device: the sort's kernel attributes are set, and how many blocks of the
+// single-launch sort an SM holds (0 = one launch per pass)
+std::atomic<bool> g_sort_ready[64];
+std::atomic<int> g_sort_coop_per_sm[64];
+}  // namespace
+
 struct BhWorkspace {
     int device = 0;
     cudaStream_t stream = nullptr;  // allocations and frees are ordered on it
@@ -1603,7 +1710,8 @@ struct BhWorkspace {
     uint64_t *keys[2] = {nullptr, nullptr};
     uint32_t *vals[2] = {nullptr, nullptr};
     // sort_meta: digit histograms of the passes, then the passes' tile
-    // counters, then the epoch; sort_status: look-back words, tiles x digits
+    // counters, the epoch and the single-launch sort's grid barrier;
+    // sort_status: look-back words, tiles x digits
     uint32_t *sort_meta = nullptr;
     unsigned long long *sort_status = nullptr;
     float4 *sbody = nullptr;
@@ -1655,13 +1763,21 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf, cudaStream_t st
         delete ws;
         ws = nullptr;
     }
-    // the radix pass stages its tile in 96 KB of dynamic shared memory; set
-    // once per device, here (never inside a stream capture)
-    static std::atomic<bool> sort_smem_set[64];
-    if (device >= 0 && device < 64 && !sort_smem_set[device].load()) {
+    // the radix sort stages its tile in 96 KB of dynamic shared memory; set
+    // once per device, here (never inside a stream capture), with the number
+    // of single-launch sort blocks an SM holds (0: no cooperative launch)
+    if (device >= 0 && device < 64 && !g_sort_ready[device].load()) {
         PG_CUDA(cudaFuncSetAttribute(radix_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)kSortSmem));
-        sort_smem_set[device].store(true);
+        PG_CUDA(cudaFuncSetAttribute(radix_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kSortSmem));
+        int coop = 0, per_sm = 0;
+        PG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device));
+        if (coop)
+            PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, radix_sort_kernel,
+                                                                  kSortThreads, kSortSmem));
+        g_sort_coop_per_sm[device].store(per_sm);
+        g_sort_ready[device].store(true);
     }
     BhWorkspace *w = new (std::nothrow) BhWorkspace();
     PG_CHECK(w, PHYSIM_ERR_MEMORY, "out of host memory");
@@ -1683,7 +1799,7 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf, cudaStream_t st
     PG_WA(w->keys[1], cap);
     PG_WA(w->vals[0], cap);
     PG_WA(w->vals[1], cap);
-    PG_WA(w->sort_meta, (size_t)kSortPasses * kRadixBuckets + kSortPasses + 1);
+    PG_WA(w->sort_meta, (size_t)kSortPasses * kRadixBuckets + kSortPasses + 2);
     PG_WA(w->sort_status, (size_t)kRadixBuckets * tiles);
     PG_WA(w->sbody, cap);
     PG_WA(w->lcp, cap);
@@ -1718,7 +1834,7 @@ int bh_reserve(BhWorkspace *&ws, size_t n, int device, int leaf, cudaStream_t st
          cudaMemsetAsync(w->nd.arrivals, 0, ncap * sizeof(uint32_t), stream) != cudaSuccess ||
          cudaMemsetAsync(w->lv, 0, sizeof(LevelInfo), stream) != cudaSuccess ||
          cudaMemsetAsync(w->sort_meta, 0,
-                         ((size_t)kSortPasses * kRadixBuckets + kSortPasses + 1) * sizeof(uint32_t),
+                         ((size_t)kSortPasses * kRadixBuckets + kSortPasses + 2) * sizeof(uint32_t),
                          stream) != cudaSuccess ||
          cudaMemsetAsync(w->sort_status, 0,
                          (size_t)kRadixBuckets * tiles * sizeof(unsigned long long),
@@ -1773,7 +1889,8 @@ int bh_check(BhWorkspace *ws, cudaStream_t st)
     PG_CUDA(cudaMemsetAsync(ws->flags + kFlagStack, 0, 2 * sizeof(uint32_t), st));
     PG_CUDA(cudaStreamSynchronize(st));
     if (f[kFlagSort]) {
-        set_error("Barnes-Hut build: a look-back wait (radix sort or tree level) gave up; "
+        set_error("Barnes-Hut build: a bounded wait (radix sort look-back or pass barrier, "
+                  "or tree level) gave up; "
                   "results are invalid");
         return PHYSIM_ERR_TIMEOUT;
     }
@@ -1795,6 +1912,7 @@ int bh_stats(BhWorkspace *ws, cudaStream_t st, uint64_t out[2])
 namespace {
 std::atomic<uint32_t> g_wait_limit{0};  // 0: kLookbackSpins
 std::atomic<int32_t> g_stall_tile{-1};
+std::atomic<int> g_sort_single{1};
 int wait_limit()
 {
     const uint32_t v = g_wait_limit.load();
@@ -1812,21 +1930,43 @@ static int bh_build(BhWorkspace *ws, const DeviceBodies &b, const BhParams &p, c
     uint32_t *ghist = ws->sort_meta;
     uint32_t *tile_ctr = ws->sort_meta + kSortPasses * kRadixBuckets;
     uint32_t *epoch = tile_ctr + kSortPasses;
+    uint32_t *sort_bar = epoch + 1;
     PG_CUDA(cudaMemsetAsync(ghist, 0, kSortPasses * kRadixBuckets * sizeof(uint32_t), st));
     keys_kernel<<<std::min(cdiv(n, 256), sms * 8), 256, 0, st>>>(
         b.x, b.y, b.z, n, p.nchild, ws->extent_bits, ws->keys[0], ws->vals[0], ghist, tile_ctr,
-        epoch);
+        epoch, sort_bar);
     launches += 2;
-    // one-sweep radix sort: one launch per 9-bit digit
+    // one-sweep radix sort over 9-bit digits: all passes in one cooperative
+    // launch where the device allows it, else one launch per pass
     const int tiles = cdiv(n, kSortTile);
+    const int per_sm = ws->device >= 0 && ws->device < 64 ? g_sort_coop_per_sm[ws->device].load() : 0;
     int cur = 0;
-    for (int pass = 0; pass < kSortPasses; ++pass) {
-        radix_pass_kernel<<<tiles, kSortThreads, kSortSmem, st>>>(
-            ws->keys[cur], pass == 0 ? nullptr : ws->vals[cur], ws->keys[cur ^ 1],
-            ws->vals[cur ^ 1], n, pass, ghist, tile_ctr, ws->sort_status, epoch, ws->flags,
-            wait_limit(), g_stall_tile.load());
-        cur ^= 1;
+    if (g_sort_single.load() && per_sm > 0) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)std::min(tiles, per_sm * sms));
+        cfg.blockDim = dim3(kSortThreads);
+        cfg.dynamicSmemBytes = kSortSmem;
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        PG_CUDA(cudaLaunchKernelEx(&cfg, radix_sort_kernel, ws->keys[0], ws->vals[0], ws->keys[1],
+                                   ws->vals[1], n, (const uint32_t *)ghist, ws->sort_status,
+                                   (const uint32_t *)epoch, ws->flags, wait_limit(),
+                                   (int)g_stall_tile.load(), sort_bar));
+        cur = kSortPasses & 1;
         launches += 1;
+    } else {
+        for (int pass = 0; pass < kSortPasses; ++pass) {
+            radix_pass_kernel<<<tiles, kSortThreads, kSortSmem, st>>>(
+                ws->keys[cur], pass == 0 ? nullptr : ws->vals[cur], ws->keys[cur ^ 1],
+                ws->vals[cur ^ 1], n, pass, ghist, tile_ctr, ws->sort_status, epoch, ws->flags,
+                wait_limit(), g_stall_tile.load());
+            cur ^= 1;
+            launches += 1;
+        }
     }
     ws->sorted = cur;
     // the tree: boundaries (+ sorted f32 bodies), level masks, one scan, node
@@ -1955,6 +2095,12 @@ int bh_snapshot(BhWorkspace *ws, size_t n, cudaStream_t st, PhysimTreeSnapshot *
 extern "C" int physim_gpu_set_wait_limit(uint32_t polls)
 {
     pg::g_wait_limit.store(polls);
+    return PHYSIM_OK;
+}
+
+extern "C" int physim_gpu_set_sort_single_launch(int32_t on)
+{
+    pg::g_sort_single.store(on ? 1 : 0);
     return PHYSIM_OK;
 }
 

@@ -191,16 +191,18 @@ def test_host_access_setting():
 
 
 def test_process_wide_plan_knobs_need_no_device():
-    """The each-pair-once knobs (slot cap, tile-pair schedule bound) and the
-    radix look-back limit only store a value: callable without a GPU, 0
-    restores each default."""
+    """The each-pair-once knobs (slot cap, tile-pair schedule bound), the
+    radix look-back limit and the sort's launch mode only store a value:
+    callable without a GPU; 0 restores each default (1 for the sort mode)."""
     import physim_gb300 as pg
     from physim_gb300 import lib
     try:
         pg.set_symmetric_cap(1 << 30)
         pg.set_symmetric_pairs_limit(1)
         assert lib.physim_gpu_set_wait_limit(1000) == 0
+        assert lib.physim_gpu_set_sort_single_launch(0) == 0
     finally:
         pg.set_symmetric_cap(0)
         pg.set_symmetric_pairs_limit(0)
         assert lib.physim_gpu_set_wait_limit(0) == 0
+        assert lib.physim_gpu_set_sort_single_launch(1) == 0

@@ -220,10 +220,47 @@ def test_full_size_workload(oracle_mod, theta):
     assert e_gpu <= 1.05 * e_ref + 1e-6, (e_gpu, e_ref)
 
 
-def test_bounded_sort_wait_reports_timeout(oracle_mod):
-    """The radix sort's look-back waits are bounded: with a short limit and a
-    tile whose look-back never sees its predecessors, the wait runs out, the
-    rest of the build and the traversal are skipped, and the next
+@pytest.fixture(params=[1, 0], ids=["single_launch_sort", "per_pass_sort"])
+def sort_mode(request):
+    """The radix sort as one cooperative launch (the default) and as one
+    launch per pass (physim_gpu_set_sort_single_launch)."""
+    import physim_gb300 as pg
+    pg.lib.physim_gpu_set_sort_single_launch(request.param)
+    try:
+        yield request.param
+    finally:
+        pg.lib.physim_gpu_set_sort_single_launch(1)
+
+
+@pytest.mark.parametrize("n", [40000, 1_600_000])
+def test_sort_modes_build_the_same_tree(n):
+    """Both ways of running the radix sort give the same keys, order and
+    tree and bit-identical accelerations: 5 tiles of 8,192 keys, and 196
+    tiles (more than one SM's block each, so blocks of the single launch sort
+    several tiles per pass)."""
+    import physim_gb300 as pg
+    from physim_gb300 import ics
+    s = ics.cube_with_stars(n, seed=41)
+    cfg = pg.SimConfig(gravity="astro2", theta=0.5, e=0.01, leaf_size=16, traversal="warp")
+    out = {}
+    try:
+        for mode in (1, 0):
+            pg.lib.physim_gpu_set_sort_single_launch(mode)
+            with pg.Simulation(s, cfg) as sim:
+                out[mode] = (sim.tree_snapshot(), _vec(sim.accelerations()))
+    finally:
+        pg.lib.physim_gpu_set_sort_single_launch(1)
+    (g1, a1), (g0, a0) = out[1], out[0]
+    for f in ("keys", "order", "begin", "count", "child", "nchild", "level"):
+        assert np.array_equal(g1[f], g0[f]), f
+    assert np.array_equal(a1, a0)
+
+
+def test_bounded_sort_wait_reports_timeout(oracle_mod, sort_mode):
+    """The radix sort's waits are bounded: with a short limit and a tile
+    whose look-back never sees its predecessors, the wait runs out (and, in
+    the single-launch sort, the grid barrier after that pass gives up at
+    once), the rest of the build and the traversal are skipped, and the next
     synchronising call returns PHYSIM_ERR_TIMEOUT instead of hanging; the
     library works normally after."""
     import time
