@@ -44,11 +44,32 @@ BYTES_PER_BODY_DIRECT = 200
 BYTES_PER_BODY_TREE = 700
 BYTES_FIXED = 4 << 20
 # Smallest direct-sum job that may evaluate each unordered pair once (the
-# lowest size threshold the ensemble autotuner picks), and the largest slot
-# buffer the library gives that plan (a quarter of a GB300's memory; above it
-# the library takes a one-pair plan, which has no slot buffer)
+# lowest size threshold the ensemble autotuner picks), and the largest partial
+# sum buffer the library gives that plan (a quarter of a GB300's memory; above
+# it the library takes a one-pair plan, which has no slot buffer)
 SYMMETRIC_FROM = 8192
 SYMMETRIC_CAP_BYTES = 288 * (1 << 30) // 4
+# The each-pair-once plan's f32 slot sums (csrc/direct_sym.cu,
+# direct_partial_doubles): one [3][n] slot per 1,024-body tile while those
+# stay within 4 GiB (one block per tile pair), else thread-block clusters of 8
+# I tiles over runs of 16 J tiles with [3][1,024] slots in a triangular layout
+SYM_TILE = 1024
+SYM_PAIRS_SLOT_BYTES = 4 << 30
+SYM_CLUSTER, SYM_RUN = 8, 16
+
+
+def symmetric_slot_bytes(n: int) -> int:
+    """Bytes of f32 slot sums the each-pair-once plan allocates for n bodies
+    (sym_slot_floats and make_symmetric_plan in csrc/direct_sym.cu)."""
+    t = -(-n // SYM_TILE)
+    if 12 * t * n <= SYM_PAIRS_SLOT_BYTES:
+        return 12 * t * n
+    runs = -(-t // SYM_RUN)
+    q, rem = divmod(t, SYM_RUN)
+    iside = t * runs - (SYM_RUN * q * (q - 1) // 2 + q * rem)
+    q, rem = divmod(t, SYM_CLUSTER)
+    jside = t + SYM_CLUSTER * q * (q - 1) // 2 + q * rem
+    return (iside + jside) * 3 * SYM_TILE * 4
 
 
 @dataclass(order=True)
@@ -67,13 +88,14 @@ class JobSpec:
 
     def device_bytes(self) -> int:
         per = BYTES_PER_BODY_DIRECT if self.gravity == "simple_astro" else BYTES_PER_BODY_TREE
+        slots = 0
         if self.gravity == "simple_astro" and self.n >= SYMMETRIC_FROM:
-            # evaluating each unordered pair once keeps an f32 slot sum per
-            # body for every 1,024-body tile, while that fits the library's cap
-            slots = 12 * ((self.n + 1023) // 1024)
-            if slots * self.n <= SYMMETRIC_CAP_BYTES:
-                per += slots
-        return BYTES_FIXED + per * self.n
+            # evaluating each unordered pair once adds the slot sums, while
+            # they and the f64 sums fit the library's cap
+            slots = symmetric_slot_bytes(self.n)
+            if 24 * self.n + slots > SYMMETRIC_CAP_BYTES:
+                slots = 0
+        return BYTES_FIXED + per * self.n + slots
 
     def step_seconds(self) -> float:
         """Rough device seconds per step on one GB300 (scheduling estimates

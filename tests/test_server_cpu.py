@@ -279,7 +279,8 @@ def test_async_admission(scheduling):
 
 def test_device_bytes_estimates():
     """Direct-sum jobs from the symmetric size up also hold one f32 slot sum
-    per 1,024-body tile and body; Barnes-Hut jobs hold the tree workspace."""
+    per 1,024-body tile and body (while those fit 4 GiB); Barnes-Hut jobs hold
+    the tree workspace."""
     from physim_gb300.server import BYTES_PER_BODY_TREE, SYMMETRIC_FROM
     small = job(0, SYMMETRIC_FROM - 1, 10)
     big = job(1, 32768, 10)
@@ -289,18 +290,34 @@ def test_device_bytes_estimates():
     assert tree.device_bytes() == BYTES_FIXED + BYTES_PER_BODY_TREE * tree.n
 
 
-def test_device_bytes_mirror_the_symmetric_cap():
-    """Above the library's cap on the slot buffer (a quarter of a GB300's
-    memory: about 2.4M bodies) direct sums take a one-pair plan, which keeps
-    no slot sums, so the estimate counts none."""
-    from physim_gb300.server import SYMMETRIC_CAP_BYTES
-    under = job(0, 2_000_000, 10)
-    over = job(1, 3_000_000, 10)
-    slots_under = 12 * ((under.n + 1023) // 1024)
-    assert slots_under * under.n <= SYMMETRIC_CAP_BYTES
-    assert under.device_bytes() == BYTES_FIXED + (BYTES_PER_BODY_DIRECT + slots_under) * under.n
-    assert 12 * ((over.n + 1023) // 1024) * over.n > SYMMETRIC_CAP_BYTES
+def test_device_bytes_mirror_the_symmetric_plan():
+    """Direct sums count the each-pair-once plan's slot sums as the library
+    allocates them: one [3][n] f32 slot per 1,024-body tile while those stay
+    within 4 GiB, the cluster schedule's triangular layout above (1,234,722,816
+    bytes at 1,048,580 bodies, the figure of the layout test), and none once the
+    f64 sums and slots pass the library's cap (a quarter of a GB300's memory:
+    above about 8.4M bodies), where a one-pair plan keeps no slot sums."""
+    from physim_gb300.server import (SYM_PAIRS_SLOT_BYTES, SYMMETRIC_CAP_BYTES,
+                                     symmetric_slot_bytes)
+    pairs = job(0, 500_000, 10)
+    t = -(-pairs.n // 1024)
+    assert 12 * t * pairs.n <= SYM_PAIRS_SLOT_BYTES
+    assert pairs.device_bytes() == BYTES_FIXED + (BYTES_PER_BODY_DIRECT + 12 * t) * pairs.n
+    million = job(1, 1_048_580, 10)
+    assert symmetric_slot_bytes(million.n) == 1_234_722_816
+    assert million.device_bytes() == (BYTES_FIXED + BYTES_PER_BODY_DIRECT * million.n
+                                      + 1_234_722_816)
+    three = job(2, 3_000_000, 10)  # a cluster plan: counted
+    slots3 = symmetric_slot_bytes(three.n)
+    assert 24 * three.n + slots3 <= SYMMETRIC_CAP_BYTES
+    assert three.device_bytes() == BYTES_FIXED + BYTES_PER_BODY_DIRECT * three.n + slots3
+    over = job(3, 9_000_000, 10)
+    assert 24 * over.n + symmetric_slot_bytes(over.n) > SYMMETRIC_CAP_BYTES
     assert over.device_bytes() == BYTES_FIXED + BYTES_PER_BODY_DIRECT * over.n
+    # the slot count grows with the square of the tiles in the cluster layout
+    # (3 T^2 / 32 slots), linearly in T per body below the 4 GiB bound
+    t3 = -(-three.n // 1024)
+    assert abs(slots3 / (3 * t3 * t3 / 32 * 3 * 1024 * 4) - 1) < 0.02
 
 
 def test_async_admission_cutoff_while_building():
