@@ -637,7 +637,19 @@ __device__ __forceinline__ int next_key_change(const uint64_t *__restrict__ keys
 // per-block counts of every level (blk_cnt[l * nblk + block]) and the body
 // count of the leaf starting at each body (the deepest run it starts; 0: no
 // node starts here, kLongLeaf: longer than the shared tile reaches); also
-// zeroes the child counters.
+// zeroes the child counters.  The questions about L near a body (the minimum
+// over the next `leaf` boundaries; how many consecutive boundaries either side,
+// or after the body, are at or below a level) are answered from tables of
+// window minima over 1, 2, 4, ..., 64 boundaries of the block's tile: the
+// minimum over any window of up to 64 from two overlapping entries, a run
+// length by binary lifting (the longest run is the sum of the powers of two
+// whose windows, taken largest first, stay at or below the level), so every
+// body takes the same few steps instead of a loop of data-dependent length.
+constexpr int kTreeTile = kTreeBlock + 2 * kTreeHalo;
+constexpr int kMinTables = 7;  // windows of 2^0 .. 2^6 boundaries
+static_assert(kMaxLeaf <= (1 << (kMinTables - 1)) && kMaxLeaf + 1 < kTreeHalo,
+              "leaf windows fit the tables and the halo");
+
 __global__ void __launch_bounds__(kTreeBlock)
 mask_kernel(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ lcp, int n,
             int nchild, int leaf, uint32_t *__restrict__ mask, uint32_t *__restrict__ blk_cnt,
@@ -645,7 +657,9 @@ mask_kernel(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ lcp, 
             const uint32_t *__restrict__ flags)
 {
     if (sort_failed(flags)) return;
-    __shared__ int8_t sL[kTreeBlock + 2 * kTreeHalo];
+    // sM[p][t]: minimum of L over boundaries t .. t + 2^p - 1 of the tile
+    // (clipped at the tile's end; every query below stays inside it)
+    __shared__ int8_t sM[kMinTables][kTreeTile];
     __shared__ uint32_t cnt[32];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cap; k += gridDim.x * blockDim.x)
         nchild32[k] = 0u;
@@ -653,32 +667,41 @@ mask_kernel(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ lcp, 
     const int base = blockIdx.x * kTreeBlock;
     // boundaries base - halo .. base + block + halo; -1 marks "no boundary
     // beyond here" (index 0 starts every run, indices >= n end them)
-    for (int t = threadIdx.x; t < kTreeBlock + 2 * kTreeHalo; t += blockDim.x) {
+    for (int t = threadIdx.x; t < kTreeTile; t += blockDim.x) {
         const int j = base - kTreeHalo + t;
-        sL[t] = (j >= 1 && j < n) ? (int8_t)lcp[j] : (int8_t)-1;
+        sM[0][t] = (j >= 1 && j < n) ? (int8_t)lcp[j] : (int8_t)-1;
     }
     if (threadIdx.x < 32) cnt[threadIdx.x] = 0u;
     __syncthreads();
+    for (int q = 1; q < kMinTables; ++q) {
+        const int h = 1 << (q - 1);
+        for (int t = threadIdx.x; t < kTreeTile; t += blockDim.x) {
+            const int a = sM[q - 1][t];
+            sM[q][t] = (int8_t)(t + h < kTreeTile ? min(a, (int)sM[q - 1][t + h]) : a);
+        }
+        __syncthreads();
+    }
+    const int8_t *sL = sM[0];
     const int i = base + threadIdx.x;
     uint32_t m = 0u;
     if (i < n) {
-        const int s = threadIdx.x + kTreeHalo;  // i's slot in sL
+        const int s = threadIdx.x + kTreeHalo;  // i's slot in the tile
         const int Li = i == 0 ? -1 : sL[s];
         // m(i): min of L over the next leaf boundaries, -1 if fewer remain
         int mi = -1;
         if (i + leaf <= n - 1) {
-            mi = D;
-            for (int q = 1; q <= leaf; ++q) mi = min(mi, (int)sL[s + q]);
+            const int q = 31 - __clz(leaf);
+            mi = min((int)sM[q][s + 1], (int)sM[q][s + leaf + 1 - (1 << q)]);
         }
         // u(i): the next body with another key; L(u(i)), -1 if none
         int Lu = -1;
         {
             int j = i + 1, t = s + 1;
-            while (j < n && t < kTreeBlock + 2 * kTreeHalo && sL[t] == D) {
+            while (j < n && t < kTreeTile && sL[t] == D) {
                 ++j;
                 ++t;
             }
-            if (j < n && t >= kTreeBlock + 2 * kTreeHalo) j = next_key_change(keys, i, j, n);
+            if (j < n && t >= kTreeTile) j = next_key_change(keys, i, j, n);
             if (j < n) Lu = lcp[j];
         }
         const int c = min(min(mi, Lu), D - 1);
@@ -687,9 +710,15 @@ mask_kernel(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ lcp, 
             for (int l = 1; l <= c + 1; ++l) m |= 1u << l;
         } else if (Li < D) {
             // the run at level Li containing i - 1 and i: more than leaf bodies?
+            // (lft, rgt: consecutive boundaries at or below Li before and
+            // after i, up to leaf each)
             int lft = 0, rgt = 0;
-            for (int q = 1; q <= leaf && sL[s - q] >= Li; ++q) ++lft;
-            for (int q = 1; q <= leaf && sL[s + q] >= Li; ++q) ++rgt;
+#pragma unroll
+            for (int q = kMinTables - 1; q >= 0; --q) {
+                const int k = 1 << q;
+                if (lft + k <= leaf && sM[q][s - lft - k] >= Li) lft += k;
+                if (rgt + k <= leaf && sM[q][s + rgt + 1] >= Li) rgt += k;
+            }
             if (lft + rgt + 2 > leaf) {
                 m |= 1u << (Li + 1);
                 for (int l = Li + 2; l <= c + 1; ++l) m |= 1u << l;
@@ -701,20 +730,27 @@ mask_kernel(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ lcp, 
         uint8_t lc = 0;
         if (m != 0u) {
             const int lf = 31 - __clz(m);
-            int t = s + 1, e = i + 1;
-            while (e < n && t < kTreeBlock + 2 * kTreeHalo && sL[t] >= lf) {
-                ++e;
-                ++t;
+            const int room = kTreeTile - 1 - s;  // boundaries after i in the tile
+            int run = 0;
+            while (run + 64 <= room && sM[6][s + 1 + run] >= lf) run += 64;
+#pragma unroll
+            for (int q = kMinTables - 2; q >= 0; --q) {
+                const int k = 1 << q;
+                if (run + k <= room && sM[q][s + 1 + run] >= lf) run += k;
             }
-            lc = (e < n && t >= kTreeBlock + 2 * kTreeHalo) || e - i >= (int)kLongLeaf
-                     ? kLongLeaf
-                     : (uint8_t)(e - i);
+            const int e = i + 1 + run, t = s + 1 + run;
+            lc = (e < n && t >= kTreeTile) || e - i >= (int)kLongLeaf ? kLongLeaf
+                                                                      : (uint8_t)(e - i);
         }
         leafcnt[i] = lc;
     }
-    for (int l = 0; l <= D; ++l) {
+    // per-level counts: only the levels some lane of the warp starts
+    uint32_t present = __reduce_or_sync(0xffffffffu, m);
+    while (present) {
+        const int l = __ffs(present) - 1;
+        present &= present - 1u;
         const uint32_t b = __ballot_sync(0xffffffffu, (m >> l) & 1u);
-        if ((threadIdx.x & 31) == 0 && b) atomicAdd(&cnt[l], (uint32_t)__popc(b));
+        if ((threadIdx.x & 31) == 0) atomicAdd(&cnt[l], (uint32_t)__popc(b));
     }
     __syncthreads();
     if (threadIdx.x < 32) blk_cnt[(size_t)threadIdx.x * nblk + blockIdx.x] = cnt[threadIdx.x];

@@ -64,7 +64,7 @@ def _sim(state, gravity, leaf, theta=0.5, e=0.01, traversal="exact"):
 
 @pytest.mark.parametrize("name", ["cube", "plummer", "edges"])
 @pytest.mark.parametrize("gravity,nchild", [("astro2", 8), ("astro", 4)])
-@pytest.mark.parametrize("leaf", [1, 16])
+@pytest.mark.parametrize("leaf", [1, 5, 16, 64])
 def test_tree_bit_exact_vs_model(oracle_mod, name, gravity, nchild, leaf):
     s = states()[name]
     with _sim(s, gravity, leaf) as sim:
