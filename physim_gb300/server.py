@@ -45,10 +45,10 @@ BYTES_PER_BODY_TREE = 700
 BYTES_FIXED = 4 << 20
 # Smallest direct-sum job that may evaluate each unordered pair once (the
 # lowest size threshold the ensemble autotuner picks), and the largest partial
-# sum buffer the library gives that plan (a quarter of a GB300's memory; above
-# it the library takes a one-pair plan, which has no slot buffer)
+# sum buffer the library gives that plan (a quarter of a GB300's 284,208 MiB;
+# above it the library takes a one-pair plan, which has no slot buffer)
 SYMMETRIC_FROM = 8192
-SYMMETRIC_CAP_BYTES = 288 * (1 << 30) // 4
+SYMMETRIC_CAP_BYTES = 284_208 * (1 << 20) // 4
 # The each-pair-once plan's f32 slot sums (csrc/direct_sym.cu,
 # direct_partial_doubles): one [3][n] slot per 1,024-body tile while those
 # stay within 4 GiB (one block per tile pair), else thread-block clusters of 8

@@ -296,7 +296,7 @@ def test_device_bytes_mirror_the_symmetric_plan():
     within 4 GiB, the cluster schedule's triangular layout above (1,234,722,816
     bytes at 1,048,580 bodies, the figure of the layout test), and none once the
     f64 sums and slots pass the library's cap (a quarter of a GB300's memory:
-    above about 8.4M bodies), where a one-pair plan keeps no slot sums."""
+    above about 8.2M bodies), where a one-pair plan keeps no slot sums."""
     from physim_gb300.server import (SYM_PAIRS_SLOT_BYTES, SYMMETRIC_CAP_BYTES,
                                      symmetric_slot_bytes)
     pairs = job(0, 500_000, 10)
