@@ -389,9 +389,10 @@ int physim_gpu_set_symmetric_cap(uint64_t bytes);
  * is made.  No reference counterpart (simple_astro, transformers.rs:219-244,
  * has no plans). */
 int physim_gpu_set_symmetric_pairs_limit(uint64_t bytes);
-/* Barnes-Hut builds wait on other thread blocks only in the radix sort's
- * decoupled look-back; every such wait gives up after `polls` polls that saw
- * no progress (0 restores the default, 2^20), raising an error flag: later
+/* Barnes-Hut builds wait on other thread blocks only in the radix sort: its
+ * decoupled look-back and, when its passes run as one launch, the barrier
+ * between passes.  Every such wait gives up after `polls` polls that saw no
+ * progress (0 restores the default, 2^20), raising an error flag: later
  * kernels of the build and the traversal then return at once and the next
  * synchronising call (physim_gpu_sim_synchronize / _download, the transform)
  * reports PHYSIM_ERR_TIMEOUT.  Process-wide, read when a build is enqueued or
