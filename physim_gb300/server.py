@@ -44,26 +44,35 @@ BYTES_PER_BODY_DIRECT = 200
 BYTES_PER_BODY_TREE = 700
 BYTES_FIXED = 4 << 20
 # Smallest direct-sum job that may evaluate each unordered pair once (the
-# lowest size threshold the ensemble autotuner picks), and the largest partial
-# sum buffer the library gives that plan (a quarter of a GB300's 284,208 MiB;
-# above it the library takes a one-pair plan, which has no slot buffer)
+# lowest size threshold the ensemble autotuner picks), and the largest slot
+# buffer the library gives that evaluation (a quarter of a GB300's 284,208
+# MiB; above it the library takes one-pair kernels, which keep no slot sums)
 SYMMETRIC_FROM = 8192
 SYMMETRIC_CAP_BYTES = 284_208 * (1 << 20) // 4
-# The each-pair-once plan's f32 slot sums (csrc/direct_sym.cu,
-# direct_partial_doubles): one [3][n] slot per 1,024-body tile while those
-# stay within 4 GiB (one block per tile pair), else thread-block clusters of 8
-# I tiles over runs of 16 J tiles with [3][1,024] slots in a triangular layout
+# The slot sums, by where a direct-sum job runs:
+#   * in an ensemble (GpuExecutor): one [3][n] f32 slot per 1,024-body tile
+#     for each member from the threshold up (csrc/ensemble.cu, plan_ensemble);
+#   * as its own simulation (PlainExecutor): the same while those stay within
+#     4 GiB (one block per tile pair), else thread-block clusters of 8 I tiles
+#     over runs of 16 J tiles with [3][1,024] slots in a triangular layout
+#     (csrc/direct_sym.cu, make_symmetric_plan and direct_partial_doubles)
 SYM_TILE = 1024
 SYM_PAIRS_SLOT_BYTES = 4 << 30
 SYM_CLUSTER, SYM_RUN = 8, 16
 
 
+def tile_slot_bytes(n: int) -> int:
+    """Slot bytes of one [3][n] f32 slot per 1,024-body tile."""
+    return 12 * (-(-n // SYM_TILE)) * n
+
+
 def symmetric_slot_bytes(n: int) -> int:
-    """Bytes of f32 slot sums the each-pair-once plan allocates for n bodies
-    (sym_slot_floats and make_symmetric_plan in csrc/direct_sym.cu)."""
+    """Bytes of f32 slot sums a simulation's each-pair-once plan allocates
+    for n bodies (sym_slot_floats and make_symmetric_plan in
+    csrc/direct_sym.cu)."""
     t = -(-n // SYM_TILE)
-    if 12 * t * n <= SYM_PAIRS_SLOT_BYTES:
-        return 12 * t * n
+    if tile_slot_bytes(n) <= SYM_PAIRS_SLOT_BYTES:
+        return tile_slot_bytes(n)
     runs = -(-t // SYM_RUN)
     q, rem = divmod(t, SYM_RUN)
     iside = t * runs - (SYM_RUN * q * (q - 1) // 2 + q * rem)
@@ -86,15 +95,23 @@ class JobSpec:
     seed: int = field(default=0, compare=False)
     leaf_size: int = field(default=16, compare=False)
 
-    def device_bytes(self) -> int:
+    def device_bytes(self, runs_as: str = "ensemble") -> int:
+        """Device bytes the job holds while it runs: in an ensemble (how
+        GpuExecutor runs direct sums) or as its own simulation
+        (`runs_as="simulation"`, PlainExecutor and Barnes-Hut jobs)."""
         per = BYTES_PER_BODY_DIRECT if self.gravity == "simple_astro" else BYTES_PER_BODY_TREE
         slots = 0
         if self.gravity == "simple_astro" and self.n >= SYMMETRIC_FROM:
             # evaluating each unordered pair once adds the slot sums, while
-            # they and the f64 sums fit the library's cap
-            slots = symmetric_slot_bytes(self.n)
-            if 24 * self.n + slots > SYMMETRIC_CAP_BYTES:
-                slots = 0
+            # they fit the library's cap
+            if runs_as == "simulation":
+                slots = symmetric_slot_bytes(self.n)
+                if 24 * self.n + slots > SYMMETRIC_CAP_BYTES:
+                    slots = 0
+            else:
+                slots = tile_slot_bytes(self.n)
+                if slots > SYMMETRIC_CAP_BYTES:
+                    slots = 0
         return BYTES_FIXED + per * self.n + slots
 
     def step_seconds(self) -> float:
@@ -205,6 +222,10 @@ class Unit:
 class Executor:
     def make_units(self, jobs: list[JobSpec]) -> list[Unit]: ...
 
+    def job_bytes(self, job: JobSpec) -> int:
+        """Device bytes `job` holds in this executor's units (admission)."""
+        return job.device_bytes()
+
     def unit_cost(self, job: JobSpec) -> int:
         """Units a job adds when admitted (0: it joins an existing unit)."""
         return 1
@@ -283,6 +304,9 @@ class PlainExecutor(Executor):
 
     def make_units(self, jobs: list[JobSpec]) -> list[Unit]:
         return [_SimUnit(j, self) for j in jobs]
+
+    def job_bytes(self, job: JobSpec) -> int:
+        return job.device_bytes("simulation")
 
 
 class _CudaTick:
@@ -531,6 +555,8 @@ class Server:
                          if async_admission else None)
         self._building: list[tuple[concurrent.futures.Future, list[JobSpec], int]] = []
         self.executor = executor
+        # device bytes of a job in this executor's units (admission and release)
+        self._job_bytes = getattr(executor, "job_bytes", None) or (lambda j: j.device_bytes())
         self.max_batch = max_batch
         self.keep_states = keep_states
         self.budget = hbm_budget
@@ -560,7 +586,7 @@ class Server:
     def _admit(self, now: float) -> None:
         while self.arrivals and self.arrivals[0][0] <= now:
             j = heapq.heappop(self.arrivals)[2]
-            if j.device_bytes() > self.budget:
+            if self._job_bytes(j) > self.budget:
                 self.rejected.append(j)  # can never fit
             else:
                 self.pending.append(j)
@@ -578,7 +604,7 @@ class Server:
         cost = getattr(self.executor, "unit_cost", lambda job: 1)
         while self.pending:
             j = self.pending.popleft()
-            need = j.device_bytes()
+            need = self._job_bytes(j)
             c = cost(j)
             if (need <= room and len(self.units) + new_units + c <= self.max_units
                     and len(batch) < self.max_batch):
@@ -591,7 +617,7 @@ class Server:
         if batch:
             for j in batch:
                 self.admitted_at[j.id] = now
-                self.in_use += j.device_bytes()
+                self.in_use += self._job_bytes(j)
             if self._builder is not None:
                 cost_new = new_units - sum(c for _, _, c in self._building)
                 self._building.append((self._builder.submit(self.executor.make_units, batch),
@@ -611,7 +637,7 @@ class Server:
         t = self.clock() - self.t0
         for j in batch:
             self.failed.append(JobResult(j, self.admitted_at.get(j.id, t), t, None, repr(err)))
-            self.in_use -= j.device_bytes()
+            self.in_use -= self._job_bytes(j)
 
     def _collect_built(self) -> None:
         """Units whose building finished join the running set."""
@@ -638,7 +664,7 @@ class Server:
         for j in u.jobs:
             if j.id not in done_ids:
                 self.failed.append(JobResult(j, self.admitted_at.get(j.id, t), t, None, repr(err)))
-                self.in_use -= j.device_bytes()
+                self.in_use -= self._job_bytes(j)
         try:
             u.close()
         except Exception:
@@ -697,7 +723,7 @@ class Server:
                         t = self.clock() - self.t0
                         self.results.append(JobResult(j, self.admitted_at[j.id], t,
                                                       state if self.keep_states else None))
-                        self.in_use -= j.device_bytes()
+                        self.in_use -= self._job_bytes(j)
                         self.steps_done += j.steps
                 if u.alive():
                     still.append(u)

@@ -290,34 +290,65 @@ def test_device_bytes_estimates():
     assert tree.device_bytes() == BYTES_FIXED + BYTES_PER_BODY_TREE * tree.n
 
 
-def test_device_bytes_mirror_the_symmetric_plan():
-    """Direct sums count the each-pair-once plan's slot sums as the library
-    allocates them: one [3][n] f32 slot per 1,024-body tile while those stay
-    within 4 GiB, the cluster schedule's triangular layout above (1,234,722,816
-    bytes at 1,048,580 bodies, the figure of the layout test), and none once the
-    f64 sums and slots pass the library's cap (a quarter of a GB300's memory:
-    above about 8.2M bodies), where a one-pair plan keeps no slot sums."""
+def test_device_bytes_in_an_ensemble_mirror_plan_ensemble():
+    """GpuExecutor runs direct sums in ensembles, whose each-pair-once members
+    keep one [3][n] f32 slot per 1,024-body tile at any size
+    (csrc/ensemble.cu, plan_ensemble) while the slots fit the library's cap (a
+    quarter of a GB300's memory: up to about 2.4M bodies for one job)."""
+    from physim_gb300.server import SYMMETRIC_CAP_BYTES
+    for n in (500_000, 1_048_580, 2_000_000):
+        j = job(0, n, 10)
+        slots = 12 * -(-n // 1024) * n
+        assert slots <= SYMMETRIC_CAP_BYTES
+        assert j.device_bytes() == BYTES_FIXED + BYTES_PER_BODY_DIRECT * n + slots
+    over = job(1, 3_000_000, 10)
+    assert 12 * -(-over.n // 1024) * over.n > SYMMETRIC_CAP_BYTES
+    assert over.device_bytes() == BYTES_FIXED + BYTES_PER_BODY_DIRECT * over.n
+
+
+def test_device_bytes_as_a_simulation_mirror_the_symmetric_plan():
+    """A direct sum run as its own simulation (PlainExecutor) counts the slot
+    sums of the schedule the library picks: one [3][n] slot per tile while
+    those stay within 4 GiB, the cluster schedule's triangular layout above
+    (1,234,722,816 bytes at 1,048,580 bodies, the figure of the layout test),
+    and none once the f64 sums and slots pass the library's cap (above about
+    8.2M bodies), where a one-pair plan keeps no slot sums."""
     from physim_gb300.server import (SYM_PAIRS_SLOT_BYTES, SYMMETRIC_CAP_BYTES,
                                      symmetric_slot_bytes)
     pairs = job(0, 500_000, 10)
     t = -(-pairs.n // 1024)
     assert 12 * t * pairs.n <= SYM_PAIRS_SLOT_BYTES
-    assert pairs.device_bytes() == BYTES_FIXED + (BYTES_PER_BODY_DIRECT + 12 * t) * pairs.n
+    assert pairs.device_bytes("simulation") == (BYTES_FIXED
+                                                + (BYTES_PER_BODY_DIRECT + 12 * t) * pairs.n)
     million = job(1, 1_048_580, 10)
     assert symmetric_slot_bytes(million.n) == 1_234_722_816
-    assert million.device_bytes() == (BYTES_FIXED + BYTES_PER_BODY_DIRECT * million.n
-                                      + 1_234_722_816)
+    assert million.device_bytes("simulation") == (BYTES_FIXED + BYTES_PER_BODY_DIRECT * million.n
+                                                  + 1_234_722_816)
     three = job(2, 3_000_000, 10)  # a cluster plan: counted
     slots3 = symmetric_slot_bytes(three.n)
     assert 24 * three.n + slots3 <= SYMMETRIC_CAP_BYTES
-    assert three.device_bytes() == BYTES_FIXED + BYTES_PER_BODY_DIRECT * three.n + slots3
+    assert three.device_bytes("simulation") == (BYTES_FIXED + BYTES_PER_BODY_DIRECT * three.n
+                                                + slots3)
     over = job(3, 9_000_000, 10)
     assert 24 * over.n + symmetric_slot_bytes(over.n) > SYMMETRIC_CAP_BYTES
-    assert over.device_bytes() == BYTES_FIXED + BYTES_PER_BODY_DIRECT * over.n
+    assert over.device_bytes("simulation") == BYTES_FIXED + BYTES_PER_BODY_DIRECT * over.n
     # the slot count grows with the square of the tiles in the cluster layout
     # (3 T^2 / 32 slots), linearly in T per body below the 4 GiB bound
     t3 = -(-three.n // 1024)
     assert abs(slots3 / (3 * t3 * t3 / 32 * 3 * 1024 * 4) - 1) < 0.02
+
+
+def test_admission_uses_the_executors_estimate():
+    """The server admits and releases a job with the bytes of the executor
+    that runs it: ensembles for GpuExecutor, simulations for PlainExecutor
+    (constructing either touches no GPU)."""
+    from physim_gb300.server import GpuExecutor, PlainExecutor, Server
+    big = job(0, 1_048_580, 10)
+    assert GpuExecutor().job_bytes(big) == big.device_bytes()
+    assert PlainExecutor().job_bytes(big) == big.device_bytes("simulation")
+    assert big.device_bytes("simulation") < big.device_bytes()
+    assert Server(PlainExecutor())._job_bytes(big) == big.device_bytes("simulation")
+    assert Server(GpuExecutor())._job_bytes(big) == big.device_bytes()
 
 
 def test_async_admission_cutoff_while_building():
