@@ -133,6 +133,16 @@ def law_kats() -> dict:
                         "acc0": [float(v) for v in acc]}}
 
 
+def _zero_padding(a: np.ndarray) -> np.ndarray:
+    """The same records with zero struct padding (the oracle copies whole C
+    structs, whose padding bytes are unspecified), so that the fixture file
+    regenerates byte for byte."""
+    out = np.zeros(a.shape, a.dtype)
+    for name in a.dtype.names:
+        out[name] = a[name]
+    return out
+
+
 def oracle_fixtures(path: Path) -> None:
     import oracle
     from physim_gb300.entity import ACCELERATION, ENTITY  # noqa: F401 (dtype only)
@@ -143,8 +153,8 @@ def oracle_fixtures(path: Path) -> None:
     acc_direct = oracle.simple_astro(st, 0.01)
     acc_oct = oracle.barnes_hut(st, 0.5, 0.01, nchild=8)
     acc_quad = oracle.barnes_hut(st, 0.7, 0.01, nchild=4)
-    traj = oracle.run_pipeline(st, "simple_astro", 3, 1e-5, 0.01)
-    traj_bh = oracle.run_pipeline(st, "astro2", 3, 1e-5, 0.01, theta=1.0)
+    traj = _zero_padding(oracle.run_pipeline(st, "simple_astro", 3, 1e-5, 0.01))
+    traj_bh = _zero_padding(oracle.run_pipeline(st, "astro2", 3, 1e-5, 0.01, theta=1.0))
     np.savez_compressed(path, state=st.view(np.uint8), acc_direct=acc_direct.view(np.uint8),
                         acc_octree=acc_oct.view(np.uint8), acc_quadtree=acc_quad.view(np.uint8),
                         traj_direct=traj.view(np.uint8), traj_astro2=traj_bh.view(np.uint8))
